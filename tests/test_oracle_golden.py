@@ -1,0 +1,107 @@
+"""Pin the CPU oracle to the fixtures produced by running the reference itself."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import maxwellian, rel_linf
+from oracle import fs_inelastic as fo
+from oracle import integrators as it
+from oracle import transport as tr
+
+TOL = 1e-12  # FP64 restatement vs FP64 reference (FFT rounding only)
+
+
+def _op(params):
+    nv, nr, ns, e, e0, g, s = params
+    m = fo.Mesh(int(nv), s, int(nr), int(ns))
+    return m, fo.FSInelasticVHS(m, e, e0, g)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_operator_small(golden, case):
+    d = golden("op_small.npz")
+    m, op = _op(d[f"case{case}_params"])
+    f = d[f"case{case}_f"]
+    assert rel_linf(op.collide(f), d[f"case{case}_gain"]) < TOL
+    assert rel_linf(op.collide(f, with_loss=True), d[f"case{case}_full"]) < TOL
+    assert rel_linf(op(f, heat_bath=0.3), d[f"case{case}_heat"]) < TOL
+    assert rel_linf(op.collide(f[0]), d[f"case{case}_gain_cell0"]) < TOL
+
+
+def test_operator_c32_two_beam(golden):
+    d = golden("op_c32.npz")
+    m, op = _op(d["params"])
+    f = d["f"]
+    assert rel_linf(op.collide(f, with_loss=True), d["full"]) < TOL
+    assert rel_linf(op.collide(f), d["gain"]) < TOL
+
+
+def test_transport(golden):
+    d = golden("transport.npz")
+    v = d["v"]
+    for bc in ("extrap", "periodic"):
+        for j in range(2):
+            df = tr.df_advection(d[f"{bc}_f"], v, float(d[f"{bc}_dt{j}"]), float(d[f"{bc}_dx"]), bc, bc)
+            assert rel_linf(df, d[f"{bc}_df{j}"]) < TOL, (bc, j)
+
+
+@pytest.mark.parametrize("name,integ", [("pfe", "PFE"), ("pfe_full", "PFE"), ("tpi2", "TPI2"),
+                                        ("tpi3", "TPI3"), ("euler", "Euler")])
+def test_solver1d(golden, name, integ):
+    d = golden("solver1d.npz")
+    nv, nr, ns, e, e0, g, s, nx = d["params"]
+    m, op = _op((nv, nr, ns, e, e0, g, s))
+    dt, tend, kn, dx = d[f"{name}_meta"]
+    bc = "extrap" if name in ("pfe", "pfe_full", "euler") else "periodic"
+    with_loss = name.endswith("_full") or name == "tpi3"
+
+    def df(f, h):
+        return it.boltzmann_df(f, h, lambda x: op.collide(x, with_loss=with_loss), kn,
+                               lambda x, hh: tr.df_advection(x, m.v, hh, dx, bc, bc))
+
+    f = d[f"{name}_f0"].copy()
+    it.evolve(f, 0.0, tend, dt, df, integ, list(d[f"{name}_K"]), list(d[f"{name}_h"]))
+    assert rel_linf(f, d[f"{name}_f"]) < 1e-11
+
+
+def test_euler_history_c32(golden):
+    """First steps of the 100-step forward-Euler run (full run checked on the GPU)."""
+    d = golden("euler_c32.npz")
+    c = golden("op_c32.npz")
+    m, op = _op(c["params"])
+    f = c["f"].copy()
+    for k in range(3):
+        f += float(d["dt"]) * op.collide(f, with_loss=True)
+        mo = it.moments(f, m.v, m.delta)
+        assert abs(mo["T"] - d["T"][k + 1]) < 1e-12 * d["T"][k + 1]
+        assert abs(mo["rho"] - d["rho"][k + 1]) < 1e-12
+
+
+def test_cooling_law_maxwell_molecules():
+    """-dT/dt = (1 - e^2) rho T / 4 for Maxwell molecules (gamma = 0)."""
+    for e in (0.9, 0.5):
+        m = fo.Mesh(16, 16.0 / (3 + math.sqrt(2)), 8, 12)
+        op = fo.FSInelasticVHS(m, e, e, 0.0)
+        f = maxwellian(m.v, 1.0, (0.3, 0.0, 0.0), 1.0)
+        q = op.collide(f, with_loss=True)
+        V = np.meshgrid(m.v, m.v, m.v, indexing="ij")
+        dv = m.delta**3
+        rho = f.sum() * dv
+        u = np.array([(f * V[d]).sum() * dv / rho for d in range(3)])
+        E = 0.5 * (f * (V[0] ** 2 + V[1] ** 2 + V[2] ** 2)).sum() * dv
+        T = (2 / 3) * (E / rho - 0.5 * (u**2).sum())
+        dE = 0.5 * (q * (V[0] ** 2 + V[1] ** 2 + V[2] ** 2)).sum() * dv
+        dmom = np.array([(q * V[d]).sum() * dv for d in range(3)])
+        drho = q.sum() * dv
+        # dT/dt from dE, d(rho u), d rho (rho, u nearly conserved)
+        dT = (2 / 3) * (dE / rho - E * drho / rho**2 - (u * (dmom - u * drho)).sum() / rho)
+        k = -dT / (rho * T * (1 - e**2))
+        assert abs(k - 0.25) < 5e-3, (e, k)
+
+
+def test_mass_mode_correction():
+    q = np.random.default_rng(1).random((2, 8, 8, 8))
+    qc = fo.mass_mode_correction(q)
+    assert np.abs(qc.sum(axis=(1, 2, 3))).max() < 1e-12
+    assert rel_linf(qc - q, -q.mean(axis=(1, 2, 3), keepdims=True) + 0 * q) < 1e-14
