@@ -1,0 +1,142 @@
+/*
+ * pii_gb300.h -- C ABI of the GB300 (sm_103a) fast-spectral inelastic
+ * collision operator Q(f,f) and the projective / telescopic time steps that
+ * call it.
+ *
+ * Plain pointers and sizes only.  Every array argument named f, q, df, out is
+ * DEVICE memory (cudaMalloc'd or a torch CUDA tensor's data_ptr), row-major,
+ * FP64, layout (cells, n, n, n) with the last axis fastest; the first velocity
+ * axis is the advection speed v1 (the reference's f layout, src/state.py:64-69,
+ * src/solution.py:53-55).  Host arrays (quadrature nodes, integrator
+ * parameters) are plain C arrays read during the call.
+ *
+ * Ownership: the caller owns every array it passes; the library owns the plan,
+ * its device tables and its workspace (allocated once in pii_plan_create).
+ * Calls are stream-ordered on the given cudaStream_t (NULL = legacy default
+ * stream) and are not re-entrant for one plan: one plan, one stream at a time.
+ *
+ * Errors: every entry point returns PII_OK (0) or a negative status; the
+ * message of the last failure on the calling thread is pii_last_error().
+ * The Python wrapper raises ValueError / RuntimeError from these codes, the
+ * exceptions the reference raises (src/collision/inelastic_collisions.py:47,
+ * src/collision/spectral_mesh.py:23, src/solver.py:126-128).
+ */
+#ifndef PII_GB300_H
+#define PII_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PII_OK 0
+#define PII_ERR_ARG (-1)      /* invalid argument (ValueError in Python)   */
+#define PII_ERR_CUDA (-2)     /* CUDA runtime error                        */
+#define PII_ERR_SIZE (-3)     /* batch / size beyond the plan's capacity   */
+#define PII_ERR_NONFINITE (-4) /* NaN/Inf guard tripped on FP64 moments   */
+
+#define PII_PREC_FP32 0 /* FP32 FFTs and quadrature sums, FP64 state and islands */
+#define PII_PREC_FP64 1 /* everything in FP64 (the parity path)                  */
+
+#define PII_BC_EXTRAP 1   /* src/solver.py:8-9, BC.extrap   */
+#define PII_BC_PERIODIC 2 /* src/solver.py:8-10, BC.periodic */
+
+#define PII_INT_EULER 0 /* src/boltzmann.py:82-84   */
+#define PII_INT_PFE 1   /* src/boltzmann.py:120-128 */
+#define PII_INT_TPI2 2  /* src/boltzmann.py:130-140 */
+#define PII_INT_TPI3 3  /* src/boltzmann.py:142-158 */
+
+typedef struct pii_plan pii_plan;
+
+/* Message of the last error on this thread ("" if none). */
+const char* pii_last_error(void);
+
+/* Library version string. */
+const char* pii_version(void);
+
+/*
+ * Build an operator plan: quadrature, kernel tables and workspace for up to
+ * batch_max cells of n^3 velocity points.  Replaces the construction of
+ * FSInelasticVHSCollision(config, SpectralMesh(config))
+ * (src/collision/base.py:7-30, src/collision/inelastic_collisions.py:30-137,
+ * src/collision/spectral_mesh.py:8-66).
+ *   r, w_r       : n_r Gauss-Legendre nodes / weights on [0, R]
+ *   sigma        : n_sigma x 3 unit vectors (spherical design), w_sigma weight
+ *   L, R         : velocity half-width and collision radius (L = (3+sqrt2)S/2, R = 2S)
+ *   e, e0, gamma : restitution law e(r) = (e0-e)/2 tanh(r - R/2) + (e0+e)/2,
+ *                  VHS exponent (0 Maxwell molecules, 1 hard spheres)
+ * n must be one of 8, 16, 24, 32, 48, 64.
+ */
+int pii_plan_create(pii_plan** out, int n, int n_r, int n_sigma, const double* r, const double* w_r,
+                    const double* sigma, double w_sigma, double L, double R, double e, double e0,
+                    double gamma, int precision, int64_t batch_max, int device);
+
+/* Free the plan, its tables and workspace (no reference counterpart: the
+ * reference's numpy/cupy arrays are garbage collected). */
+int pii_plan_destroy(pii_plan* plan);
+
+/* Bytes of device memory the plan holds. */
+int64_t pii_plan_workspace_bytes(const pii_plan* plan);
+
+/*
+ * q = Q+(f,f) [- Q-(f,f) if with_loss] [+ heat_bath * Lap_v f], per cell.
+ * Replaces BaseCollision.__call__ (src/collision/base.py:32-58) and
+ * FSInelasticVHSCollision.collide / laplacian
+ * (src/collision/inelastic_collisions.py:208-230).  f and q: cells x n^3 FP64
+ * device arrays (may not alias).  mass_fix != 0 subtracts the per-cell mean of
+ * q in FP64 (the k = 0 mass-mode correction; not in the reference).
+ */
+int pii_collide(pii_plan* plan, const double* f, double* q, int64_t cells, int with_loss,
+                double heat_bath, int mass_fix, void* stream);
+
+/*
+ * Transport increment of the second-order upwind + minmod TVD scheme in x,
+ * df = -dt/dx (A-dq + A+dq) - dt/dx (F_{i+1/2} - F_{i-1/2}), two ghost cells.
+ * Replaces BoltzmannSolver1D.df_advection (src/boltzmann.py:177-205) with the
+ * ghost fill of Solver._apply_bcs (src/solver.py:59-105), advection_1D
+ * (src/riemann/advection_1D.py:4-21) and tvd.limit / minmod
+ * (src/limiters/tvd.py:6-40).  v1: n first-axis velocity centres (host).
+ */
+int pii_transport_df(pii_plan* plan, const double* f, double* df, int64_t nx, double dt, double dx,
+                     const double* v1, int bc_lower, int bc_upper, void* stream);
+
+/*
+ * df = transport(f, dt) + dt * Q(f) / kn   (nx == 0: homogeneous, no transport).
+ * Replaces BoltzmannSolver.df (src/boltzmann.py:160-164).
+ */
+int pii_boltzmann_df(pii_plan* plan, const double* f, double* df, int64_t nx, double dt, double dx,
+                     const double* v1, int bc_lower, int bc_upper, double kn, int with_loss,
+                     int mass_fix, void* stream);
+
+/*
+ * One macro-step of size dt of the chosen integrator, updating f in place
+ * (FP64).  Replaces BoltzmannSolver.step and its euler_step /
+ * proj_euler_step / tel_proj_step2 / tel_proj_step3 (src/boltzmann.py:46-158).
+ * inner_steps / inner_dt: host arrays of length levels (1 for PFE, 2 for
+ * TPI2, 3 for TPI3; ignored for Euler).  use_graph != 0 captures the whole
+ * macro-step into a CUDA graph on first use and replays it on later calls
+ * with the same arguments.
+ */
+int pii_step(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, const int* inner_steps,
+             const double* inner_dt, int levels, double dx, const double* v1, int bc_lower, int bc_upper,
+             double kn, int with_loss, int mass_fix, int use_graph, void* stream);
+
+/*
+ * FP64 moments per cell: out[c*5 + {0,1,2,3,4}] = sum f, sum f v1, sum f v2,
+ * sum f v3, sum f |v|^2 / 2, each times delta^3 (3D-velocity form of
+ * State.rho / u / T, src/state.py:31-52,91-92).  v: n velocity centres (host).
+ * out is a device array of cells*5 doubles.
+ */
+int pii_moments(pii_plan* plan, const double* f, double* out, int64_t cells, const double* v, double delta,
+                void* stream);
+
+/* f[i] += a * (b * d[i]) for i < count, FP64 (the projective extrapolation
+ * f += M_l * df_l, src/boltzmann.py:128,138-140,154-158). */
+int pii_axpby(double* f, const double* d, double a, double b, int64_t count, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PII_GB300_H */

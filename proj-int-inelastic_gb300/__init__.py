@@ -1,0 +1,16 @@
+"""GB300-native fast-spectral inelastic collision operator and projective steps.
+
+Drop-in for the hot path of Mayuyu/proj-int-inelastic: the operator classes of
+``src/collision`` and the step interface of ``src/solver.py`` /
+``src/boltzmann.py`` / ``src/iter_solver.py``, evaluated by hand-written
+sm_103a CUDA kernels in ``libpii_gb300.so`` (C ABI: ``include/pii_gb300.h``).
+"""
+from . import _lib
+from .collision import FSInelasticVHSCollision, Plan, SpectralMesh, get_sphrquadrule
+from .solver import (BC, BoltzmannSolver, BoltzmannSolver0D, BoltzmannSolver1D, IterativeBoltzmannSolver,
+                     Solution, Solver, State)
+
+__all__ = [
+    "BC", "BoltzmannSolver", "BoltzmannSolver0D", "BoltzmannSolver1D", "FSInelasticVHSCollision",
+    "IterativeBoltzmannSolver", "Plan", "Solution", "Solver", "SpectralMesh", "State", "get_sphrquadrule",
+]

@@ -1,0 +1,327 @@
+"""Drop-in GB300 collision operator with the reference's call signatures.
+
+* ``SpectralMesh(config)`` -- velocity mesh and quadratures
+  (src/collision/spectral_mesh.py:8-132);
+* ``FSInelasticVHSCollision(config, spectral_mesh)`` -- the fast
+  Fourier-spectral inelastic VHS operator with ``__call__(input_f,
+  heat_bath=None, device=...)``, ``collide(input_f, with_loss=False)`` and
+  ``laplacian(input_f)`` (src/collision/base.py:7-58,
+  src/collision/inelastic_collisions.py:116-230).
+
+Both take the reference's nested-dict config (``config["velocity-mesh"]["nv"]``
+...).  The operator evaluates on the GPU through ``libpii_gb300.so``; it
+accepts NumPy arrays (returned as NumPy, as the reference returns) or torch
+CUDA tensors (returned as torch CUDA tensors, no host copy).  There is no CPU
+path: ``device`` is accepted for signature compatibility only.
+"""
+import math
+import os
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_DESIGNS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "sphere_designs.npz")
+
+
+def get_sphrquadrule(sstype, rule=None, npts=None, qdeg=None):
+    """Symmetric spherical design by point count or strength.
+
+    Mirrors ``get_sphrquadrule`` (src/collision/spherical_design/__init__.py:91-116)
+    for the stored Womersley symmetric designs: select by ``npts`` (exact) or
+    the smallest design with strength >= ``qdeg``.  ``rule`` may also be an
+    (m, 3) array of unit vectors (a tabulated rule).
+    """
+    if sstype != "symmetric":
+        raise ValueError(f"unknown spherical design type {sstype!r}")
+    if rule is not None and not isinstance(rule, str):
+        pts = np.asarray(rule, np.float64).reshape(-1, 3)
+        if npts and npts != len(pts):
+            raise ValueError("Invalid number of points in provided rule")
+        return pts
+    if rule not in (None, "womersley"):
+        raise ValueError("No suitable spherical quadrature rule found")
+    if not npts and not qdeg:
+        raise ValueError("Must specify either npts or qdeg")
+    d = np.load(_DESIGNS)
+    best = None
+    for key in d.files:
+        if not key.startswith("m"):
+            continue
+        m = int(key[1:])
+        q = int(d[f"qdeg_{key}"])
+        if (not npts or npts == m) and (not qdeg or qdeg <= q):
+            if best is None or (npts and q > best[2]) or (qdeg and m < best[1]):
+                best = (key, m, q)
+    if best is None:
+        raise ValueError("No suitable spherical quadrature rule found")
+    return d[best[0]].copy()
+
+
+class SpectralMesh:
+    """Velocity mesh and quadratures (src/collision/spectral_mesh.py:8-132)."""
+
+    def __init__(self, config, *args, **kwargs):
+        self.config = config
+        vm = config["velocity-mesh"]
+        self._nv = int(vm["nv"])
+        self._nr = int(vm.get("nr", int(self._nv / 2)))
+        self._S = float(vm["s"])
+        self._R = 2 * self._S
+        self._L = 0.5 * (3.0 + math.sqrt(2)) * self._S
+        quad_rule = vm.get("quad-rule", "legendre")
+        if quad_rule != "legendre":
+            raise KeyError(quad_rule)
+        x, w = np.polynomial.legendre.leggauss(self._nr)
+        self._r = 0.5 * (x + 1) * self._R
+        self._wr = 0.5 * self._R * w
+        self._ndim = int(config["collision-model"]["dim"])
+        if self._ndim == 2:
+            raise NotImplementedError("the GB300 operator implements the 3D-velocity model only")
+        if self._ndim != 3:
+            raise ValueError("Dimension must be 2 or 3.")
+        sp = config["spherical-design-rule"]
+        self._ssrule = sp.get("ssrule", "womersley")
+        self._nsphr = int(sp["nsphr"])
+        self._spts = get_sphrquadrule("symmetric", rule=sp.get("points", self._ssrule), npts=self._nsphr)
+        self._wspts = 4 * math.pi / self._nsphr
+        self._v_center = None
+        self._v_centers = None
+
+    @property
+    def v_center(self):
+        if self._v_center is None:
+            self._v_center = np.array([-self.L + (i + 0.5) * self.delta for i in range(self.nv)])
+        return self._v_center
+
+    @property
+    def v_centers(self):
+        if self._v_centers is None:
+            index = np.indices(self.nv_s)
+            self._v_centers = [self.v_center[index[i, ...]] for i in range(self.ndim)]
+        return self._v_centers
+
+    @property
+    def ncirc_or_nsphr(self):
+        return self._nsphr
+
+    def circ_or_sphr_quad(self):
+        return self._spts, self._wspts
+
+    @property
+    def ndim(self):
+        return self._ndim
+
+    @property
+    def nv(self):
+        return self._nv
+
+    @property
+    def nv_s(self):
+        return [self.nv] * self.ndim
+
+    @property
+    def L(self):
+        return self._L
+
+    @property
+    def R(self):
+        return self._R
+
+    @property
+    def delta(self):
+        return 2 * self.L / self.nv
+
+    @property
+    def nr(self):
+        return self._nr
+
+    def rquad(self):
+        return self._r, self._wr
+
+
+def _precision_of(config, precision):
+    if precision is None:
+        precision = str(config.get("config", {}).get("precision", "mixed")).lower()
+    if precision in ("double", "fp64", "float64"):
+        return _lib.PREC_FP64
+    if precision in ("mixed", "single", "fp32", "float32"):
+        return _lib.PREC_FP32
+    raise ValueError(f"precision must be 'mixed'/'fp32' or 'double'/'fp64', got {precision!r}")
+
+
+class Plan:
+    """Owner of one ``pii_plan`` (device tables + workspace for batch_max cells)."""
+
+    def __init__(self, mesh, e, e0, gamma, precision, batch_max, device):
+        lib = _lib.load()
+        self.n = mesh.nv
+        self.batch_max = int(batch_max)
+        self.device = int(device)
+        self.precision = precision
+        r, wr = mesh.rquad()
+        sigma, wsigma = mesh.circ_or_sphr_quad()
+        self._r = np.ascontiguousarray(r, np.float64)
+        self._wr = np.ascontiguousarray(wr, np.float64)
+        self._sigma = np.ascontiguousarray(sigma, np.float64)
+        h = _lib._vp()
+        torch.cuda.init()
+        st = lib.pii_plan_create(
+            _lib.ctypes.byref(h), int(mesh.nv), int(len(self._r)), int(len(self._sigma)), _lib.dptr(self._r),
+            _lib.dptr(self._wr), _lib.dptr(self._sigma), float(wsigma), float(mesh.L), float(mesh.R), float(e),
+            float(e0), float(gamma), int(precision), self.batch_max, self.device)
+        _lib.check(st, "pii_plan_create")
+        self.handle = h.value
+        self._lib = lib
+
+    @property
+    def workspace_bytes(self):
+        return int(self._lib.pii_plan_workspace_bytes(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.pii_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _stream_handle():
+    return torch.cuda.current_stream().cuda_stream
+
+
+class FSInelasticVHSCollision:
+    """GB300 fast-spectral inelastic VHS collision operator.
+
+    Same constructor and methods as the reference class
+    (src/collision/inelastic_collisions.py:116-230, src/collision/base.py:6-58).
+    Extra keyword arguments (not in the reference):
+
+    * ``precision``  -- "mixed" (FP32 FFTs and quadrature sums, the default) or
+      "double" (all FP64); also read from ``config["config"]["precision"]``;
+    * ``with_loss``  -- what ``__call__`` evaluates: the reference's ``__call__``
+      never passes ``with_loss``, so it returns the gain term only (default
+      False, kept); True returns Q+ - Q-;
+    * ``mass_fix``   -- subtract the per-cell mean of Q in FP64 (k = 0 mode);
+    * ``batch_max``  -- initial cell capacity of the plan (grown on demand);
+    * ``device``     -- CUDA device index.
+    """
+
+    collision_model = "vhs"
+
+    def __init__(self, config, spectral_mesh, precision=None, with_loss=False, mass_fix=False, batch_max=1,
+                 device=0, **kwargs):
+        self.config = config
+        self.sm = spectral_mesh
+        self.ndim = int(config["collision-model"]["dim"])
+        assert self.ndim == self.sm.ndim, (
+            "'spectral_mesh' has different velocity dimensions from collision model! This may be caused by "
+            "using different config files. Please check the consistency.")
+        self.load_parameters()
+        self._precision = _precision_of(config, precision)
+        self.default_with_loss = bool(with_loss)
+        self.mass_fix = bool(mass_fix)
+        self._device = int(device)
+        self._plan = None
+        self._batch_max = max(1, int(batch_max))
+        self._pinned = {}
+        self._input_shape = None
+
+    # -- reference hooks -------------------------------------------------
+    def load_parameters(self):
+        """``load_parameters`` (src/collision/inelastic_collisions.py:30-52)."""
+        cm = self.config["collision-model"]
+        self._e = float(cm.get("e", 1.0))
+        self._e0 = float(cm.get("e0", 1.0))
+        self._gamma = float(cm.get("gamma", 0.0))
+        if self.ndim != 3:
+            raise ValueError("Dimension must be 2 or 3.")
+        self._sphr_fac = 2 * math.pi ** (0.5 * self.ndim) / math.gamma(0.5 * self.ndim)
+
+    def perform_precomputation(self):
+        """Tables are built on the device by the plan (``pii_plan_create``)."""
+        self._ensure_plan(self._batch_max)
+
+    @property
+    def precision(self):
+        return "double" if self._precision == _lib.PREC_FP64 else "mixed"
+
+    @property
+    def plan(self):
+        return self._ensure_plan(self._batch_max)
+
+    def _ensure_plan(self, cells):
+        if self._plan is None or self._plan.batch_max < cells:
+            if self._plan is not None:
+                torch.cuda.synchronize(self._device)
+                self._plan.close()
+            self._batch_max = max(self._batch_max, int(cells))
+            self._plan = Plan(self.sm, self._e, self._e0, self._gamma, self._precision, self._batch_max,
+                              self._device)
+        return self._plan
+
+    # -- evaluation --------------------------------------------------------
+    def _as_device(self, input_f):
+        """(device FP64 contiguous tensor, was_numpy)."""
+        n = self.sm.nv
+        if tuple(input_f.shape[-3:]) != (n, n, n):
+            raise ValueError(f"input_f must end with ({n}, {n}, {n}), got {tuple(input_f.shape)}")
+        if isinstance(input_f, torch.Tensor):
+            t = input_f
+            if not t.is_cuda:
+                t = t.to(f"cuda:{self._device}")
+            return t.to(torch.float64).contiguous(), False
+        a = np.ascontiguousarray(input_f, dtype=np.float64)
+        key = a.shape
+        pin = self._pinned.get(key)
+        if pin is None:
+            pin = (torch.empty(key, dtype=torch.float64).pin_memory(),
+                   torch.empty(key, dtype=torch.float64).pin_memory())
+            self._pinned = {key: pin}
+        pin[0].numpy()[...] = a
+        return pin[0].to(f"cuda:{self._device}", non_blocking=True), True
+
+    def _run(self, input_f, with_loss, heat_bath):
+        f, was_np = self._as_device(input_f)
+        lead = f.shape[:-3]
+        cells = int(np.prod(lead)) if len(lead) else 1
+        plan = self._ensure_plan(cells)
+        q = torch.empty_like(f)
+        st = plan._lib.pii_collide(plan.handle, f.data_ptr(), q.data_ptr(), cells, int(bool(with_loss)),
+                                   float(heat_bath or 0.0), int(self.mass_fix), _stream_handle())
+        _lib.check(st, "pii_collide")
+        self._input_shape = tuple(f.shape)
+        if was_np:
+            out = self._pinned[tuple(f.shape)][1]
+            out.copy_(q, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            return out.numpy().copy()
+        return q
+
+    def __call__(self, input_f, heat_bath=None, device="gpu"):
+        """``BaseCollision.__call__`` (src/collision/base.py:32-58): Q of each
+        cell (gain only unless the operator was built with ``with_loss=True``),
+        plus ``heat_bath * laplacian`` when ``heat_bath`` is truthy."""
+        if device not in ("cpu", "gpu", "cuda"):
+            raise ValueError(f"unknown device {device!r}")
+        return self._run(input_f, self.default_with_loss, heat_bath if heat_bath else 0.0)
+
+    def collide(self, input_f, with_loss=False):
+        """``collide`` (src/collision/inelastic_collisions.py:208-227)."""
+        return self._run(input_f, with_loss, 0.0)
+
+    def laplacian(self, input_f):
+        """Heat-bath Laplacian (src/collision/inelastic_collisions.py:229-230)."""
+        with_hb = self._run(input_f, False, 1.0)
+        gain = self._run(input_f, False, 0.0)
+        return with_hb - gain
+
+    def close(self):
+        if self._plan is not None:
+            self._plan.close()
+            self._plan = None

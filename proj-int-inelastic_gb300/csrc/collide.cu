@@ -1,0 +1,92 @@
+// Orchestration of one batched Q(f,f) evaluation (pii_collide) and dispatch on
+// (precision, n) to the templated kernels.
+#include "pii_internal.cuh"
+
+namespace pii {
+
+template <typename T, int NV>
+static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb,
+                     cudaStream_t s) {
+  using K = CollideKernels<T, NV>;
+  const int64_t N = p->N;
+  PII_TRY(K::fwd(p, f, 0, cells, s));
+  // items = (cell, pair); a chunk holds Cc cells x Pc pairs in the L2-resident buffer
+  int64_t Cc = std::max<int64_t>(1, (int64_t(131072) + N - 1) / N);
+  Cc = std::min<int64_t>(Cc, std::min<int64_t>(cells, p->chunk_items));
+  const int64_t Pc = std::max<int64_t>(1, std::min<int64_t>(p->Q, p->chunk_items / Cc));
+  for (int64_t c0 = 0; c0 < cells; c0 += Cc) {
+    const int64_t cc = std::min(Cc, cells - c0);
+    for (int64_t p0 = 0; p0 < p->Q; p0 += Pc) {
+      const int64_t np = std::min(Pc, p->Q - p0);
+      PII_TRY(K::pairs(p, c0, cc, p0, np, p0 == 0, s));
+    }
+  }
+  const int64_t Fc = std::max<int64_t>(1, p->chunk_items / 2);
+  for (int64_t c0 = 0; c0 < cells; c0 += Fc) {
+    const int64_t cc = std::min(Fc, cells - c0);
+    PII_TRY(K::finish(p, f, q, c0, cc, with_loss, hb, s));
+  }
+  return PII_OK;
+}
+
+template <typename T>
+static int collide_n(pii_plan* p, const double* f, double* q, int64_t cells, int wl, double hb, cudaStream_t s) {
+  switch (p->n) {
+    case 8: return collide_t<T, 8>(p, f, q, cells, wl, hb, s);
+    case 16: return collide_t<T, 16>(p, f, q, cells, wl, hb, s);
+    case 24: return collide_t<T, 24>(p, f, q, cells, wl, hb, s);
+    case 32: return collide_t<T, 32>(p, f, q, cells, wl, hb, s);
+    case 48: return collide_t<T, 48>(p, f, q, cells, wl, hb, s);
+    case 64: return collide_t<T, 64>(p, f, q, cells, wl, hb, s);
+    default: set_error("collide: unsupported n = %d", p->n); return PII_ERR_ARG;
+  }
+}
+
+int prepare_impl(pii_plan* p) {
+  const bool f32 = p->precision == PII_PREC_FP32;
+  switch (p->n) {
+    case 8: return f32 ? CollideKernels<float, 8>::prepare() : CollideKernels<double, 8>::prepare();
+    case 16: return f32 ? CollideKernels<float, 16>::prepare() : CollideKernels<double, 16>::prepare();
+    case 24: return f32 ? CollideKernels<float, 24>::prepare() : CollideKernels<double, 24>::prepare();
+    case 32: return f32 ? CollideKernels<float, 32>::prepare() : CollideKernels<double, 32>::prepare();
+    case 48: return f32 ? CollideKernels<float, 48>::prepare() : CollideKernels<double, 48>::prepare();
+    case 64: return f32 ? CollideKernels<float, 64>::prepare() : CollideKernels<double, 64>::prepare();
+    default: set_error("unsupported n = %d", p->n); return PII_ERR_ARG;
+  }
+}
+
+int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb, int mass_fix,
+                 cudaStream_t s) {
+  if (!p || !f || !q) {
+    set_error("pii_collide: NULL argument");
+    return PII_ERR_ARG;
+  }
+  if (cells <= 0 || cells > p->batch_max) {
+    set_error("pii_collide: cells = %lld outside [1, batch_max = %lld]", (long long)cells,
+              (long long)p->batch_max);
+    return PII_ERR_SIZE;
+  }
+  if (f == q) {
+    set_error("pii_collide: f and q must not alias");
+    return PII_ERR_ARG;
+  }
+  int st = p->precision == PII_PREC_FP32 ? collide_n<float>(p, f, q, cells, with_loss, hb, s)
+                                         : collide_n<double>(p, f, q, cells, with_loss, hb, s);
+  if (st != PII_OK) return st;
+  if (mass_fix) PII_TRY(mass_fix_impl(q, cells, p->N, s));
+  return PII_OK;
+}
+
+}  // namespace pii
+
+extern "C" int pii_collide(pii_plan* plan, const double* f, double* q, int64_t cells, int with_loss,
+                           double heat_bath, int mass_fix, void* stream) {
+  if (plan) {
+    cudaError_t e = cudaSetDevice(plan->device);
+    if (e != cudaSuccess) {
+      pii::set_error("cudaSetDevice: %s", cudaGetErrorString(e));
+      return PII_ERR_CUDA;
+    }
+  }
+  return pii::collide_impl(plan, f, q, cells, with_loss, heat_bath, mass_fix, (cudaStream_t)stream);
+}

@@ -1,0 +1,126 @@
+// Internal declarations shared by the translation units of libpii_gb300.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/pii_gb300.h"
+
+namespace pii {
+
+void set_error(const char* fmt, ...);
+
+#define PII_CUDA(call)                                                                    \
+  do {                                                                                    \
+    cudaError_t _e = (call);                                                              \
+    if (_e != cudaSuccess) {                                                              \
+      ::pii::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(_e)); \
+      return PII_ERR_CUDA;                                                                \
+    }                                                                                     \
+  } while (0)
+
+#define PII_CHECK_LAUNCH()                                                                 \
+  do {                                                                                     \
+    cudaError_t _e = cudaGetLastError();                                                   \
+    if (_e != cudaSuccess) {                                                               \
+      ::pii::set_error("%s:%d kernel launch: %s", __FILE__, __LINE__, cudaGetErrorString(_e)); \
+      return PII_ERR_CUDA;                                                                 \
+    }                                                                                      \
+  } while (0)
+
+#define PII_TRY(expr)          \
+  do {                         \
+    int _s = (expr);           \
+    if (_s != PII_OK) return _s; \
+  } while (0)
+
+// Device tables, all in the plan's working precision (float or double).
+//   ephase [Q][3][n] complex : exp(-i pi r sigma_d k / L); the d = 0 row also
+//                              carries the 1/n^3 of the first inverse FFT
+//   gphase [Q][3][n] complex : exp(+i a(r) r sigma_d k)
+//   gsinc  [n_r][M+1] real   : r^{gamma+2} w_r w_sigma sinc(a(r) r sqrt(m))
+//                              (the 4 pi prefactor cancels the 1/(4 pi) of collide)
+//   lossk  [M+1] real        : sum_r 4 pi r^{gamma+2} w_r sinc(pi r sqrt(m) / L)
+//   lapl   [M+1] real        : -pi^2 m / L^2
+// with k the signed spectral index of the storage position and m = |k|^2 <= M = 3 (n/2)^2.
+struct Tables {
+  void* ephase = nullptr;
+  void* gphase = nullptr;
+  void* gsinc = nullptr;
+  void* lossk = nullptr;
+  void* lapl = nullptr;
+  int M = 0;
+};
+
+struct GraphKey {
+  int integrator;
+  double* f;
+  int64_t nx;
+  double dt, dx, kn;
+  int bc_lo, bc_hi, with_loss, mass_fix, levels;
+  int K[3];
+  double h[3];
+  void* stream;
+  bool operator<(const GraphKey& o) const;
+};
+
+struct GraphEntry {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+}  // namespace pii
+
+struct pii_plan {
+  int n = 0, nr = 0, ns = 0, Q = 0;
+  int64_t N = 0;
+  int precision = 0;
+  int device = 0;
+  double L = 0, R = 0, e = 0, e0 = 0, gamma = 0, wsigma = 0;
+  int64_t batch_max = 0;
+  std::vector<double> r, wr, sigma;
+  pii::Tables tab;
+  // workspace (precision-typed unless noted)
+  void* fhat = nullptr;  // batch_max * N complex
+  void* fT = nullptr;    // batch_max * N real
+  void* G = nullptr;     // batch_max * N complex
+  void* buf = nullptr;   // chunk_items * N complex
+  int64_t chunk_items = 0;
+  double* q = nullptr;    // batch_max * N, FP64 collide output inside the solver
+  double* d0 = nullptr;   // batch_max * N, FP64 level increments
+  double* d1 = nullptr;
+  double* d2 = nullptr;
+  double* v1dev = nullptr;  // n first-axis velocities (device)
+  int64_t bytes = 0;
+  std::map<pii::GraphKey, pii::GraphEntry> graphs;
+};
+
+namespace pii {
+
+// collide.cu
+int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb,
+                 int mass_fix, cudaStream_t s);
+int prepare_impl(pii_plan* p);
+// transport.cu
+int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
+                   double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);
+int mass_fix_impl(double* q, int64_t cells, int64_t N, cudaStream_t s);
+int axpby_impl(double* f, const double* d, double a, double b, int64_t count, cudaStream_t s);
+int upload_v1(pii_plan* p, const double* v1, cudaStream_t s);
+
+// per-precision, per-size kernels (collide_kernels_*.cu)
+template <typename T, int NV>
+struct CollideKernels {
+  static int prepare();
+  static int fwd(pii_plan* p, const double* f, int64_t c0, int64_t cells, cudaStream_t s);
+  static int pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t p0, int64_t np, bool first,
+                   cudaStream_t s);
+  static int finish(pii_plan* p, const double* f, double* q, int64_t c0, int64_t cells, int with_loss,
+                    double hb, cudaStream_t s);
+};
+
+}  // namespace pii

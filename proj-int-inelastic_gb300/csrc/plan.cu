@@ -1,0 +1,209 @@
+// Plan construction: quadrature tables in FP64 on the host, uploaded once in
+// the working precision; workspace sized for batch_max cells.
+//
+// Tables follow FSInelasticVHSCollision.perform_precomputation
+// (src/collision/inelastic_collisions.py:57-137), factored so that nothing of
+// size n_r * n_sigma * n^3 is stored:
+//   exp(-i pi r k.sigma / L) = prod_d exp(-i pi r sigma_d k_d / L)   (per-axis rows)
+//   exp(+i a(r) r k.sigma)    = prod_d exp(+i a(r) r sigma_d k_d)    (per-axis rows)
+//   sinc(a(r) r |k|), sinc(pi r |k| / L) depend on |k|^2 = m only  (tables over m)
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "pii_internal.cuh"
+
+namespace pii {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+bool GraphKey::operator<(const GraphKey& o) const {
+  return std::tie(integrator, f, nx, dt, dx, kn, bc_lo, bc_hi, with_loss, mass_fix, levels, K[0], K[1], K[2],
+                  h[0], h[1], h[2], stream) <
+         std::tie(o.integrator, o.f, o.nx, o.dt, o.dx, o.kn, o.bc_lo, o.bc_hi, o.with_loss, o.mass_fix,
+                  o.levels, o.K[0], o.K[1], o.K[2], o.h[0], o.h[1], o.h[2], o.stream);
+}
+
+static double sinc(double x) { return x == 0.0 ? 1.0 : std::sin(x) / x; }
+
+template <typename T>
+static int upload_tables(pii_plan* p) {
+  const int n = p->n, nr = p->nr, ns = p->ns, Q = p->Q;
+  const int M = 3 * (n / 2) * (n / 2);
+  p->tab.M = M;
+  const double pi = 3.141592653589793238462643383279502884;
+  std::vector<T> eph(size_t(Q) * 3 * n * 2), gph(size_t(Q) * 3 * n * 2);
+  std::vector<T> gs(size_t(nr) * (M + 1)), lk(M + 1), lp(M + 1);
+  const double invN = 1.0 / double(p->N);
+  std::vector<double> lk_d(M + 1, 0.0);
+  for (int ir = 0; ir < nr; ++ir) {
+    const double r = p->r[ir], wr = p->wr[ir];
+    // restitution law and exponential factor (inelastic_collisions.py:77-80)
+    const double er = 0.5 * (p->e0 - p->e) * std::tanh(r - 0.5 * p->R) + 0.5 * (p->e0 + p->e);
+    const double afac = 0.25 * pi * (1.0 + er) / p->L;
+    const double rg = std::pow(r, p->gamma + 2.0);  // pre_fac(r) / (4 pi)  (:54-55)
+    for (int m = 0; m <= M; ++m) {
+      const double kn = std::sqrt(double(m));
+      gs[size_t(ir) * (M + 1) + m] = T(rg * wr * p->wsigma * sinc(afac * r * kn));
+      lk_d[m] += 4.0 * pi * rg * wr * sinc(pi * r * kn / p->L);  // loss (:109-114)
+    }
+    for (int is = 0; is < ns; ++is) {
+      const int pair = ir * ns + is;
+      for (int d = 0; d < 3; ++d) {
+        const double sd = p->sigma[size_t(is) * 3 + d];
+        for (int i = 0; i < n; ++i) {
+          const int k = i < n / 2 ? i : i - n;
+          const double th_e = -pi * r * sd * double(k) / p->L;
+          const double th_g = afac * r * sd * double(k);
+          const double sc = (d == 0) ? invN : 1.0;
+          const size_t o = ((size_t(pair) * 3 + d) * n + i) * 2;
+          eph[o] = T(sc * std::cos(th_e));
+          eph[o + 1] = T(sc * std::sin(th_e));
+          gph[o] = T(std::cos(th_g));
+          gph[o + 1] = T(std::sin(th_g));
+        }
+      }
+    }
+  }
+  for (int m = 0; m <= M; ++m) {
+    lk[m] = T(lk_d[m]);
+    lp[m] = T(-pi * pi / (p->L * p->L) * double(m));  // (:69)
+  }
+  auto up = [&](void** dst, const void* src, size_t bytes) -> int {
+    PII_CUDA(cudaMalloc(dst, bytes));
+    PII_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+    p->bytes += int64_t(bytes);
+    return PII_OK;
+  };
+  PII_TRY(up(&p->tab.ephase, eph.data(), eph.size() * sizeof(T)));
+  PII_TRY(up(&p->tab.gphase, gph.data(), gph.size() * sizeof(T)));
+  PII_TRY(up(&p->tab.gsinc, gs.data(), gs.size() * sizeof(T)));
+  PII_TRY(up(&p->tab.lossk, lk.data(), lk.size() * sizeof(T)));
+  PII_TRY(up(&p->tab.lapl, lp.data(), lp.size() * sizeof(T)));
+  return PII_OK;
+}
+
+static int alloc(pii_plan* p, void** dst, size_t bytes) {
+  PII_CUDA(cudaMalloc(dst, bytes));
+  p->bytes += int64_t(bytes);
+  return PII_OK;
+}
+
+static void free_plan(pii_plan* p) {
+  if (!p) return;
+  for (auto& kv : p->graphs) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
+                  p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete p;
+}
+
+static int create(pii_plan** out, int n, int nr, int ns, const double* r, const double* wr, const double* sigma,
+                  double wsigma, double L, double R, double e, double e0, double gamma, int precision,
+                  int64_t batch_max, int device) {
+  if (!out) {
+    set_error("pii_plan_create: out is NULL");
+    return PII_ERR_ARG;
+  }
+  *out = nullptr;
+  if (!(n == 8 || n == 16 || n == 24 || n == 32 || n == 48 || n == 64)) {
+    set_error("pii_plan_create: n = %d unsupported (8, 16, 24, 32, 48, 64)", n);
+    return PII_ERR_ARG;
+  }
+  if (nr <= 0 || ns <= 0 || !r || !wr || !sigma || batch_max <= 0 || !(L > 0) || !(R > 0)) {
+    set_error("pii_plan_create: invalid quadrature / domain arguments");
+    return PII_ERR_ARG;
+  }
+  if (precision != PII_PREC_FP32 && precision != PII_PREC_FP64) {
+    set_error("pii_plan_create: precision must be PII_PREC_FP32 or PII_PREC_FP64");
+    return PII_ERR_ARG;
+  }
+  PII_CUDA(cudaSetDevice(device));
+  pii_plan* p = new pii_plan();
+  p->n = n;
+  p->nr = nr;
+  p->ns = ns;
+  p->Q = nr * ns;
+  p->N = int64_t(n) * n * n;
+  p->precision = precision;
+  p->device = device;
+  p->L = L;
+  p->R = R;
+  p->e = e;
+  p->e0 = e0;
+  p->gamma = gamma;
+  p->wsigma = wsigma;
+  p->batch_max = batch_max;
+  p->r.assign(r, r + nr);
+  p->wr.assign(wr, wr + nr);
+  p->sigma.assign(sigma, sigma + size_t(ns) * 3);
+  int st = precision == PII_PREC_FP32 ? upload_tables<float>(p) : upload_tables<double>(p);
+  if (st != PII_OK) {
+    free_plan(p);
+    return st;
+  }
+  const size_t rs = precision == PII_PREC_FP32 ? 4 : 8;
+  const size_t cs = 2 * rs;
+  const size_t N = size_t(p->N);
+  // L2-resident chunk of (cell, pair) items: ~48 MB, at least 2 items
+  const size_t target = size_t(48) << 20;
+  p->chunk_items = std::max<int64_t>(2, int64_t(target / (N * cs)));
+  int s2 = PII_OK;
+  if ((s2 = alloc(p, &p->fhat, size_t(batch_max) * N * cs)) != PII_OK ||
+      (s2 = alloc(p, &p->fT, size_t(batch_max) * N * rs)) != PII_OK ||
+      (s2 = alloc(p, &p->G, size_t(batch_max) * N * cs)) != PII_OK ||
+      (s2 = alloc(p, &p->buf, size_t(p->chunk_items) * N * cs)) != PII_OK ||
+      (s2 = alloc(p, (void**)&p->q, size_t(batch_max) * N * 8)) != PII_OK ||
+      (s2 = alloc(p, (void**)&p->d0, size_t(batch_max) * N * 8)) != PII_OK ||
+      (s2 = alloc(p, (void**)&p->v1dev, size_t(n) * 8)) != PII_OK) {
+    free_plan(p);
+    return s2;
+  }
+  if ((s2 = prepare_impl(p)) != PII_OK) {
+    free_plan(p);
+    return s2;
+  }
+  *out = p;
+  return PII_OK;
+}
+
+}  // namespace pii
+
+extern "C" {
+
+const char* pii_last_error(void) { return pii::g_err; }
+
+const char* pii_version(void) { return "pii_gb300 0.1 (sm_103a)"; }
+
+int pii_plan_create(pii_plan** out, int n, int n_r, int n_sigma, const double* r, const double* w_r,
+                    const double* sigma, double w_sigma, double L, double R, double e, double e0,
+                    double gamma, int precision, int64_t batch_max, int device) {
+  return pii::create(out, n, n_r, n_sigma, r, w_r, sigma, w_sigma, L, R, e, e0, gamma, precision, batch_max,
+                     device);
+}
+
+int pii_plan_destroy(pii_plan* plan) {
+  if (!plan) {
+    pii::set_error("pii_plan_destroy: NULL plan");
+    return PII_ERR_ARG;
+  }
+  cudaSetDevice(plan->device);
+  pii::free_plan(plan);
+  return PII_OK;
+}
+
+int64_t pii_plan_workspace_bytes(const pii_plan* plan) { return plan ? plan->bytes : -1; }
+
+}  // extern "C"

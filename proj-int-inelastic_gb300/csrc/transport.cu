@@ -1,0 +1,224 @@
+// FP64 islands and the transport step:
+//   * k_df        : second-order upwind + minmod TVD increment in x, fused with
+//                   the collision term  df = transport(f, dt) + dt * Q / kn
+//                   (src/boltzmann.py:160-205, src/solver.py:59-105,
+//                    src/riemann/advection_1D.py:4-21, src/limiters/tvd.py:6-40)
+//   * k_axpy3     : f += s2 * (s1 * (s0 * d))  -- the projective extrapolations
+//                   with the reference's rounding order (src/boltzmann.py:120-158)
+//   * k_massfix   : per-cell FP64 mean removal of Q (k = 0 mode; not in the reference)
+//   * k_moments   : per-cell FP64 sums of f, f v, f |v|^2 / 2
+// The state f and every increment are FP64 in every precision mode.
+#include "pii_internal.cuh"
+
+namespace pii {
+
+struct DfArgs {
+  const double* f;
+  const double* q;  // may be NULL (transport only)
+  double* df;
+  const double* v1;  // n first-axis velocities
+  int64_t nx, N, N2;
+  double dt, dtdx, kn;
+  int bc_lo, bc_hi, transport;
+};
+
+__device__ __forceinline__ double limited_wave(double w, double wl, double wr, double s) {
+  // tvd.limit: r = (upwind wave * w) / w^2 (0 where w^2 == 0), minmod phi = max(0, min(1, r))
+  const double den = w * w;
+  double r = 0.0;
+  if (den != 0.0) r = (s > 0.0 ? w * wl : wr * w) / den;
+  const double phi = fmax(0.0, fmin(1.0, r));
+  return (w == 0.0) ? w : phi * w;
+}
+
+__global__ void __launch_bounds__(256) k_df(DfArgs a) {
+  const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= a.nx * a.N) return;
+  const int64_t c = gid / a.N;
+  const int64_t j = gid - c * a.N;
+  double d = 0.0;
+  if (a.transport) {
+    const double s = a.v1[j / a.N2];
+    // ghost cells: extrapolation copies the edge cell, periodic wraps (any nx >= 1)
+    auto at = [&](int64_t ci) -> double {
+      if (ci < 0) ci = (a.bc_lo == PII_BC_PERIODIC) ? ((ci % a.nx) + a.nx) % a.nx : 0;
+      if (ci >= a.nx) ci = (a.bc_hi == PII_BC_PERIODIC) ? ci % a.nx : a.nx - 1;
+      return a.f[ci * a.N + j];
+    };
+    const double fm2 = at(c - 2), fm1 = at(c - 1), f0 = a.f[c * a.N + j], fp1 = at(c + 1), fp2 = at(c + 2);
+    const double wm2 = fm1 - fm2, wm1 = f0 - fm1, w0 = fp1 - f0, wp1 = fp2 - fp1;
+    const double dtdx = a.dtdx;
+    d = -dtdx * (fmin(s, 0.0) * w0 + fmax(s, 0.0) * wm1);
+    const double sabs = fabs(s);
+    const double om = 1.0 - sabs * dtdx;
+    const double cf = 0.5 * sabs * om;
+    const double Fl = cf * limited_wave(wm1, wm2, w0, s);
+    const double Fr = cf * limited_wave(w0, wm1, wp1, s);
+    d -= dtdx * (Fr - Fl);
+  }
+  if (a.q) d += a.dt * a.q[gid] / a.kn;
+  a.df[gid] = d;
+}
+
+__global__ void __launch_bounds__(256) k_axpy3(double* f, const double* d, double s0, double s1, double s2,
+                                                int64_t count) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  double t = s0 * d[i];
+  t = s1 * t;
+  t = s2 * t;
+  f[i] += t;
+}
+
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < NT / 32) r = sh[threadIdx.x];
+  if (w == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(256) k_massfix(double* q, int64_t N) {
+  __shared__ double sh[8];
+  __shared__ double mean;
+  double* qc = q + int64_t(blockIdx.x) * N;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < N; i += blockDim.x) s += qc[i];
+  s = block_sum<256>(s, sh);
+  if (threadIdx.x == 0) mean = s / double(N);
+  __syncthreads();
+  const double m = mean;
+  for (int64_t i = threadIdx.x; i < N; i += blockDim.x) qc[i] -= m;
+}
+
+__global__ void __launch_bounds__(256) k_moments(const double* f, double* out, const double* v, int n,
+                                                  double dv) {
+  __shared__ double sh[8];
+  const int64_t N = int64_t(n) * n * n;
+  const double* fc = f + int64_t(blockIdx.x) * N;
+  double m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0;
+  for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
+    const int a = int(i / (int64_t(n) * n));
+    const int b = int((i / n) % n);
+    const int c = int(i % n);
+    const double x = fc[i];
+    const double va = v[a], vb = v[b], vc = v[c];
+    m0 += x;
+    m1 += x * va;
+    m2 += x * vb;
+    m3 += x * vc;
+    m4 += x * (va * va + vb * vb + vc * vc);
+  }
+  double r[5] = {m0, m1, m2, m3, m4};
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double t = block_sum<256>(r[k], sh);
+    if (threadIdx.x == 0) out[int64_t(blockIdx.x) * 5 + k] = (k == 4 ? 0.5 * t : t) * dv;
+  }
+}
+
+int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt, double dx,
+                   int bc_lo, int bc_hi, double kn, cudaStream_t s) {
+  DfArgs a{};
+  a.f = f;
+  a.q = q;
+  a.df = df;
+  a.v1 = p->v1dev;
+  a.nx = nx;
+  a.N = p->N;
+  a.N2 = int64_t(p->n) * p->n;
+  a.dt = dt;
+  a.kn = kn;
+  a.transport = dx > 0.0 ? 1 : 0;
+  a.dtdx = dx > 0.0 ? dt / dx : 0.0;
+  a.bc_lo = bc_lo;
+  a.bc_hi = bc_hi;
+  const int64_t total = nx * p->N;
+  k_df<<<unsigned((total + 255) / 256), 256, 0, s>>>(a);
+  PII_CHECK_LAUNCH();
+  return PII_OK;
+}
+
+int mass_fix_impl(double* q, int64_t cells, int64_t N, cudaStream_t s) {
+  k_massfix<<<unsigned(cells), 256, 0, s>>>(q, N);
+  PII_CHECK_LAUNCH();
+  return PII_OK;
+}
+
+int axpy3_impl(double* f, const double* d, double s0, double s1, double s2, int64_t count, cudaStream_t s) {
+  if (count <= 0) return PII_OK;
+  k_axpy3<<<unsigned((count + 255) / 256), 256, 0, s>>>(f, d, s0, s1, s2, count);
+  PII_CHECK_LAUNCH();
+  return PII_OK;
+}
+
+int upload_v1(pii_plan* p, const double* v1, cudaStream_t s) {
+  if (!v1) {
+    set_error("v1 velocity array is NULL");
+    return PII_ERR_ARG;
+  }
+  PII_CUDA(cudaMemcpyAsync(p->v1dev, v1, size_t(p->n) * sizeof(double), cudaMemcpyHostToDevice, s));
+  return PII_OK;
+}
+
+int check_bcs(int lo, int hi) {
+  if ((lo != PII_BC_EXTRAP && lo != PII_BC_PERIODIC) || (hi != PII_BC_EXTRAP && hi != PII_BC_PERIODIC)) {
+    set_error("Boundary condition (%d, %d) not implemented", lo, hi);
+    return PII_ERR_ARG;
+  }
+  return PII_OK;
+}
+
+}  // namespace pii
+
+extern "C" {
+
+int pii_transport_df(pii_plan* plan, const double* f, double* df, int64_t nx, double dt, double dx,
+                     const double* v1, int bc_lower, int bc_upper, void* stream) {
+  if (!plan || !f || !df || nx <= 0 || !(dx > 0)) {
+    pii::set_error("pii_transport_df: invalid arguments");
+    return PII_ERR_ARG;
+  }
+  if (nx > plan->batch_max) {
+    pii::set_error("pii_transport_df: nx beyond batch_max");
+    return PII_ERR_SIZE;
+  }
+  PII_TRY(pii::check_bcs(bc_lower, bc_upper));
+  cudaStream_t s = (cudaStream_t)stream;
+  PII_CUDA(cudaSetDevice(plan->device));
+  PII_TRY(pii::upload_v1(plan, v1, s));
+  return pii::transport_impl(plan, f, nullptr, df, nx, dt, dx, bc_lower, bc_upper, 1.0, s);
+}
+
+int pii_moments(pii_plan* plan, const double* f, double* out, int64_t cells, const double* v, double delta,
+                void* stream) {
+  if (!plan || !f || !out || !v || cells <= 0) {
+    pii::set_error("pii_moments: invalid arguments");
+    return PII_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PII_CUDA(cudaSetDevice(plan->device));
+  PII_TRY(pii::upload_v1(plan, v, s));
+  pii::k_moments<<<unsigned(cells), 256, 0, s>>>(f, out, plan->v1dev, plan->n, delta * delta * delta);
+  PII_CHECK_LAUNCH();
+  return PII_OK;
+}
+
+int pii_axpby(double* f, const double* d, double a, double b, int64_t count, void* stream) {
+  if (!f || !d || count < 0) {
+    pii::set_error("pii_axpby: invalid arguments");
+    return PII_ERR_ARG;
+  }
+  return pii::axpy3_impl(f, d, b, 1.0, a, count, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,454 @@
+"""Time integrators with the reference's solver interface, stepping on the GPU.
+
+* ``BC``, ``Solver``, ``BoltzmannSolver``, ``BoltzmannSolver1D`` keep the
+  attributes and methods of src/solver.py:1-146 and src/boltzmann.py:16-205
+  (``kn``, ``dt``, ``time_integrator`` in {"Euler", "PFE", "TPI2", "TPI3"},
+  ``inner_steps``, ``inner_dt``, ``bc_lower`` / ``bc_upper`` / ``all_bcs``,
+  ``step``, ``df``, ``df_advection``, ``evolve_to_time``).
+* ``State`` / ``Solution`` hold f as a torch CUDA FP64 tensor of shape
+  (n_x, n, n, n) (or (n, n, n) for a space-homogeneous problem), with FP64
+  3D-velocity moments ``rho``, ``u``, ``T`` (src/state.py, src/solution.py).
+* ``IterativeBoltzmannSolver`` keeps ``solve`` / ``step``
+  (src/iter_solver.py:9-35).
+
+With the GB300 ``FSInelasticVHSCollision`` as the collision operator, a whole
+macro-step (all inner steps, transport, FP64 extrapolations) runs as one
+``pii_step`` call, captured into a CUDA graph on first use.  Any other
+collision callable is stepped by the same nesting in Python, with the
+transport and FP64 updates still on the GPU.
+"""
+import logging
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .collision import FSInelasticVHSCollision
+
+_INTEGRATORS = {"Euler": _lib.INT_EULER, "PFE": _lib.INT_PFE, "TPI2": _lib.INT_TPI2, "TPI3": _lib.INT_TPI3}
+_LEVELS = {"Euler": 0, "PFE": 1, "TPI2": 2, "TPI3": 3}
+
+
+class BC:
+    extrap = _lib.BC_EXTRAP
+    periodic = _lib.BC_PERIODIC
+
+
+class State:
+    """Phase-space state: f on the GPU, FP64 (src/state.py:6-122)."""
+
+    def __init__(self, num_cells, lower, upper, num_dim_x, device=0):
+        self.num_cells = list(num_cells)
+        self.lower = list(lower)
+        self.upper = list(upper)
+        self.num_dim_x = int(num_dim_x)
+        self.delta = [(u - lo) / n for lo, u, n in zip(self.lower, self.upper, self.num_cells)]
+        self.device = int(device)
+        self.t = 0.0
+        self.f = torch.zeros(self.num_cells, dtype=torch.float64, device=f"cuda:{self.device}")
+        self.problem_data = {}
+
+    def centers(self, axis):
+        lo, d, n = self.lower[axis], self.delta[axis], self.num_cells[axis]
+        return np.array([lo + (i + 0.5) * d for i in range(n)])
+
+    @property
+    def v(self):
+        """Velocity centres (same on the three velocity axes)."""
+        return self.centers(self.num_dim_x)
+
+    @property
+    def v1(self):
+        return self.v
+
+    @property
+    def dv(self):
+        return self.delta[self.num_dim_x]
+
+    def moments(self):
+        """FP64 (rho, u[3], T) per cell from ``pii_moments`` (3D-velocity form of
+        State.rho / u / T, src/state.py:31-52)."""
+        f = self.f
+        n = f.shape[-1]
+        cells = f.numel() // (n**3)
+        out = torch.empty((cells, 5), dtype=torch.float64, device=f.device)
+        plan = _moment_plan(n, f.device.index or 0)
+        v = np.ascontiguousarray(self.v, np.float64)
+        st = plan._lib.pii_moments(plan.handle, f.contiguous().data_ptr(), out.data_ptr(), cells, _lib.dptr(v),
+                                   float(self.dv), torch.cuda.current_stream().cuda_stream)
+        _lib.check(st, "pii_moments")
+        m = out.cpu().numpy()
+        rho = m[:, 0]
+        u = m[:, 1:4] / rho[:, None]
+        T = (2.0 / 3.0) * (m[:, 4] / rho - 0.5 * (u**2).sum(-1))
+        shape = f.shape[:-3]
+        return rho.reshape(shape), u.reshape(shape + (3,)), T.reshape(shape)
+
+    @property
+    def rho(self):
+        return self.moments()[0]
+
+    @property
+    def u(self):
+        return self.moments()[1]
+
+    @property
+    def T(self):
+        return self.moments()[2]
+
+
+_MPLANS = {}
+
+
+def _moment_plan(n, device):
+    """A minimal plan used only for its moment / velocity buffers."""
+    key = (n, device)
+    if key not in _MPLANS:
+        from .collision import Plan
+
+        class _Mesh:
+            nv = n
+            L = 1.0
+            R = 1.0
+
+            @staticmethod
+            def rquad():
+                return np.array([0.5]), np.array([1.0])
+
+            @staticmethod
+            def circ_or_sphr_quad():
+                return np.array([[0.0, 0.0, 1.0]]), 4 * math.pi
+
+        _MPLANS[key] = Plan(_Mesh, 1.0, 1.0, 0.0, _lib.PREC_FP64, 1, device)
+    return _MPLANS[key]
+
+
+class Solution:
+    """``Solution(config)`` (src/solution.py:47-57): config has dim_x, dim_v,
+    xmin, xmax, l, nx, nv (attribute or key access).  dim_x = 0 gives a
+    space-homogeneous state f of shape (nv, nv, nv)."""
+
+    def __init__(self, config, device=0):
+        get = (lambda k: config[k]) if isinstance(config, dict) else (lambda k: getattr(config, k))
+        dim_x, dim_v = int(get("dim_x")), int(get("dim_v"))
+        if dim_v != 3:
+            raise NotImplementedError("the GB300 solver implements 3D velocity only")
+        lower, upper, nn = [], [], []
+        if dim_x:
+            lower += [float(get("xmin"))] * dim_x
+            upper += [float(get("xmax"))] * dim_x
+            nn += [int(get("nx"))] * dim_x
+        lower += [-float(get("l"))] * dim_v
+        upper += [float(get("l"))] * dim_v
+        nn += [int(get("nv"))] * dim_v
+        self.state = State(nn, lower, upper, dim_x, device)
+        self.state.problem_data = {"v1": self.state.v}
+
+    @property
+    def t(self):
+        return self.state.t
+
+    @t.setter
+    def t(self, value):
+        self.state.t = value
+
+    @property
+    def f(self):
+        return self.state.f
+
+    def __getattr__(self, key):
+        if key in ("rho", "u", "T", "num_cells", "lower", "upper", "delta", "num_dim_x", "v"):
+            return getattr(self.state, key)
+        raise AttributeError(key)
+
+
+class Solver:
+    """``Solver`` (src/solver.py:13-146)."""
+
+    num_dim_x = 1
+
+    @property
+    def all_bcs(self):
+        return self.bc_lower, self.bc_upper
+
+    @all_bcs.setter
+    def all_bcs(self, all_bcs):
+        for i in range(self.num_dim_x):
+            self.bc_lower[i] = all_bcs
+            self.bc_upper[i] = all_bcs
+
+    def __init__(self, riemann_solver=None, collision_operator=None):
+        self.dt_initial = 0.01
+        self.dt_max = 1e99
+        self.max_steps = 10000
+        self.dt_variable = False
+        self.rp = riemann_solver
+        self.collision = collision_operator
+        self.before_step = None
+        self.dt = self.dt_initial
+        self.bc_lower = [None] * max(self.num_dim_x, 1)
+        self.bc_upper = [None] * max(self.num_dim_x, 1)
+        self._is_set_up = False
+
+    def setup(self, solution):
+        self._is_set_up = True
+
+    def evolve_to_time(self, solution, tend=None):
+        """src/solver.py:107-143."""
+        if not self._is_set_up:
+            self.setup(solution)
+        take_one_step = tend is None
+        tstart = solution.t
+        if not self.dt_variable:
+            if take_one_step:
+                self.max_steps = 1
+            else:
+                self.max_steps = int((tend - tstart + 1e-10) / self.dt)
+                if abs(self.max_steps * self.dt - (tend - tstart)) > 1e-5 * (tend - tstart):
+                    raise Exception("dt does not divide (tend-tstart) and dt is fixed!")
+        for n in range(self.max_steps):
+            if self.before_step is not None:
+                self.before_step(self, solution.state)
+            self.step(solution, take_one_step, tstart, tend)
+            solution.t = tstart + (n + 1) * self.dt
+
+    def step(self, solution, take_one_step, tstart, tend):
+        raise NotImplementedError("No stepping routine has been defined!")
+
+
+class BoltzmannSolver(Solver):
+    """``BoltzmannSolver`` (src/boltzmann.py:16-167) on the GPU.
+
+    Extra attributes: ``with_loss`` (None: use the operator's own default,
+    i.e. gain only as the reference solver does), ``mass_fix`` (FP64 k = 0
+    correction of Q) and ``use_graph`` (capture each macro-step as a CUDA graph).
+    """
+
+    num_dim_x = 0
+
+    def __init__(self, kn=1.0, riemann_solver=None, collision_operator=None):
+        self.kn = kn
+        self.tau = None
+        self.e = None
+        self.num_ghost = 2
+        self.order = 2
+        self.limiters = "minmod"
+        self.time_integrator = "Euler"
+        self.penalty = None
+        self.num_levels = 3
+        self.inner_steps = [3, 3, 3]
+        self.inner_dt = [kn, 5 * kn, 10 * kn]
+        self.with_loss = None
+        self.mass_fix = None
+        self.use_graph = True
+        self._stream = None
+        super().__init__(riemann_solver, collision_operator)
+
+    # -- helpers -----------------------------------------------------------
+    def _transport_args(self, state):
+        """(nx, dx, v1, bc_lo, bc_hi); dx = 0 disables transport."""
+        f = state.f
+        n = f.shape[-1]
+        cells = f.numel() // n**3
+        return cells, 0.0, np.ascontiguousarray(state.v, np.float64), _lib.BC_EXTRAP, _lib.BC_EXTRAP
+
+    def _wl(self):
+        if self.with_loss is not None:
+            return bool(self.with_loss)
+        return bool(getattr(self.collision, "default_with_loss", False))
+
+    def _mf(self):
+        if self.mass_fix is not None:
+            return bool(self.mass_fix)
+        return bool(getattr(self.collision, "mass_fix", False))
+
+    def _get_stream(self, device):
+        if self._stream is None:
+            self._stream = torch.cuda.Stream(device=device)
+        return self._stream
+
+    # -- stepping ----------------------------------------------------------
+    def step(self, solution, take_one_step, tstart, tend):
+        """``BoltzmannSolver.step`` (src/boltzmann.py:46-80)."""
+        ti = self.time_integrator
+        if ti in ("CONSP", "CONSP_M"):
+            raise NotImplementedError("convex-splitting integrators are not implemented on the GPU")
+        if ti not in _INTEGRATORS:
+            raise NotImplementedError("This time integrator is not implemented.")
+        state = solution.state
+        if isinstance(self.collision, FSInelasticVHSCollision):
+            self._fused_step(state, ti)
+        else:
+            self._generic_step(state, ti)
+
+    def _fused_step(self, state, ti):
+        f = state.f
+        if not (f.is_cuda and f.dtype == torch.float64 and f.is_contiguous()):
+            raise ValueError("state.f must be a contiguous CUDA float64 tensor")
+        nx, dx, v1, lo, hi = self._transport_args(state)
+        plan = self.collision._ensure_plan(nx)
+        lev = _LEVELS[ti]
+        K = np.ascontiguousarray(list(self.inner_steps[:lev]) + [0] * (3 - lev), np.int32)
+        h = np.ascontiguousarray(list(self.inner_dt[:lev]) + [0.0] * (3 - lev), np.float64)
+        cur = torch.cuda.current_stream(f.device)
+        s = self._get_stream(f.device) if self.use_graph else cur
+        if s is not cur:
+            s.wait_stream(cur)
+        st = plan._lib.pii_step(plan.handle, _INTEGRATORS[ti], f.data_ptr(), nx, float(self.dt), _lib.iptr(K),
+                                _lib.dptr(h), max(lev, 1), float(dx), _lib.dptr(v1), int(lo), int(hi),
+                                float(self.kn), int(self._wl()), int(self._mf()), int(bool(self.use_graph)),
+                                s.cuda_stream)
+        _lib.check(st, "pii_step")
+        if s is not cur:
+            cur.wait_stream(s)
+
+    def _generic_step(self, state, ti):
+        """Same nesting as src/boltzmann.py:82-158 for an arbitrary collision callable."""
+        f = state.f
+        dt, K, h = self.dt, self.inner_steps, self.inner_dt
+        if ti == "Euler":
+            f += self.df(state, dt)
+        elif ti == "PFE":
+            M = dt / h[0] - K[0]
+            for _ in range(K[0]):
+                d = self.df(state, h[0])
+                f += d
+            f += M * d
+        elif ti == "TPI2":
+            M1 = dt / h[1] - K[1]
+            for _ in range(K[1]):
+                M0 = h[1] / h[0] - K[0]
+                for _ in range(K[0]):
+                    d0 = self.df(state, h[0])
+                    f += d0
+                d1 = M0 * d0
+                f += d1
+            f += M1 * d1
+        else:
+            M2 = dt / h[2] - K[2]
+            for _ in range(K[2]):
+                M1 = h[2] / h[1] - K[1]
+                for _ in range(K[1]):
+                    M0 = h[1] / h[0] - K[0]
+                    for _ in range(K[0]):
+                        d0 = self.df(state, h[0])
+                        f += d0
+                    d1 = M0 * d0
+                    f += d1
+                d2 = M1 * d1
+                f += d2
+            f += M2 * d2
+
+    def df(self, state, dt):
+        """``BoltzmannSolver.df`` (src/boltzmann.py:160-164)."""
+        deltaf = self.df_advection(state, dt)
+        if self.collision is not None:
+            q = self.collision(state.f)
+            if not isinstance(q, torch.Tensor):
+                q = torch.as_tensor(q, device=state.f.device)
+            deltaf += dt * q / self.kn
+        return deltaf
+
+    def df_advection(self, state, dt):
+        return torch.zeros_like(state.f)
+
+
+class BoltzmannSolver0D(BoltzmannSolver):
+    """Space-homogeneous solver: df = dt Q / kn (no transport)."""
+
+    num_dim_x = 0
+
+
+class BoltzmannSolver1D(BoltzmannSolver):
+    """``BoltzmannSolver1D`` (src/boltzmann.py:170-205): transport in x with the
+    second-order upwind + minmod TVD flux, two ghost cells."""
+
+    num_dim_x = 1
+
+    def __init__(self, kn=1, riemann_solver=None, collision_operator=None):
+        super().__init__(kn, riemann_solver, collision_operator)
+
+    def setup(self, solution):
+        for b in (self.bc_lower[0], self.bc_upper[0]):
+            if b is None:
+                raise Exception("Lower boundary condition not specified.")
+            if b not in (BC.extrap, BC.periodic):
+                raise NotImplementedError("Boundary condition %s not implemented" % b)
+        super().setup(solution)
+
+    def _transport_args(self, state):
+        f = state.f
+        nx = f.shape[0]
+        return (nx, float(state.delta[0]), np.ascontiguousarray(state.v, np.float64), int(self.bc_lower[0]),
+                int(self.bc_upper[0]))
+
+    def df_advection(self, state, dt):
+        if not self._is_set_up:
+            self.setup(None)
+        f = state.f.contiguous()
+        nx, dx, v1, lo, hi = self._transport_args(state)
+        out = torch.empty_like(f)
+        plan = _moment_plan(f.shape[-1], f.device.index or 0)
+        if plan.batch_max < nx:
+            _MPLANS.pop((f.shape[-1], f.device.index or 0)).close()
+            plan = _grow_mplan(f.shape[-1], f.device.index or 0, nx)
+        st = plan._lib.pii_transport_df(plan.handle, f.data_ptr(), out.data_ptr(), nx, float(dt), dx, _lib.dptr(v1),
+                                        lo, hi, torch.cuda.current_stream().cuda_stream)
+        _lib.check(st, "pii_transport_df")
+        return out
+
+
+def _grow_mplan(n, device, cells):
+    from .collision import Plan
+
+    class _Mesh:
+        nv = n
+        L = 1.0
+        R = 1.0
+
+        @staticmethod
+        def rquad():
+            return np.array([0.5]), np.array([1.0])
+
+        @staticmethod
+        def circ_or_sphr_quad():
+            return np.array([[0.0, 0.0, 1.0]]), 4 * math.pi
+
+    _MPLANS[(n, device)] = Plan(_Mesh, 1.0, 1.0, 0.0, _lib.PREC_FP64, cells, device)
+    return _MPLANS[(n, device)]
+
+
+class IterativeBoltzmannSolver:
+    """``IterativeBoltzmannSolver`` (src/iter_solver.py:9-35): ``solve`` loops
+    ``step(state)`` until the returned error is below ``tol``."""
+
+    def __init__(self, log_path=None, collision=None, kn=0.1, tol=1e-6):
+        if log_path:
+            logger = logging.getLogger()
+            logger.setLevel(logging.INFO)
+            if not logger.handlers:
+                fh = logging.FileHandler(log_path)
+                fh.setFormatter(logging.Formatter("%(asctime)s:%(levelname)s: %(message)s"))
+                logger.addHandler(fh)
+                sh = logging.StreamHandler()
+                sh.setFormatter(logging.Formatter("%(message)s"))
+                logger.addHandler(sh)
+        self.collision = collision
+        self.kn = kn
+        self.tol = tol
+
+    def solve(self, solution, n_iter=0, disp=False):
+        err = 1
+        num_steps = 1
+        while err > self.tol:
+            if n_iter and num_steps >= n_iter:
+                return err, num_steps
+            err = self.step(solution.state)
+            num_steps += 1
+            if disp and (num_steps % 1 == 0):
+                logging.info("Current error: {}; Number of iterations: {}".format(err, num_steps))
+        return err, num_steps
+
+    def step(self, solution):
+        raise NotImplementedError("No stepping routine has been defined!")

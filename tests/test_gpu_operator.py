@@ -1,0 +1,177 @@
+"""GPU parity of the collision operator against the golden fixtures and the oracle.
+
+Tolerances: <= 1e-12 relative L-inf for the FP64 GPU path, <= 1e-5 for the
+mixed-precision (FP32 FFT / quadrature) path, both against FP64 references.
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+from conftest import L8_S, maxwellian, op_config, rel_linf
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = {"double": 1e-12, "mixed": 1e-5}
+
+
+def _pkg():
+    import proj_int_inelastic_gb300 as pkg
+
+    return pkg
+
+
+def _op(params, precision, **kw):
+    nv, nr, ns, e, e0, g, s = params
+    cfg = op_config(nv, s, nr, ns, e, e0, g)
+    pkg = _pkg()
+    sm = pkg.SpectralMesh(cfg)
+    return sm, pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, **kw)
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+@pytest.mark.parametrize("case", range(4))
+def test_operator_small_golden(golden, case, precision):
+    d = golden("op_small.npz")
+    sm, col = _op(d[f"case{case}_params"], precision)
+    f = d[f"case{case}_f"]
+    tol = TOL[precision]
+    assert rel_linf(col(f), d[f"case{case}_gain"]) < tol  # __call__ = gain only (reference default)
+    assert rel_linf(col.collide(f, with_loss=True), d[f"case{case}_full"]) < tol
+    assert rel_linf(col(f, heat_bath=0.3), d[f"case{case}_heat"]) < tol
+    assert rel_linf(col(f[0]), d[f"case{case}_gain_cell0"]) < tol  # (n, n, n) input
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_operator_c32_two_beam_golden(golden, precision):
+    d = golden("op_c32.npz")
+    sm, col = _op(d["params"], precision)
+    tol = TOL[precision]
+    assert rel_linf(col.collide(d["f"], with_loss=True), d["full"]) < tol
+    assert rel_linf(col.collide(d["f"]), d["gain"]) < tol
+
+
+def test_torch_in_torch_out_and_input_untouched(golden):
+    d = golden("op_small.npz")
+    sm, col = _op(d["case2_params"], "mixed")
+    f = torch.as_tensor(d["case2_f"], device="cuda:0")
+    f0 = f.clone()
+    q = col.collide(f, with_loss=True)
+    assert isinstance(q, torch.Tensor) and q.is_cuda and q.dtype == torch.float64 and q.shape == f.shape
+    assert torch.equal(f, f0)
+    assert rel_linf(q.cpu().numpy(), d["case2_full"]) < 1e-5
+
+
+@pytest.mark.parametrize("nv", [24, 48])
+def test_radix3_sizes_vs_oracle(nv):
+    """n = 24 / 48 (radix-3 stages) against the oracle, FP64 and mixed."""
+    from oracle import fs_inelastic as fo
+
+    nr, ns = (6, 6) if nv == 48 else (8, 12)
+    m = fo.Mesh(nv, L8_S, nr, ns)
+    op = fo.FSInelasticVHS(m, 0.6, 0.9, 1.0)
+    f = maxwellian(m.v, 1.0, (0.5, -0.3, 0.2), 1.2) + 0.3 * maxwellian(m.v, 1.0, (-2, 1, 0), 0.6)
+    ref = op.collide(f, with_loss=True)
+    for prec in ("double", "mixed"):
+        sm, col = _op((nv, nr, ns, 0.6, 0.9, 1.0, L8_S), prec)
+        assert rel_linf(col.collide(f, with_loss=True), ref) < TOL[prec], prec
+
+
+def test_n64_vs_oracle():
+    from oracle import fs_inelastic as fo
+
+    m = fo.Mesh(64, L8_S * 1.25, 4, 6)
+    op = fo.FSInelasticVHS(m, 0.7, 0.7, 1.0)
+    f = maxwellian(m.v, 1.0, (1.0, 0.0, -1.0), 1.5)
+    ref = op.collide(f, with_loss=True)
+    sm, col = _op((64, 4, 6, 0.7, 0.7, 1.0, L8_S * 1.25), "mixed")
+    assert rel_linf(col.collide(f, with_loss=True), ref) < 1e-5
+
+
+def test_full_size_properties_c2():
+    """128 cells x 32^3 (the 1D Riemann workload): quadratic scaling Q(2f) = 4 Q(f),
+    batch-order independence, single-cell equality, mixed vs FP64 agreement."""
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 32, 32, 0.8, 0.8, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    v = sm.v_center
+    nx = 128
+    x = (np.arange(nx) + 0.5) / nx
+    left = maxwellian(v, 1.0, (0, 0, 0), 1.0)
+    right = maxwellian(v, 0.125, (0, 0, 0), 0.8)
+    f = torch.as_tensor(np.stack([left if xi < 0.5 else right for xi in x]), device="cuda:0")
+    f += 1e-3 * torch.rand_like(f) * f
+    mixed = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=nx)
+    dbl = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=nx)
+    q = mixed.collide(f, with_loss=True)
+    q64 = dbl.collide(f, with_loss=True)
+    err = (q - q64).abs().amax(dim=(1, 2, 3)) / q64.abs().amax(dim=(1, 2, 3))
+    assert float(err.max()) < 1e-5
+    q2 = mixed.collide(2 * f, with_loss=True)
+    assert float((q2 - 4 * q).abs().max() / (4 * q).abs().max()) < 1e-6
+    perm = torch.randperm(nx, device="cuda:0")
+    qp = mixed.collide(f[perm].contiguous(), with_loss=True)
+    assert torch.equal(qp, q[perm])
+    q7 = mixed.collide(f[7:8].contiguous(), with_loss=True)  # other pair chunking: rounding only
+    assert float((q7[0] - q[7]).abs().max() / q[7].abs().max()) < 1e-6
+
+
+def test_mass_fix_conserves_mass_fp32():
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 32, 32, 0.9, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", mass_fix=True)
+    f = 0.5 * (maxwellian(sm.v_center, 1, (2, 0, 0), 1) + maxwellian(sm.v_center, 1, (-2, 0, 0), 1))
+    q = col.collide(f, with_loss=True)
+    dv = sm.delta**3
+    assert abs(q.sum() * dv) / (f.sum() * dv) < 1e-6
+    # and the uncorrected operator, checked against the oracle's correction
+    from oracle import fs_inelastic as fo
+
+    raw = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed").collide(f, with_loss=True)
+    assert rel_linf(q, fo.mass_mode_correction(raw)) < 1e-6
+
+
+def test_cooling_law_gpu():
+    """Maxwell molecules: -dT/dt / (rho T (1 - e^2)) = 1/4."""
+    pkg = _pkg()
+    for e in (0.9, 0.5):
+        cfg = op_config(32, L8_S, 16, 32, e, e, 0.0)
+        sm = pkg.SpectralMesh(cfg)
+        col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed")
+        v = sm.v_center
+        f = maxwellian(v, 1.0, (0.0, 0.0, 0.0), 1.0)
+        q = col.collide(f, with_loss=True)
+        V = np.meshgrid(v, v, v, indexing="ij")
+        dv = sm.delta**3
+        rho = f.sum() * dv
+        dE = 0.5 * (q * (V[0] ** 2 + V[1] ** 2 + V[2] ** 2)).sum() * dv
+        E = 0.5 * (f * (V[0] ** 2 + V[1] ** 2 + V[2] ** 2)).sum() * dv
+        T = (2 / 3) * E / rho
+        drho = q.sum() * dv
+        dT = (2 / 3) * (dE / rho - E * drho / rho**2)
+        k = -dT / (rho * T * (1 - e**2))
+        assert abs(k - 0.25) < 5e-3, (e, k)
+
+
+def test_c_abi_errors_on_gpu():
+    pkg = _pkg()
+    lib = pkg._lib.load()
+    sm, col = _op((8, 4, 6, 0.9, 0.9, 1.0, L8_S), "mixed", batch_max=2)
+    plan = col.plan
+    f = torch.zeros((3, 8, 8, 8), dtype=torch.float64, device="cuda:0")
+    q = torch.empty_like(f)
+    st = lib.pii_collide(plan.handle, f.data_ptr(), q.data_ptr(), 3, 1, 0.0, 0, None)
+    assert st == pkg._lib.PII_ERR_SIZE
+    st = lib.pii_collide(plan.handle, f.data_ptr(), f.data_ptr(), 1, 1, 0.0, 0, None)
+    assert st == pkg._lib.PII_ERR_ARG
+    v = np.ascontiguousarray(sm.v_center)
+    st = lib.pii_transport_df(plan.handle, f.data_ptr(), q.data_ptr(), 2, 1e-3, 0.1, pkg._lib.dptr(v), 7, 1, None)
+    assert st == pkg._lib.PII_ERR_ARG and "Boundary condition" in pkg._lib.last_error()
+    # the plan keeps working after rejected calls
+    st = lib.pii_collide(plan.handle, f.data_ptr(), q.data_ptr(), 2, 1, 0.0, 0, None)
+    assert st == pkg._lib.PII_OK
+    torch.cuda.synchronize()
+    assert float(q[:2].abs().max()) == 0.0  # Q(0) = 0; cell 2 was not part of the call

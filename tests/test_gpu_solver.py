@@ -1,0 +1,160 @@
+"""GPU parity of the transport step and the Euler / PFE / TPI2 / TPI3 integrators."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import L8_S, maxwellian, op_config, rel_linf
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _pkg():
+    import proj_int_inelastic_gb300 as pkg
+
+    return pkg
+
+
+def test_transport_golden(golden):
+    pkg = _pkg()
+    d = golden("transport.npz")
+    v = d["v"]
+    for bc, code in (("extrap", pkg.BC.extrap), ("periodic", pkg.BC.periodic)):
+        solver = pkg.BoltzmannSolver1D(1.0)
+        solver.all_bcs = code
+        sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": 8.0, "nx": 12, "nv": 8})
+        sol.state.f.copy_(torch.as_tensor(d[f"{bc}_f"]))
+        assert abs(sol.state.delta[0] - float(d[f"{bc}_dx"])) < 1e-15
+        assert np.array_equal(sol.state.v, v)
+        for j in range(2):
+            df = solver.df_advection(sol.state, float(d[f"{bc}_dt{j}"]))
+            assert rel_linf(df.cpu().numpy(), d[f"{bc}_df{j}"]) < 1e-12, (bc, j)
+
+
+RUNS = [("pfe", "PFE", "extrap"), ("pfe_full", "PFE", "extrap"), ("tpi2", "TPI2", "periodic"),
+        ("tpi3", "TPI3", "periodic"), ("euler", "Euler", "extrap")]
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+@pytest.mark.parametrize("name,integ,bc", RUNS)
+def test_solver1d_golden(golden, name, integ, bc, precision, use_graph):
+    pkg = _pkg()
+    d = golden("solver1d.npz")
+    nv, nr, ns, e, e0, g, s, nx = d["params"]
+    cfg = op_config(nv, s, nr, ns, e, e0, g)
+    sm = pkg.SpectralMesh(cfg)
+    with_loss = name.endswith("_full") or name == "tpi3"
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, with_loss=with_loss)
+    dt, tend, kn, dx = d[f"{name}_meta"]
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": int(nx), "nv": int(nv)})
+    sol.state.f.copy_(torch.as_tensor(d[f"{name}_f0"]))
+    solver = pkg.BoltzmannSolver1D(float(kn), collision_operator=col)
+    solver.all_bcs = pkg.BC.extrap if bc == "extrap" else pkg.BC.periodic
+    solver.time_integrator = integ
+    solver.inner_steps = [int(k) for k in d[f"{name}_K"]]
+    solver.inner_dt = [float(h) for h in d[f"{name}_h"]]
+    solver.dt = float(dt)
+    solver.use_graph = use_graph
+    solver.evolve_to_time(sol, float(tend))
+    torch.cuda.synchronize()
+    tol = 1e-11 if precision == "double" else 1e-5
+    assert rel_linf(sol.f.cpu().numpy(), d[f"{name}_f"]) < tol
+    assert abs(sol.t - float(tend)) < 1e-12
+
+
+def test_generic_collision_callable_path(golden):
+    """A plain callable as collision_operator steps through the Python nesting."""
+    pkg = _pkg()
+    d = golden("solver1d.npz")
+    nv, nr, ns, e, e0, g, s, nx = d["params"]
+    cfg = op_config(nv, s, nr, ns, e, e0, g)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="double")
+    dt, tend, kn, dx = d["tpi3_meta"]
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": int(nx), "nv": int(nv)})
+    sol.state.f.copy_(torch.as_tensor(d["tpi3_f0"]))
+    solver = pkg.BoltzmannSolver1D(float(kn), collision_operator=lambda f: col.collide(f, with_loss=True))
+    solver.all_bcs = pkg.BC.periodic
+    solver.time_integrator = "TPI3"
+    solver.inner_steps = [int(k) for k in d["tpi3_K"]]
+    solver.inner_dt = [float(h) for h in d["tpi3_h"]]
+    solver.dt = float(dt)
+    solver.evolve_to_time(sol, float(tend))
+    assert rel_linf(sol.f.cpu().numpy(), d["tpi3_f"]) < 1e-11
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_euler_c32_temperature_history(golden, precision):
+    """100 forward-Euler steps of the homogeneous two-beam problem (n = 32, 32 x 32
+    quadrature, e = 0.9, hard spheres): T(t) and final f against the reference."""
+    pkg = _pkg()
+    c = golden("op_c32.npz")
+    d = golden("euler_c32.npz")
+    nv, nr, ns, e, e0, g, s = c["params"]
+    cfg = op_config(nv, s, nr, ns, e, e0, g)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, with_loss=True)
+    sol = pkg.Solution({"dim_x": 0, "dim_v": 3, "l": sm.L, "nv": 32})
+    sol.state.f.copy_(torch.as_tensor(c["f"]))
+    solver = pkg.BoltzmannSolver0D(1.0, collision_operator=col)
+    solver.dt = float(d["dt"])
+    T = [float(sol.state.T)]
+    for _ in range(int(d["nsteps"])):
+        solver.evolve_to_time(sol)  # one step
+        T.append(float(sol.state.T))
+    T = np.array(T)
+    tol = 1e-11 if precision == "double" else 1e-5
+    assert np.abs(T - d["T"]).max() / d["T"].max() < tol
+    assert rel_linf(sol.f.cpu().numpy(), d["f_final"]) < (1e-10 if precision == "double" else 1e-5)
+
+
+def test_moments_vs_oracle():
+    pkg = _pkg()
+    from oracle import integrators as it
+
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": 8.0, "nx": 3, "nv": 16})
+    v = sol.state.v
+    f = np.stack([maxwellian(v, r, u, T) for r, u, T in ((1, (0, 0, 0), 1), (0.5, (1, -1, 0.5), 2), (2, (0, 2, 0), 0.7))])
+    sol.state.f.copy_(torch.as_tensor(f))
+    rho, u, T = sol.state.moments()
+    ref = it.moments(f, v, sol.state.dv)
+    assert np.abs(rho - ref["rho"]).max() < 1e-13
+    assert np.abs(u - ref["u"]).max() < 1e-12
+    assert np.abs(T - ref["T"]).max() < 1e-12
+
+
+def test_pfe_c2_full_size_mass_and_parity():
+    """The 1D Riemann workload at full size (128 cells x 32^3, e = 0.8, kn = 1e-2,
+    PFE K = 2): one macro-step in mixed precision vs FP64 on the GPU, and mass
+    conservation of the mass-fixed operator with outflow data (cells far from the
+    boundary)."""
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 32, 32, 0.8, 0.8, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    nx = 128
+    x = (np.arange(nx) + 0.5) / nx
+    v = sm.v_center
+    left, right = maxwellian(v, 1.0, (0, 0, 0), 1.0), maxwellian(v, 0.125, (0, 0, 0), 0.8)
+    f0 = torch.as_tensor(np.stack([left if xi < 0.5 else right for xi in x]), device="cuda:0")
+    out = {}
+    for prec in ("mixed", "double"):
+        col = pkg.FSInelasticVHSCollision(cfg, sm, precision=prec, with_loss=True, mass_fix=True, batch_max=nx)
+        sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": nx, "nv": 32})
+        sol.state.f.copy_(f0)
+        solver = pkg.BoltzmannSolver1D(1e-2, collision_operator=col)
+        solver.all_bcs = pkg.BC.extrap
+        solver.time_integrator = "PFE"
+        solver.inner_steps = [2]
+        h = 4.0e-4  # CFL 0.5 bound: 0.5 dx / v_max
+        solver.inner_dt = [h]
+        solver.dt = 4 * h
+        rho0 = sol.state.rho
+        solver.evolve_to_time(sol, 4 * h)
+        out[prec] = (sol.f.clone(), rho0, sol.state.rho)
+    fm, fd = out["mixed"][0], out["double"][0]
+    assert float((fm - fd).abs().max() / fd.abs().max()) < 1e-5
+    rho0, rho1 = out["mixed"][1], out["mixed"][2]
+    # total mass changes only by the boundary fluxes; interior cells far from x = 0.5 keep rho
+    assert abs(rho1[:20].mean() - rho0[:20].mean()) / rho0[:20].mean() < 1e-6
