@@ -1,0 +1,504 @@
+#!/usr/bin/env python
+"""Benchmark: Q(f,f) cell-evaluations per second on the 1D Riemann workload.
+
+Workload (one step = one projective forward-Euler macro-step): n_x = 128
+cells on [0, 1] with outflow (extrapolation) ghost cells, Sod data
+(rho = 1, T = 1 | rho = 0.125, T = 0.8, zero velocity, local Maxwellians),
+velocity grid 32^3 on [-8, 8]^3, 32 Gauss-Legendre radial nodes x the
+32-point symmetric spherical design, hard spheres, e = e0 = 0.8,
+kn = 1e-2, K = 2 inner steps of dt0 = 4e-4 (CFL 0.40) and macro-step 2e-3.
+Each step evaluates Q(f,f) (gain - loss) twice on every cell: 256
+cell-evaluations per step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Under torchrun (N > 1) every rank runs an
+independent replica (the operator has no data-path collective; cells shard
+with a 2-cell halo, which a single-GPU pool cannot exercise).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Q(f,f) cell-evals/s at N_v=32³/64³, mixed vs FP64 GPU at ≤1e-5 rel L∞ err"
+UNIT = "cell-evals/s"
+NX, NV, NR, NS = 128, 32, 32, 32
+S_L8 = 16.0 / (3.0 + math.sqrt(2.0))
+E = 0.8
+KN = 1e-2
+K_INNER, DT0, DT = 2, 4e-4, 2e-3
+CELL_EVALS_PER_STEP = K_INNER * NX
+WORKLOAD = (f"1D Riemann (Sod) PFE macro-step: n_x={NX} cells, N_v={NV}^3 on [-8,8]^3, {NR} GL radial x {NS} "
+            f"symmetric spherical design, hard spheres, e=e0={E}, kn={KN}, K={K_INNER} inner steps dt0={DT0}, "
+            f"macro dt={DT}, Q = gain - loss")
+
+
+def op_config():
+    return {
+        "velocity-mesh": {"nv": NV, "s": S_L8, "nr": NR},
+        "spherical-design-rule": {"ssrule": "womersley", "nsphr": NS},
+        "collision-model": {"dim": 3, "type": "vhs", "e": E, "e0": E, "gamma": 1.0},
+    }
+
+
+def maxwellian(v, rho, u, T):
+    import numpy as np
+
+    V = np.meshgrid(v, v, v, indexing="ij")
+    d2 = (V[0] - u[0]) ** 2 + (V[1] - u[1]) ** 2 + (V[2] - u[2]) ** 2
+    return rho / (2 * math.pi * T) ** 1.5 * np.exp(-d2 / (2 * T))
+
+
+def sod_state(v):
+    import numpy as np
+
+    x = (np.arange(NX) + 0.5) / NX
+    left = maxwellian(v, 1.0, (0, 0, 0), 1.0)
+    right = maxwellian(v, 0.125, (0, 0, 0), 0.8)
+    return np.stack([left if xi < 0.5 else right for xi in x])
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        out.update(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows),
+                   power_w_max=max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None))
+        return out
+
+
+# ---------------------------------------------------------------------------
+# the plain FP64 GPU implementation of the same method (torch.fft complex128),
+# the reference's broadcast evaluation (src/collision/inelastic_collisions.py:208-227)
+# ---------------------------------------------------------------------------
+class TorchFP64Operator:
+    def __init__(self, mesh, device):
+        import numpy as np
+        import torch
+
+        n = mesh.nv
+        r, wr = mesh.rquad()
+        sigma, wsig = mesh.circ_or_sphr_quad()
+        idx = np.fft.fftshift(np.arange(-n // 2, n // 2)).astype(np.float64)
+        t = lambda a: torch.as_tensor(a, device=device)
+        kx, ky, kz = torch.meshgrid(t(idx), t(idx), t(idx), indexing="ij")
+        knorm = torch.sqrt(kx**2 + ky**2 + kz**2)
+        sig = t(sigma)
+        kdots = sig[:, 0, None, None, None] * kx + sig[:, 1, None, None, None] * ky + sig[:, 2, None, None, None] * kz
+        rr = t(r)[:, None, None, None, None]
+        er = 0.5 * (E - E) * np.tanh(r - 0.5 * mesh.R) + 0.5 * (E + E)
+        a = t(0.25 * math.pi * (1 + er) / mesh.L)[:, None, None, None, None]
+        pre = 4 * math.pi * rr ** 3.0
+        sinc = lambda x: torch.where(x == 0, torch.ones_like(x), torch.sin(x) / torch.where(x == 0, torch.ones_like(x), x))
+        self.gain = pre * torch.exp(1j * a * rr * kdots) * sinc(a * rr * knorm) * t(wr)[:, None, None, None, None] * wsig
+        self.exp = torch.exp(-1j * math.pi * rr * kdots / mesh.L)
+        loss = 4 * math.pi * t(r) ** 3.0 * t(wr)
+        self.loss = loss[:, None, None, None]
+        self.sp = sinc(math.pi * t(r)[:, None, None, None] * knorm / mesh.L)
+
+    def collide(self, f):
+        import torch
+
+        fft = lambda x: torch.fft.fftn(x, dim=(-3, -2, -1))
+        ifft = lambda x: torch.fft.ifftn(x, dim=(-3, -2, -1))
+        fh = fft(f)
+        gain_hat = fft(ifft(self.exp * fh) * f)
+        gain_hat *= self.gain
+        gain = ifft(gain_hat.sum(dim=(0, 1)))
+        loss = (ifft(self.sp * fh) * (self.loss * f)).sum(dim=0)
+        return (gain / (4 * math.pi) - loss).real
+
+
+def time_torch_fp64(mesh, f_dev, cells, device):
+    import torch
+
+    op = TorchFP64Operator(mesh, device)
+    fc = f_dev[:cells].to(torch.complex128)
+    op.collide(fc[0])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for c in range(cells):
+        op.collide(fc[c])
+    e1.record()
+    torch.cuda.synchronize()
+    return cells / (e0.elapsed_time(e1) / 1e3)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle restatement of the reference operator, host cores)
+# ---------------------------------------------------------------------------
+def cpu_baseline(budget_s=15.0, max_cells=16):
+    import numpy as np
+
+    from oracle import fs_inelastic as fo
+
+    workers = os.cpu_count() or 1
+    m = fo.Mesh(NV, S_L8, NR, NS)
+    op = fo.FSInelasticVHS(m, E, E, 1.0)
+    f = sod_state(m.v)
+    picks = [0, NX - 1]
+    op.collide_cell(f[0], True, workers)  # warm-up (tables, FFT plans)
+    t0 = time.perf_counter()
+    done = 0
+    while done < max_cells and (time.perf_counter() - t0) < budget_s:
+        op.collide_cell(f[picks[done % 2]], True, workers)
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"{done} single-cell Q(f,f) (gain - loss) evaluations of the Sod state (left/right cells), "
+                      f"FP64 NumPy/SciPy restatement of the reference operator, scipy.fft workers={workers}, "
+                      f"{dt:.1f} s"}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(n_gpus):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    from oracle import fs_inelastic as fo
+
+    workers = os.cpu_count() or 1
+    m = fo.Mesh(NV, S_L8, NR, NS)
+    op = fo.FSInelasticVHS(m, E, E, 1.0)
+    f = sod_state(m.v)
+    cells = [0, NX - 1]
+    for w in range(args.warmup):
+        op.collide_cell(f[cells[w % 2]], True, workers)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        op.collide_cell(f[cells[k % 2]], True, workers)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "reference_step": "one Q(f,f) cell-evaluation of the workload "
+                   "(bounded sample: alternating left/right Sod cells)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+                         "sample": f"{args.steps} single-cell Q(f,f) evaluations, FP64 NumPy/SciPy restatement of "
+                                   f"the reference operator (the reference itself cannot run on the GPU box: "
+                                   f"pyfftw/cupy absent), scipy.fft workers={workers}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def ncu_case(cells):
+    """Small profiling case: 3 mixed-precision Q(f,f) evaluations on `cells` cells."""
+    import torch
+
+    import proj_int_inelastic_gb300 as pkg
+
+    cfg = op_config()
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=cells)
+    f = torch.as_tensor(sod_state(sm.v_center)[:cells], device="cuda:0").contiguous()
+    for _ in range(3):
+        q = col.collide(f, with_loss=True)
+    torch.cuda.synchronize()
+    print(json.dumps({"ncu_case_cells": cells, "q_abs_max": float(q.abs().max())}))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--ncu-case", type=int, default=0,
+                    help="profiling case: run 3 Q(f,f) evaluations on this many cells of the workload and exit")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.ncu_case:
+        return ncu_case(args.ncu_case)
+    args.warmup = max(3, args.warmup)
+
+    import numpy as np
+    import torch
+
+    world, rank, local, dist = dist_setup(args.gpus)
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    import proj_int_inelastic_gb300 as pkg
+
+    lib = pkg._lib.load()
+    cfg = op_config()
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=NX, device=local)
+    f0_host = sod_state(sm.v_center)
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": NX, "nv": NV},
+                       device=local)
+    sol.state.f.copy_(torch.as_tensor(f0_host))
+    solver = pkg.BoltzmannSolver1D(KN, collision_operator=col)
+    solver.all_bcs = pkg.BC.extrap
+    solver.time_integrator = "PFE"
+    solver.inner_steps = [K_INNER]
+    solver.inner_dt = [DT0]
+    solver.dt = DT
+    solver.setup(sol)
+
+    def step():
+        solver.step(sol, False, 0.0, DT)
+
+    for _ in range(args.warmup):
+        step()
+    stream = solver._get_stream(device)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)  # > 129 MB L2
+
+    # ---------------- timed region: device time of K macro-steps -------------
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.pii_kernel_launches()
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()  # L2 flush between timed steps (outside the event pair)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            evs.append((a, b))
+    torch.cuda.synchronize()
+    launches = lib.pii_kernel_launches() - launches0
+    if dist:
+        dist.barrier()
+    ck = clocks.stop()
+    total_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    if dist:
+        t = torch.tensor([total_s], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t)
+    value = world * CELL_EVALS_PER_STEP * args.steps / total_s
+    ms_per_step = total_s / args.steps * 1e3
+
+    # ---------------- e2e: host f in, host f out, through the solver API -------
+    pin_in = torch.empty(sol.f.shape, dtype=torch.float64).pin_memory()
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    pin_in.copy_(torch.as_tensor(f0_host))
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sol.state.f.copy_(pin_in, non_blocking=True)
+        step()
+        pin_out.copy_(sol.state.f, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t)
+    nbytes = sol.f.numel() * 8
+    e2e = {"value": world * CELL_EVALS_PER_STEP * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes,
+           "path": "pinned host f -> device, BoltzmannSolver1D.step (PFE macro-step), device f -> pinned host"}
+
+    # ---------------- attribution: per-kernel CUDA-event timing ---------------
+    plan = col.plan
+    lib.pii_plan_profile(plan.handle, 1)
+    with torch.cuda.stream(stream):
+        step()
+    ms = (pkg._lib.ctypes.c_double * pkg._lib.NSTAGES)()
+    cnt = (pkg._lib.ctypes.c_int64 * pkg._lib.NSTAGES)()
+    lib.pii_plan_profile_read(plan.handle, ms, cnt)
+    lib.pii_plan_profile(plan.handle, 0)
+    stages = {pkg._lib.STAGES[i]: {"ms": ms[i], "launches": int(cnt[i])} for i in range(pkg._lib.NSTAGES) if cnt[i]}
+    tot = sum(v["ms"] for v in stages.values())
+    for v in stages.values():
+        v["share"] = v["ms"] / tot if tot else None
+    dom = max(stages, key=lambda k: stages[k]["ms"])
+    # algorithmic FLOPs: one 1D pass over a grid = 5 N log2(n); items = (cell, pair)
+    N = NV**3
+    items_per_collide = NX * NR * NS
+    pass_flops = 5.0 * N * math.log2(NV)
+    per_item = {"pair_plane": 4 * pass_flops + 2 * N, "col_pstart": pass_flops + 12 * N,
+                "col_pend": pass_flops + 14 * N, "reduce": 2 * N}
+    collides = K_INNER
+    if dom in per_item:
+        flops_total = per_item[dom] * items_per_collide * collides
+    else:
+        flops_total = None
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, FP32 FMA lanes x clock
+    roof = {"kernel": dom, "bound": "fp32", "unit": "TFLOP/s", "peak": fp32_peak,
+            "peak_source": f"152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz={sm_max:.0f} (MEASURED_PEAKS.json); "
+                           "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
+            "launches_per_step": stages[dom]["launches"], "avg_launch_ms": stages[dom]["ms"] / stages[dom]["launches"]}
+    if flops_total:
+        per_launch = flops_total / stages[dom]["launches"]
+        roof["achieved"] = per_launch / (roof["avg_launch_ms"] / 1e3) / 1e12
+        roof["frac"] = roof["achieved"] / fp32_peak
+        roof["algorithmic_flops_per_launch"] = per_launch
+    else:
+        roof["achieved"] = roof["frac"] = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    roof["traffic"] = None
+    if os.path.exists(tfile):
+        tr = json.load(open(tfile))
+        if dom in tr:
+            roof["traffic"] = tr[dom].get("dram_bytes_per_launch")
+            roof["traffic_source"] = tr[dom].get("source")
+    # whole-step FLOP rate (algorithmic F per cell-eval, survey formula) for context
+    F_cell = (2 * NR * NS + NR + 2) * 5 * N * math.log2(N) + 16 * NR * NS * N
+    roof["step_algorithmic_tflops"] = F_cell * value / world / 1e12
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "precision": "FP32 FFTs and quadrature sums; FP64 state, increments, extrapolation",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": NX, "n_v": NV, "n_r": NR, "n_sigma": NS,
+                   "cell_evals_per_step": CELL_EVALS_PER_STEP, "l2": "flushed (256 MB write) between timed steps",
+                   "graph": "each macro-step replayed as one CUDA graph", "parallelism": f"replicas x{world}"},
+        "clocks": ck, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "kernels": stages, "hbm_peak_gbs": hbm_peak,
+    }
+
+    # ---------------- comparators (rank 0, N = 1 legs) -------------------------
+    if rank == 0 and not args.no_fp64:
+        f_dev = sol.state.f.new_tensor(f0_host)
+        dbl = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", with_loss=True, batch_max=NX, device=local)
+        qm = col.collide(f_dev, with_loss=True)
+        q64 = dbl.collide(f_dev, with_loss=True)
+        err = (qm - q64).abs().amax(dim=(1, 2, 3)) / q64.abs().amax(dim=(1, 2, 3))
+        line["rel_linf_err_vs_fp64"] = float(err.max())
+        plan64 = dbl.plan
+        q = torch.empty_like(f_dev)
+        cells64 = 16
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        st = lib.pii_collide(plan64.handle, f_dev.data_ptr(), q.data_ptr(), cells64, 1, 0.0, 0,
+                             torch.cuda.current_stream().cuda_stream)
+        b.record()
+        torch.cuda.synchronize()
+        pkg._lib.check(st, "pii_collide fp64")
+        pii64 = cells64 / (a.elapsed_time(b) / 1e3)
+        dbl.close()
+        try:
+            torch64 = time_torch_fp64(sm, f_dev, 4, device)
+        except Exception as ex:  # noqa: BLE001
+            torch64 = None
+            line["fp64_torch_error"] = str(ex)[:200]
+        collide_rate = None
+        # collide-only throughput of the mixed path on the full batch (device time)
+        qm2 = torch.empty_like(f_dev)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(3):
+            lib.pii_collide(col.plan.handle, f_dev.data_ptr(), qm2.data_ptr(), NX, 1, 0.0, 0,
+                            torch.cuda.current_stream().cuda_stream)
+        b.record()
+        torch.cuda.synchronize()
+        collide_rate = 3 * NX / (a.elapsed_time(b) / 1e3)
+        line["fp64_gpu"] = {
+            "torch_fft_complex128": torch64,
+            "pii_fp64_kernels": pii64,
+            "unit": UNIT,
+            "what": "Q(f,f) gain - loss on the workload's cells: the reference's broadcast method in "
+                    "torch.fft complex128 (4 cells), and this library's kernels in FP64 (16 cells)",
+        }
+        line["mixed_collide_only"] = collide_rate
+        if torch64:
+            line["speedup_vs_fp64_gpu"] = collide_rate / torch64
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

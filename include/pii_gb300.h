@@ -135,6 +135,22 @@ int pii_moments(pii_plan* plan, const double* f, double* out, int64_t cells, con
  * f += M_l * df_l, src/boltzmann.py:128,138-140,154-158). */
 int pii_axpby(double* f, const double* d, double a, double b, int64_t count, void* stream);
 
+/*
+ * Instrumentation (no reference counterpart).
+ * pii_kernel_launches: number of kernels this library has enqueued in the
+ * process (eager launches, plus the kernel nodes of every CUDA-graph replay).
+ * pii_plan_profile(plan, 1) starts per-stage CUDA-event timing of the plan's
+ * eager launches (graph capture is bypassed while it is on);
+ * pii_plan_profile_read fills ms[PII_NSTAGES] (summed device time) and
+ * launches[PII_NSTAGES] after synchronising, and resets the counters.
+ */
+#define PII_NSTAGES 11
+/* stage order: fwd_plane, col_fwd, col_pstart, pair_plane, col_pend, reduce,
+ * col_iprep, finish, df, axpy, massfix */
+int64_t pii_kernel_launches(void);
+int pii_plan_profile(pii_plan* plan, int enable);
+int pii_plan_profile_read(pii_plan* plan, double* ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

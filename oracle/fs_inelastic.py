@@ -108,6 +108,9 @@ class FSInelasticVHS:
         self.kdotsig = idx_mesh
         # loss (:109-114)
         self.loss_kern = self.pre_fac(r) * mesh.wr
+        # the reference precomputes every table once (:57-137); cache them up to ~4 GB
+        self._cache = {}
+        self._cache_ok = 2 * mesh.nr * mesh.nsphr * mesh.nv**3 * 16 <= (4 << 30)
 
     def pre_fac(self, r):
         return self.sphr_fac * r ** (self.gamma + 3 - 1)  # :54-55
@@ -118,6 +121,14 @@ class FSInelasticVHS:
 
     def tables_r(self, ir):
         """Gain and exp tables of radial node ``ir``: (n_sigma, n, n, n) complex128 (:91-105)."""
+        if ir in self._cache:
+            return self._cache[ir]
+        out = self._tables_r(ir)
+        if self._cache_ok:
+            self._cache[ir] = out
+        return out
+
+    def _tables_r(self, ir):
         r = self.m.r[ir]
         wr = self.m.wr[ir]
         a = self.exp_fac[ir]

@@ -73,7 +73,7 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
   int st = p->precision == PII_PREC_FP32 ? collide_n<float>(p, f, q, cells, with_loss, hb, s)
                                          : collide_n<double>(p, f, q, cells, with_loss, hb, s);
   if (st != PII_OK) return st;
-  if (mass_fix) PII_TRY(mass_fix_impl(q, cells, p->N, s));
+  if (mass_fix) PII_TRY(mass_fix_impl(p, q, cells, p->N, s));
   return PII_OK;
 }
 

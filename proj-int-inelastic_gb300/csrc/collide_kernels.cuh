@@ -385,13 +385,19 @@ int CollideKernels<T, NV>::fwd(pii_plan* p, const double* f, int64_t c0, int64_t
   const int64_t nplanes = cells * NV;
   V* fhat = reinterpret_cast<V*>(p->fhat) + c0 * N3;
   T* fT = reinterpret_cast<T*>(p->fT) + c0 * N3;
-  k_fwd_plane<T, NV><<<unsigned((nplanes + PPB - 1) / PPB), Geo<NV>::THREADS, smem, s>>>(f + c0 * N3, fhat,
-                                                                                         fT, nplanes);
+  {
+    StageTimer st(p, ST_FWD_PLANE, s);
+    k_fwd_plane<T, NV><<<unsigned((nplanes + PPB - 1) / PPB), Geo<NV>::THREADS, smem, s>>>(f + c0 * N3, fhat, fT,
+                                                                                           nplanes);
+  }
   PII_CHECK_LAUNCH();
   ColArgs a = col_args<T, NV>(p);
   a.dst = fhat;
   a.items = cells;
-  k_col<T, NV, COL_FWD><<<unsigned((cells * N2 + 127) / 128), 128, 0, s>>>(a);
+  {
+    StageTimer st(p, ST_COL_FWD, s);
+    k_col<T, NV, COL_FWD><<<unsigned((cells * N2 + 127) / 128), 128, 0, s>>>(a);
+  }
   PII_CHECK_LAUNCH();
   return PII_OK;
 }
@@ -411,16 +417,28 @@ int CollideKernels<T, NV>::pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t
   a.p0 = p0;
   a.np = np;
   const unsigned colblocks = unsigned((items * N2 + 127) / 128);
-  k_col<T, NV, COL_PSTART><<<colblocks, 128, 0, s>>>(a);
+  {
+    StageTimer st(p, ST_COL_PSTART, s);
+    k_col<T, NV, COL_PSTART><<<colblocks, 128, 0, s>>>(a);
+  }
   PII_CHECK_LAUNCH();
   const int64_t nplanes = items * NV;
-  k_pair_plane<T, NV><<<unsigned((nplanes + PPB - 1) / PPB), Geo<NV>::THREADS, smem, s>>>(
-      reinterpret_cast<V*>(p->buf), reinterpret_cast<const T*>(p->fT), c0, np, nplanes);
+  {
+    StageTimer st(p, ST_PAIR_PLANE, s);
+    k_pair_plane<T, NV><<<unsigned((nplanes + PPB - 1) / PPB), Geo<NV>::THREADS, smem, s>>>(
+        reinterpret_cast<V*>(p->buf), reinterpret_cast<const T*>(p->fT), c0, np, nplanes);
+  }
   PII_CHECK_LAUNCH();
-  k_col<T, NV, COL_PEND><<<colblocks, 128, 0, s>>>(a);
+  {
+    StageTimer st(p, ST_COL_PEND, s);
+    k_col<T, NV, COL_PEND><<<colblocks, 128, 0, s>>>(a);
+  }
   PII_CHECK_LAUNCH();
-  k_reduce<T><<<unsigned((cells * N3 + 255) / 256), 256, 0, s>>>(
-      reinterpret_cast<V*>(p->G), reinterpret_cast<const V*>(p->buf), c0, cells, np, N3, first ? 1 : 0);
+  {
+    StageTimer st(p, ST_REDUCE, s);
+    k_reduce<T><<<unsigned((cells * N3 + 255) / 256), 256, 0, s>>>(
+        reinterpret_cast<V*>(p->G), reinterpret_cast<const V*>(p->buf), c0, cells, np, N3, first ? 1 : 0);
+  }
   PII_CHECK_LAUNCH();
   return PII_OK;
 }
@@ -438,11 +456,17 @@ int CollideKernels<T, NV>::finish(pii_plan* p, const double* f, double* q, int64
   a.items = cells;
   a.c0 = c0;
   a.hb = hb;
-  k_col<T, NV, COL_IPREP><<<unsigned((cells * N2 + 127) / 128), 128, 0, s>>>(a);
+  {
+    StageTimer st(p, ST_COL_IPREP, s);
+    k_col<T, NV, COL_IPREP><<<unsigned((cells * N2 + 127) / 128), 128, 0, s>>>(a);
+  }
   PII_CHECK_LAUNCH();
   const int64_t nplanes = cells * NV;
-  k_finish<T, NV><<<unsigned((nplanes + PPB - 1) / PPB), Geo<NV>::THREADS, smem, s>>>(
-      reinterpret_cast<const V*>(p->buf), f, q, c0, nplanes, with_loss);
+  {
+    StageTimer st(p, ST_FINISH, s);
+    k_finish<T, NV><<<unsigned((nplanes + PPB - 1) / PPB), Geo<NV>::THREADS, smem, s>>>(
+        reinterpret_cast<const V*>(p->buf), f, q, c0, nplanes, with_loss);
+  }
   PII_CHECK_LAUNCH();
   return PII_OK;
 }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <tuple>
@@ -13,6 +14,14 @@
 namespace pii {
 
 void set_error(const char* fmt, ...);
+
+// kernels enqueued by the library (eager launches + kernel nodes of graph replays)
+extern std::atomic<int64_t> g_launches;
+
+enum Stage {
+  ST_FWD_PLANE = 0, ST_COL_FWD, ST_COL_PSTART, ST_PAIR_PLANE, ST_COL_PEND, ST_REDUCE,
+  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_COUNT
+};
 
 #define PII_CUDA(call)                                                                    \
   do {                                                                                    \
@@ -25,6 +34,7 @@ void set_error(const char* fmt, ...);
 
 #define PII_CHECK_LAUNCH()                                                                 \
   do {                                                                                     \
+    ::pii::g_launches.fetch_add(1, std::memory_order_relaxed);                             \
     cudaError_t _e = cudaGetLastError();                                                   \
     if (_e != cudaSuccess) {                                                               \
       ::pii::set_error("%s:%d kernel launch: %s", __FILE__, __LINE__, cudaGetErrorString(_e)); \
@@ -71,6 +81,12 @@ struct GraphKey {
 struct GraphEntry {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  int64_t kernels = 0;  // kernel launches captured into the graph
+};
+
+struct ProfEvent {
+  int stage;
+  cudaEvent_t a, b;
 };
 
 }  // namespace pii
@@ -97,7 +113,25 @@ struct pii_plan {
   double* v1dev = nullptr;  // n first-axis velocities (device)
   int64_t bytes = 0;
   std::map<pii::GraphKey, pii::GraphEntry> graphs;
+  // per-stage CUDA-event profiling (pii_plan_profile)
+  bool prof = false;
+  std::vector<pii::ProfEvent> prof_events;
+  std::vector<cudaEvent_t> prof_pool;
+  double prof_ms[pii::ST_COUNT] = {0};
+  int64_t prof_n[pii::ST_COUNT] = {0};
 };
+
+namespace pii {
+// RAII: records a begin / end event pair around one launch when profiling is on
+struct StageTimer {
+  pii_plan* p;
+  int stage;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  StageTimer(pii_plan* p_, int stage_, cudaStream_t s_);
+  ~StageTimer();
+};
+}  // namespace pii
 
 namespace pii {
 
@@ -108,8 +142,9 @@ int prepare_impl(pii_plan* p);
 // transport.cu
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
                    double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);
-int mass_fix_impl(double* q, int64_t cells, int64_t N, cudaStream_t s);
-int axpby_impl(double* f, const double* d, double a, double b, int64_t count, cudaStream_t s);
+int mass_fix_impl(pii_plan* p, double* q, int64_t cells, int64_t N, cudaStream_t s);
+int axpy3_impl(pii_plan* p, double* f, const double* d, double s0, double s1, double s2, int64_t count,
+               cudaStream_t s);
 int upload_v1(pii_plan* p, const double* v1, cudaStream_t s);
 
 // per-precision, per-size kernels (collide_kernels_*.cu)

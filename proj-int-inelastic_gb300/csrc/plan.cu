@@ -17,6 +17,44 @@
 namespace pii {
 
 static thread_local char g_err[1024] = "";
+std::atomic<int64_t> g_launches{0};
+
+StageTimer::StageTimer(pii_plan* p_, int stage_, cudaStream_t s_) : p(p_), stage(stage_), s(s_) {
+  if (!p || !p->prof) return;
+  if (p->prof_pool.size() < 2) {
+    for (int i = 0; i < 64; ++i) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) == cudaSuccess) p->prof_pool.push_back(e);
+    }
+    if (p->prof_pool.size() < 2) return;
+  }
+  a = p->prof_pool.back();
+  p->prof_pool.pop_back();
+  b = p->prof_pool.back();
+  p->prof_pool.pop_back();
+  cudaEventRecord(a, s);
+}
+
+StageTimer::~StageTimer() {
+  if (!a) return;
+  cudaEventRecord(b, s);
+  p->prof_events.push_back(ProfEvent{stage, a, b});
+}
+
+static void prof_resolve(pii_plan* p) {
+  if (p->prof_events.empty()) return;
+  cudaDeviceSynchronize();
+  for (auto& e : p->prof_events) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
+      p->prof_ms[e.stage] += ms;
+      p->prof_n[e.stage] += 1;
+    }
+    p->prof_pool.push_back(e.a);
+    p->prof_pool.push_back(e.b);
+  }
+  p->prof_events.clear();
+}
 
 void set_error(const char* fmt, ...) {
   va_list ap;
@@ -99,6 +137,8 @@ static int alloc(pii_plan* p, void** dst, size_t bytes) {
 
 static void free_plan(pii_plan* p) {
   if (!p) return;
+  prof_resolve(p);
+  for (cudaEvent_t e : p->prof_pool) cudaEventDestroy(e);
   for (auto& kv : p->graphs) {
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
@@ -205,5 +245,32 @@ int pii_plan_destroy(pii_plan* plan) {
 }
 
 int64_t pii_plan_workspace_bytes(const pii_plan* plan) { return plan ? plan->bytes : -1; }
+
+int64_t pii_kernel_launches(void) { return pii::g_launches.load(); }
+
+int pii_plan_profile(pii_plan* plan, int enable) {
+  if (!plan) {
+    pii::set_error("pii_plan_profile: NULL plan");
+    return PII_ERR_ARG;
+  }
+  if (!enable) pii::prof_resolve(plan);
+  plan->prof = enable != 0;
+  return PII_OK;
+}
+
+int pii_plan_profile_read(pii_plan* plan, double* ms, int64_t* launches) {
+  if (!plan || !ms || !launches) {
+    pii::set_error("pii_plan_profile_read: NULL argument");
+    return PII_ERR_ARG;
+  }
+  pii::prof_resolve(plan);
+  for (int i = 0; i < pii::ST_COUNT; ++i) {
+    ms[i] = plan->prof_ms[i];
+    launches[i] = plan->prof_n[i];
+    plan->prof_ms[i] = 0;
+    plan->prof_n[i] = 0;
+  }
+  return PII_OK;
+}
 
 }  // extern "C"

@@ -14,7 +14,6 @@
 
 namespace pii {
 
-int axpy3_impl(double* f, const double* d, double s0, double s1, double s2, int64_t count, cudaStream_t s);
 int check_bcs(int lo, int hi);
 
 struct StepCtx {
@@ -33,7 +32,7 @@ static int df_into_d0(const StepCtx& c, double h) {
 }
 
 static int add(const StepCtx& c, double s0, double s1, double s2) {
-  return axpy3_impl(c.f, c.p->d0, s0, s1, s2, c.nx * c.p->N, c.s);
+  return axpy3_impl(c.p, c.f, c.p->d0, s0, s1, s2, c.nx * c.p->N, c.s);
 }
 
 static int step_body(const StepCtx& c, int integrator, double dt, const int* K, const double* h) {
@@ -159,14 +158,17 @@ int pii_step(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, c
     K[l] = inner_steps[l];
     h[l] = inner_dt[l];
   }
-  if (!use_graph || s == nullptr) return pii::step_body(c, integrator, dt, K, h);
+  if (!use_graph || s == nullptr || plan->prof) return pii::step_body(c, integrator, dt, K, h);
 
   pii::GraphKey key{integrator, f, nx, dt, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, need,
                     {K[0], K[1], K[2]}, {h[0], h[1], h[2]}, stream};
   auto it = plan->graphs.find(key);
   if (it == plan->graphs.end()) {
     PII_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = pii::g_launches.load();
     int st = pii::step_body(c, integrator, dt, K, h);
+    const int64_t captured = pii::g_launches.load() - before;
+    pii::g_launches.fetch_sub(captured);  // captured, not executed
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s, &g);
     if (st != PII_OK) {
@@ -179,6 +181,7 @@ int pii_step(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, c
     }
     pii::GraphEntry ge;
     ge.graph = g;
+    ge.kernels = captured;
     e = cudaGraphInstantiate(&ge.exec, g, 0);
     if (e != cudaSuccess) {
       cudaGraphDestroy(g);
@@ -188,6 +191,7 @@ int pii_step(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, c
     it = plan->graphs.emplace(key, ge).first;
   }
   PII_CUDA(cudaGraphLaunch(it->second.exec, s));
+  pii::g_launches.fetch_add(it->second.kernels);
   return PII_OK;
 }
 

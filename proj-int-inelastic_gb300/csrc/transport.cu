@@ -143,20 +143,30 @@ int transport_impl(pii_plan* p, const double* f, const double* q, double* df, in
   a.bc_lo = bc_lo;
   a.bc_hi = bc_hi;
   const int64_t total = nx * p->N;
-  k_df<<<unsigned((total + 255) / 256), 256, 0, s>>>(a);
+  {
+    StageTimer st(p, ST_DF, s);
+    k_df<<<unsigned((total + 255) / 256), 256, 0, s>>>(a);
+  }
   PII_CHECK_LAUNCH();
   return PII_OK;
 }
 
-int mass_fix_impl(double* q, int64_t cells, int64_t N, cudaStream_t s) {
-  k_massfix<<<unsigned(cells), 256, 0, s>>>(q, N);
+int mass_fix_impl(pii_plan* p, double* q, int64_t cells, int64_t N, cudaStream_t s) {
+  {
+    StageTimer st(p, ST_MASSFIX, s);
+    k_massfix<<<unsigned(cells), 256, 0, s>>>(q, N);
+  }
   PII_CHECK_LAUNCH();
   return PII_OK;
 }
 
-int axpy3_impl(double* f, const double* d, double s0, double s1, double s2, int64_t count, cudaStream_t s) {
+int axpy3_impl(pii_plan* p, double* f, const double* d, double s0, double s1, double s2, int64_t count,
+               cudaStream_t s) {
   if (count <= 0) return PII_OK;
-  k_axpy3<<<unsigned((count + 255) / 256), 256, 0, s>>>(f, d, s0, s1, s2, count);
+  {
+    StageTimer st(p, ST_AXPY, s);
+    k_axpy3<<<unsigned((count + 255) / 256), 256, 0, s>>>(f, d, s0, s1, s2, count);
+  }
   PII_CHECK_LAUNCH();
   return PII_OK;
 }
@@ -218,7 +228,7 @@ int pii_axpby(double* f, const double* d, double a, double b, int64_t count, voi
     pii::set_error("pii_axpby: invalid arguments");
     return PII_ERR_ARG;
   }
-  return pii::axpy3_impl(f, d, b, 1.0, a, count, (cudaStream_t)stream);
+  return pii::axpy3_impl(nullptr, f, d, b, 1.0, a, count, (cudaStream_t)stream);
 }
 
 }  // extern "C"
