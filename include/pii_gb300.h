@@ -136,6 +136,24 @@ int pii_moments(pii_plan* plan, const double* f, double* out, int64_t cells, con
 int pii_axpby(double* f, const double* d, double a, double b, int64_t count, void* stream);
 
 /*
+ * Q(f,f) without any allocation, for callers that cannot call cudaMalloc
+ * (while recording a CUDA graph, or under a host framework that owns all
+ * device memory).  No counterpart in the reference.  Same result as
+ * pii_collide in PII_PREC_FP32 (heat_bath = 0, mass_fix = 0), but the tables
+ * and workspace live in one static device array of 2.5 MiB that the library
+ * image reserves on every GPU that loads it.  Limits: n in {8, 16},
+ * cells <= 8, n_r <= 32, n_sigma <= 192, n_r * n_sigma <= 1024; larger
+ * requests return PII_ERR_SIZE.  All calls on a device share the array:
+ * calls whose GPU work overlaps race.  The first call on a device resolves
+ * the array's device address (cudaGetSymbolAddress) and must come before any
+ * stream capture.  f, q: device arrays of cells x n^3 FP64; r, w_r, sigma:
+ * host arrays as for pii_plan_create.
+ */
+int pii_collide_noalloc(const double* f, double* q, int64_t cells, int n, int n_r, int n_sigma, const double* r,
+                        const double* w_r, const double* sigma, double w_sigma, double L, double R, double e,
+                        double e0, double gamma, int with_loss, void* stream);
+
+/*
  * Instrumentation (no reference counterpart).
  * pii_kernel_launches: number of kernels this library has enqueued in the
  * process (eager launches, plus the kernel nodes of every CUDA-graph replay).

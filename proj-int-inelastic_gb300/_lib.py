@@ -46,6 +46,8 @@ SIGNATURES = {
                           _c_dbl, _c_int, _c_int, _c_int, _vp]),
     "pii_moments": (_c_int, [_vp, _vp, _vp, _c_i64, _pdbl, _c_dbl, _vp]),
     "pii_axpby": (_c_int, [_vp, _vp, _c_dbl, _c_dbl, _c_i64, _vp]),
+    "pii_collide_noalloc": (_c_int, [_vp, _vp, _c_i64, _c_int, _c_int, _c_int, _pdbl, _pdbl, _pdbl, _c_dbl, _c_dbl,
+                                     _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _vp]),
     "pii_kernel_launches": (_c_i64, []),
     "pii_plan_profile": (_c_int, [_vp, _c_int]),
     "pii_plan_profile_read": (_c_int, [_vp, _pdbl, ctypes.POINTER(ctypes.c_int64)]),
