@@ -397,8 +397,10 @@ def main():
     N = NV**3
     items_per_collide = NX * NR * NS
     pass_flops = 5.0 * N * math.log2(NV)
+    # per (cell, pair) item; the fused kernel does the whole pair (survey's per-pair term 2*5N log2 N + 16 N)
     per_item = {"pair_plane": 4 * pass_flops + 2 * N, "col_pstart": pass_flops + 12 * N,
-                "col_pend": pass_flops + 14 * N, "reduce": 2 * N}
+                "col_pend": pass_flops + 14 * N, "reduce": 2 * N,
+                "gain_cluster": 2 * 5.0 * N * math.log2(N) + 16 * N}
     collides = K_INNER
     if dom in per_item:
         flops_total = per_item[dom] * items_per_collide * collides

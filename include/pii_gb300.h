@@ -80,6 +80,14 @@ int pii_plan_destroy(pii_plan* plan);
 int64_t pii_plan_workspace_bytes(const pii_plan* plan);
 
 /*
+ * Kernel choice for the gain term of n = 32 FP32 plans (tuning knob, no
+ * reference counterpart): 1 = the fused 2-CTA-cluster kernel (the default
+ * where it exists), 0 = the column / plane pass pipeline used for every other
+ * size and for FP64.  Both compute the same operator.
+ */
+int pii_plan_set_gain_path(pii_plan* plan, int path);
+
+/*
  * q = Q+(f,f) [- Q-(f,f) if with_loss] [+ heat_bath * Lap_v f], per cell.
  * Replaces BaseCollision.__call__ (src/collision/base.py:32-58) and
  * FSInelasticVHSCollision.collide / laplacian
@@ -162,9 +170,9 @@ int pii_collide_noalloc(const double* f, double* q, int64_t cells, int n, int n_
  * pii_plan_profile_read fills ms[PII_NSTAGES] (summed device time) and
  * launches[PII_NSTAGES] after synchronising, and resets the counters.
  */
-#define PII_NSTAGES 11
+#define PII_NSTAGES 12
 /* stage order: fwd_plane, col_fwd, col_pstart, pair_plane, col_pend, reduce,
- * col_iprep, finish, df, axpy, massfix */
+ * col_iprep, finish, df, axpy, massfix, gain_cluster */
 int64_t pii_kernel_launches(void);
 int pii_plan_profile(pii_plan* plan, int enable);
 int pii_plan_profile_read(pii_plan* plan, double* ms, int64_t* launches);

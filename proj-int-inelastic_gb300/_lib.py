@@ -38,6 +38,7 @@ SIGNATURES = {
                                  _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_i64, _c_int]),
     "pii_plan_destroy": (_c_int, [_vp]),
     "pii_plan_workspace_bytes": (_c_i64, [_vp]),
+    "pii_plan_set_gain_path": (_c_int, [_vp, _c_int]),
     "pii_collide": (_c_int, [_vp, _vp, _vp, _c_i64, _c_int, _c_dbl, _c_int, _vp]),
     "pii_transport_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _vp]),
     "pii_boltzmann_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _c_dbl, _c_int,
@@ -53,9 +54,9 @@ SIGNATURES = {
     "pii_plan_profile_read": (_c_int, [_vp, _pdbl, ctypes.POINTER(ctypes.c_int64)]),
 }
 
-NSTAGES = 11
+NSTAGES = 12
 STAGES = ["fwd_plane", "col_fwd", "col_pstart", "pair_plane", "col_pend", "reduce", "col_iprep", "finish", "df",
-          "axpy", "massfix"]
+          "axpy", "massfix", "gain_cluster"]
 
 _lib = None
 

@@ -154,7 +154,7 @@ def _precision_of(config, precision):
 class Plan:
     """Owner of one ``pii_plan`` (device tables + workspace for batch_max cells)."""
 
-    def __init__(self, mesh, e, e0, gamma, precision, batch_max, device):
+    def __init__(self, mesh, e, e0, gamma, precision, batch_max, device, gain_path=None):
         lib = _lib.load()
         self.n = mesh.nv
         self.batch_max = int(batch_max)
@@ -174,6 +174,9 @@ class Plan:
         _lib.check(st, "pii_plan_create")
         self.handle = h.value
         self._lib = lib
+        if gain_path is not None:
+            _lib.check(lib.pii_plan_set_gain_path(self.handle, {"pipeline": 0, "cluster": 1}[gain_path]),
+                       "pii_plan_set_gain_path")
 
     @property
     def workspace_bytes(self):
@@ -209,13 +212,16 @@ class FSInelasticVHSCollision:
       False, kept); True returns Q+ - Q-;
     * ``mass_fix``   -- subtract the per-cell mean of Q in FP64 (k = 0 mode);
     * ``batch_max``  -- initial cell capacity of the plan (grown on demand);
-    * ``device``     -- CUDA device index.
+    * ``device``     -- CUDA device index;
+    * ``gain_path``  -- "cluster" (fused 2-CTA-cluster kernel, the default for
+      n = 32 in mixed precision) or "pipeline" (column / plane passes, every
+      other case); both evaluate the same operator.
     """
 
     collision_model = "vhs"
 
     def __init__(self, config, spectral_mesh, precision=None, with_loss=False, mass_fix=False, batch_max=1,
-                 device=0, **kwargs):
+                 device=0, gain_path=None, **kwargs):
         self.config = config
         self.sm = spectral_mesh
         self.ndim = int(config["collision-model"]["dim"])
@@ -227,6 +233,7 @@ class FSInelasticVHSCollision:
         self.default_with_loss = bool(with_loss)
         self.mass_fix = bool(mass_fix)
         self._device = int(device)
+        self._gain_path = gain_path
         self._plan = None
         self._batch_max = max(1, int(batch_max))
         self._pinned = {}
@@ -262,7 +269,7 @@ class FSInelasticVHSCollision:
                 self._plan.close()
             self._batch_max = max(self._batch_max, int(cells))
             self._plan = Plan(self.sm, self._e, self._e0, self._gamma, self._precision, self._batch_max,
-                              self._device)
+                              self._device, self._gain_path)
         return self._plan
 
     # -- evaluation --------------------------------------------------------

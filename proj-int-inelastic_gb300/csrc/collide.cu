@@ -1,8 +1,21 @@
 // Orchestration of one batched Q(f,f) evaluation (pii_collide) and dispatch on
 // (precision, n) to the templated kernels.
+#include <type_traits>
+
 #include "pii_internal.cuh"
 
 namespace pii {
+
+template <typename T, int NV>
+static int finish_all(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb,
+                      cudaStream_t s) {
+  const int64_t Fc = std::max<int64_t>(1, p->chunk_items / 2);
+  for (int64_t c0 = 0; c0 < cells; c0 += Fc) {
+    const int64_t cc = std::min(Fc, cells - c0);
+    PII_TRY((CollideKernels<T, NV>::finish(p, f, q, c0, cc, with_loss, hb, s)));
+  }
+  return PII_OK;
+}
 
 template <typename T, int NV>
 static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb,
@@ -10,6 +23,12 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
   using K = CollideKernels<T, NV>;
   const int64_t N = p->N;
   PII_TRY(K::fwd(p, f, 0, cells, s));
+  if constexpr (std::is_same<T, float>::value && NV == 32) {
+    if (p->gain_path == 1) {
+      PII_TRY(gain_cluster_run(p, cells, s));
+      return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
+    }
+  }
   // items = (cell, pair); a chunk holds Cc cells x Pc pairs in the L2-resident buffer
   int64_t Cc = std::max<int64_t>(1, (int64_t(131072) + N - 1) / N);
   Cc = std::min<int64_t>(Cc, std::min<int64_t>(cells, p->chunk_items));
@@ -21,12 +40,7 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
       PII_TRY(K::pairs(p, c0, cc, p0, np, p0 == 0, s));
     }
   }
-  const int64_t Fc = std::max<int64_t>(1, p->chunk_items / 2);
-  for (int64_t c0 = 0; c0 < cells; c0 += Fc) {
-    const int64_t cc = std::min(Fc, cells - c0);
-    PII_TRY(K::finish(p, f, q, c0, cc, with_loss, hb, s));
-  }
-  return PII_OK;
+  return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
 }
 
 template <typename T>
@@ -78,6 +92,19 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
 }
 
 }  // namespace pii
+
+extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
+  if (!plan || (path != 0 && path != 1)) {
+    pii::set_error("pii_plan_set_gain_path: path must be 0 (pipeline) or 1 (cluster)");
+    return PII_ERR_ARG;
+  }
+  if (path == 1 && (plan->gc_clusters <= 0 || plan->precision != PII_PREC_FP32 || plan->n != 32)) {
+    pii::set_error("pii_plan_set_gain_path: the cluster kernel exists for n = 32, FP32 plans only");
+    return PII_ERR_ARG;
+  }
+  plan->gain_path = path;
+  return PII_OK;
+}
 
 extern "C" int pii_collide(pii_plan* plan, const double* f, double* q, int64_t cells, int with_loss,
                            double heat_bath, int mass_fix, void* stream) {

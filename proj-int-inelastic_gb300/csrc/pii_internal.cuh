@@ -20,7 +20,7 @@ extern std::atomic<int64_t> g_launches;
 
 enum Stage {
   ST_FWD_PLANE = 0, ST_COL_FWD, ST_COL_PSTART, ST_PAIR_PLANE, ST_COL_PEND, ST_REDUCE,
-  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_COUNT
+  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_COUNT
 };
 
 #define PII_CUDA(call)                                                                    \
@@ -111,6 +111,12 @@ struct pii_plan {
   double* d1 = nullptr;
   double* d2 = nullptr;
   double* v1dev = nullptr;  // n first-axis velocities (device)
+  // fused 2-CTA-cluster gain kernel (n = 32, FP32): 1 = use it, 0 = column/plane pipeline
+  int gain_path = 0;
+  int gc_clusters = 0;
+  int64_t gc_max_items = 0;
+  void* gc_maps = nullptr;   // int2 thread -> columns [512], column -> slot [1024]
+  void* gc_hpart = nullptr;  // per-part Hermitian slots
   int64_t bytes = 0;
   std::map<pii::GraphKey, pii::GraphEntry> graphs;
   // per-stage CUDA-event profiling (pii_plan_profile)
@@ -139,6 +145,9 @@ namespace pii {
 int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb,
                  int mass_fix, cudaStream_t s);
 int prepare_impl(pii_plan* p);
+// gain_cluster.cu
+int gain_cluster_prepare(pii_plan* p);
+int gain_cluster_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // transport.cu
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
                    double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);

@@ -144,7 +144,8 @@ static void free_plan(pii_plan* p) {
     if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
   }
   void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
-                  p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev};
+                  p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
+                  p->gc_maps,    p->gc_hpart};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -214,6 +215,13 @@ static int create(pii_plan** out, int n, int nr, int ns, const double* r, const 
   if ((s2 = prepare_impl(p)) != PII_OK) {
     free_plan(p);
     return s2;
+  }
+  if (n == 32 && precision == PII_PREC_FP32) {
+    if ((s2 = gain_cluster_prepare(p)) != PII_OK) {
+      free_plan(p);
+      return s2;
+    }
+    p->gain_path = 1;
   }
   *out = p;
   return PII_OK;

@@ -118,6 +118,28 @@ def test_full_size_properties_c2():
     assert float((q7[0] - q[7]).abs().max() / q[7].abs().max()) < 1e-6
 
 
+@pytest.mark.parametrize("cells", [1, 3, 128])
+def test_cluster_kernel_matches_pipeline_and_fp64(cells):
+    """n = 32 mixed precision: the fused 2-CTA-cluster gain kernel against the
+    column / plane pipeline and against the FP64 path, gain and gain - loss."""
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 32, 32, 0.7, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    v = sm.v_center
+    rng = np.random.default_rng(cells)
+    f = np.stack([maxwellian(v, 1.0 + 0.2 * rng.random(), rng.uniform(-2, 2, 3), rng.uniform(0.5, 2.0))
+                  + 0.3 * maxwellian(v, 1.0, rng.uniform(-2, 2, 3), rng.uniform(0.5, 2.0)) for _ in range(cells)])
+    f = torch.as_tensor(f, device="cuda:0")
+    clus = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=cells, gain_path="cluster")
+    pipe = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=cells, gain_path="pipeline")
+    dbl = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=cells)
+    for wl in (False, True):
+        qc, qp, qd = clus.collide(f, with_loss=wl), pipe.collide(f, with_loss=wl), dbl.collide(f, with_loss=wl)
+        for c in range(cells):
+            assert rel_linf(qc[c].cpu().numpy(), qd[c].cpu().numpy()) < 1e-5, (wl, c)
+            assert rel_linf(qc[c].cpu().numpy(), qp[c].cpu().numpy()) < 1e-5, (wl, c)
+
+
 def test_mass_fix_conserves_mass_fp32():
     pkg = _pkg()
     cfg = op_config(32, L8_S, 32, 32, 0.9, 0.9, 1.0)
