@@ -16,8 +16,12 @@
 //      shared memory; then multiply by gain_rs(k) and accumulate.
 // Only Re IFFT3(G) is ever used, so the accumulator keeps the Hermitian part
 // H(k) = (G(k) + conj G(-k)) / 2 on half of k-space: each thread owns a column
-// pair {(b, c), (-b, -c)} (or two self-conjugate columns), 16 k_a values of its
-// CTA's parity -> 514 slots x 16 x 8 bytes = 64 KB of shared memory.  At the
+// pair {(b, c), (-b, -c)} (or two self-conjugate columns, handled by the same
+// instructions with a 0/1 weight so that no warp diverges), 16 k_a values of
+// its CTA's parity -> 514 slots x 16 x 8 bytes = 64 KB of shared memory.
+// Measured on GB300 (per-warp clock64 stamps), a pair costs ~37K cycles per
+// CTA: stage A ~9.5K, B ~12.7K, C ~8-12K (the distributed-shared-memory loads
+// dominate it: ~17 B/clk/SM), the two cluster barriers the rest.  At the
 // end of a work item the CTA writes its slots to a per-part buffer; a small
 // kernel sums the parts and expands H to the full spectrum G for the existing
 // final inverse transform.
@@ -57,7 +61,7 @@ struct GainClusterArgs {
   int64_t cells;
   int parts;        // work items per cell
   float2* hpart;    // [cells * parts][2][16][HSLOTS]
-  const int2* ucols;  // [THREADS] the two columns of each thread in stage C
+  const int4* ucols;  // [THREADS] (column, column, first slot, 1 if two self-conjugate columns)
 };
 
 // stage A for one column j: full inverse transform along a, keep this CTA's planes
@@ -108,46 +112,36 @@ __device__ __forceinline__ void stage_c_col(const float2* W, const float2* Wp, i
   });
 }
 
+// Every thread runs the same code: a column pair {j, -j} accumulates
+//   H(k_a, j) += X_j(k_a) + conj X_{-j}(-k_a)            (one slot),
+// two self-conjugate columns j0, j1 accumulate
+//   H(k_a, j_i) += X_{j_i}(k_a) + conj X_{j_i}(-k_a)     (slots z, z + 1),
+// selected by the 0 / 1 weight sc without divergence.
 template <int PAR>
-__device__ __forceinline__ void stage_c(const float2* W, const float2* Wp, float2* H, int2 uc, int t,
+__device__ __forceinline__ void stage_c(const float2* W, const float2* Wp, float2* H, int4 uc,
                                         const float2* gp, const float* gs) {
   using namespace gc;
+  const float sc = float(uc.w);
+  const int z0 = uc.z, z1 = uc.z + uc.w;
   float2 X[16];
-  if (t < 510) {
-    // column pair (j, -j): H(k_a, j) += X_j(k_a) + conj X_{-j}(-k_a), one column at a time
-    stage_c_col<PAR>(W, Wp, uc.x, gp, gs, X);
-    static_for<0, 16>([&](auto mi) {
-      constexpr int m = decltype(mi)::value;
-      float2 h = H[m * HSLOTS + t];
-      h.x += X[m].x;
-      h.y += X[m].y;
-      H[m * HSLOTS + t] = h;
-    });
-    stage_c_col<PAR>(W, Wp, uc.y, gp, gs, X);
-    static_for<0, 16>([&](auto mi) {
-      constexpr int m = decltype(mi)::value;
-      constexpr int mm = neg_m(m, PAR);
-      float2 h = H[m * HSLOTS + t];
-      h.x += X[mm].x;
-      h.y -= X[mm].y;
-      H[m * HSLOTS + t] = h;
-    });
-  } else {
-    // two self-conjugate columns, slots 510 + 2 (t - 510) + {0, 1}
-    const int s0 = 510 + 2 * (t - 510);
-#pragma unroll 1
-    for (int h2 = 0; h2 < 2; ++h2) {
-      stage_c_col<PAR>(W, Wp, h2 == 0 ? uc.x : uc.y, gp, gs, X);
-      static_for<0, 16>([&](auto mi) {
-        constexpr int m = decltype(mi)::value;
-        constexpr int mm = neg_m(m, PAR);
-        float2 h = H[m * HSLOTS + s0 + h2];
-        h.x += X[m].x + X[mm].x;
-        h.y += X[m].y - X[mm].y;
-        H[m * HSLOTS + s0 + h2] = h;
-      });
-    }
-  }
+  stage_c_col<PAR>(W, Wp, uc.x, gp, gs, X);
+  static_for<0, 16>([&](auto mi) {
+    constexpr int m = decltype(mi)::value;
+    constexpr int mm = neg_m(m, PAR);
+    float2 h = H[m * HSLOTS + z0];
+    h.x += X[m].x + sc * X[mm].x;
+    h.y += X[m].y - sc * X[mm].y;
+    H[m * HSLOTS + z0] = h;
+  });
+  stage_c_col<PAR>(W, Wp, uc.y, gp, gs, X);
+  static_for<0, 16>([&](auto mi) {
+    constexpr int m = decltype(mi)::value;
+    constexpr int mm = neg_m(m, PAR);
+    float2 h = H[m * HSLOTS + z1];
+    h.x += X[mm].x + sc * X[m].x;
+    h.y += sc * X[m].y - X[mm].y;
+    H[m * HSLOTS + z1] = h;
+  });
 }
 
 __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_cluster(GainClusterArgs a) {
@@ -163,9 +157,9 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_cluster(GainClusterArgs
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int64_t items = a.cells * a.parts;
   const int per_part = (a.Q + a.parts - 1) / a.parts;
-  const int2 uc = a.ucols[t];
-  const int nslot = t < 510 ? 1 : 2;
-  const int slot0 = t < 510 ? t : 510 + 2 * (t - 510);
+  const int4 uc = a.ucols[t];
+  const int nslot = 1 + uc.w;
+  const int slot0 = uc.z;
 
   for (int64_t it = cid; it < items; it += nclus) {
     const int64_t cell = it / a.parts;
@@ -228,9 +222,9 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_cluster(GainClusterArgs
       cluster.sync();  // both CTAs' planes are final for this pair
       // ---- C
       if (crank == 0)
-        stage_c<0>(W, Wp, H, uc, t, gp, gs);
+        stage_c<0>(W, Wp, H, uc, gp, gs);
       else
-        stage_c<1>(W, Wp, H, uc, t, gp, gs);
+        stage_c<1>(W, Wp, H, uc, gp, gs);
       cluster.sync();  // the peer has finished reading this CTA's planes
     }
     // ---- write this CTA's Hermitian slots (x 1/2) for the work item
@@ -272,37 +266,48 @@ __global__ void __launch_bounds__(256) k_herm_expand(float2* G, const float2* hp
 int gain_cluster_prepare(pii_plan* p) {
   using namespace gc;
   PII_CUDA(cudaFuncSetAttribute(k_gain_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM)));
-  // thread -> (column, column) of stage C and column -> slot map of the expansion
-  std::vector<int2> uc(THREADS), cs(N2);
-  std::vector<int> selfc;
+  // Stage-C work of each thread: a column pair {j, -j} (one slot) or two
+  // self-conjugate columns (two slots).  Warps 0..14 take rows 1..15 (every
+  // column); warp 15 takes rows 0 and 16, one row per half-warp, so its
+  // shared-memory accesses are conflict-free like the other warps'.
+  std::vector<int4> uc(THREADS);
+  std::vector<int2> cs(N2, make_int2(-1, -1));
+  int slot = 0;
+  auto pair_unit = [&](int t, int j) {
+    const int nj = neg_col(j);
+    uc[t] = make_int4(j, nj, slot, 0);
+    cs[j] = make_int2(slot, 0);
+    cs[nj] = make_int2(slot, 1);
+    ++slot;
+  };
+  for (int t = 0; t < 480; ++t) pair_unit(t, (1 + t / 32) * 32 + (t % 32));
+  for (int t = 480; t < 495; ++t) pair_unit(t, 0 * 32 + (t - 479));   // row 0, columns 1..15
+  for (int t = 496; t < 511; ++t) pair_unit(t, 16 * 32 + (t - 495));  // row 16, columns 1..15
+  const int selfc[4] = {0 * 32 + 0, 0 * 32 + 16, 16 * 32 + 0, 16 * 32 + 16};
+  for (int k = 0; k < 2; ++k) {
+    const int t = k == 0 ? 495 : 511;
+    uc[t] = make_int4(selfc[2 * k], selfc[2 * k + 1], slot, 1);
+    cs[selfc[2 * k]] = make_int2(slot, 2);
+    cs[selfc[2 * k + 1]] = make_int2(slot + 1, 2);
+    slot += 2;
+  }
   for (int j = 0; j < N2; ++j)
-    if (neg_col(j) == j) selfc.push_back(j);
-  // representatives of the column pairs {j, -j}: rows 1..15 (all columns), then
-  // rows 0 and 16, columns 1..15 -- ordered so that a warp's threads share a row
-  std::vector<int> reps;
-  for (int jb = 1; jb < 16; ++jb)
-    for (int jc = 0; jc < 32; ++jc) reps.push_back(jb * 32 + jc);
-  for (int jc = 1; jc < 16; ++jc) reps.push_back(0 * 32 + jc);
-  for (int jc = 1; jc < 16; ++jc) reps.push_back(16 * 32 + jc);
-  if (reps.size() != 510 || selfc.size() != 4) {
-    set_error("gain_cluster_prepare: bad column pairing (%zu, %zu)", reps.size(), selfc.size());
+    if (cs[j].x < 0) {
+      set_error("gain_cluster_prepare: column %d has no slot", j);
+      return PII_ERR_ARG;
+    }
+  if (slot != HSLOTS) {
+    set_error("gain_cluster_prepare: %d slots, expected %d", slot, HSLOTS);
     return PII_ERR_ARG;
   }
-  for (int t = 0; t < 510; ++t) {
-    const int j = reps[t], nj = neg_col(j);
-    uc[t] = make_int2(j, nj);
-    cs[j] = make_int2(t, 0);
-    cs[nj] = make_int2(t, 1);
-  }
-  for (int k = 0; k < 4; ++k) cs[selfc[k]] = make_int2(510 + k, 2);
-  uc[510] = make_int2(selfc[0], selfc[1]);
-  uc[511] = make_int2(selfc[2], selfc[3]);
   void* d = nullptr;
-  PII_CUDA(cudaMalloc(&d, (THREADS + N2) * sizeof(int2)));
-  p->bytes += (THREADS + N2) * sizeof(int2);
-  PII_CUDA(cudaMemcpy(d, uc.data(), THREADS * sizeof(int2), cudaMemcpyHostToDevice));
-  PII_CUDA(cudaMemcpy(static_cast<int2*>(d) + THREADS, cs.data(), N2 * sizeof(int2), cudaMemcpyHostToDevice));
+  const size_t maps = THREADS * sizeof(int4) + N2 * sizeof(int2);
+  PII_CUDA(cudaMalloc(&d, maps));
+  p->bytes += int64_t(maps);
   p->gc_maps = d;
+  PII_CUDA(cudaMemcpy(d, uc.data(), THREADS * sizeof(int4), cudaMemcpyHostToDevice));
+  PII_CUDA(cudaMemcpy(static_cast<char*>(d) + THREADS * sizeof(int4), cs.data(), N2 * sizeof(int2),
+                      cudaMemcpyHostToDevice));
   // clusters that fit at once
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -353,7 +358,7 @@ int gain_cluster_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.cells = cells;
   a.parts = parts;
   a.hpart = static_cast<float2*>(p->gc_hpart);
-  a.ucols = static_cast<const int2*>(p->gc_maps);
+  a.ucols = static_cast<const int4*>(p->gc_maps);
   const int64_t items = cells * parts;
   const int64_t grid_clusters = std::min<int64_t>(items, nclus);
   cudaLaunchConfig_t cfg = {};
@@ -380,7 +385,8 @@ int gain_cluster_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   {
     StageTimer st(p, ST_REDUCE, s);
     k_herm_expand<<<unsigned((cells * N3 + 255) / 256), 256, 0, s>>>(
-        static_cast<float2*>(p->G), a.hpart, static_cast<const int2*>(p->gc_maps) + THREADS, cells, parts);
+        static_cast<float2*>(p->G), a.hpart,
+        reinterpret_cast<const int2*>(static_cast<const char*>(p->gc_maps) + THREADS * sizeof(int4)), cells, parts);
   }
   PII_CHECK_LAUNCH();
   return PII_OK;
