@@ -223,6 +223,19 @@ def dist_setup(n_gpus):
     return 1, 0, 0, None
 
 
+def replica_aggregate(total_s, cell_evals, dist=None, device=None):
+    """Whole-job throughput of N independent replicas (no data-path collective):
+    every rank's cell-evaluations over the slowest rank's time."""
+    import torch
+
+    world = dist.get_world_size() if dist else 1
+    if dist:
+        t = torch.tensor([total_s], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t)
+    return world * cell_evals / total_s, total_s
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -350,11 +363,7 @@ def main():
         dist.barrier()
     ck = clocks.stop()
     total_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
-    if dist:
-        t = torch.tensor([total_s], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t)
-    value = world * CELL_EVALS_PER_STEP * args.steps / total_s
+    value, total_s = replica_aggregate(total_s, CELL_EVALS_PER_STEP * args.steps, dist, device)
     ms_per_step = total_s / args.steps * 1e3
 
     # ---------------- e2e: host f in, host f out, through the solver API -------
@@ -370,10 +379,7 @@ def main():
         pin_out.copy_(sol.state.f, non_blocking=True)
         torch.cuda.current_stream().synchronize()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t)
+    _, e2e_s = replica_aggregate(e2e_s, CELL_EVALS_PER_STEP * e2e_steps, dist, device)
     nbytes = sol.f.numel() * 8
     e2e = {"value": world * CELL_EVALS_PER_STEP * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes,

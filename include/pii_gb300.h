@@ -46,6 +46,8 @@ extern "C" {
 #define PII_INT_PFE 1   /* src/boltzmann.py:120-128 */
 #define PII_INT_TPI2 2  /* src/boltzmann.py:130-140 */
 #define PII_INT_TPI3 3  /* src/boltzmann.py:142-158 */
+#define PII_INT_CONSP 4   /* src/boltzmann.py:86-94   */
+#define PII_INT_CONSP_M 5 /* src/boltzmann.py:96-118 (3D-velocity form) */
 
 typedef struct pii_plan pii_plan;
 
@@ -129,6 +131,31 @@ int pii_boltzmann_df(pii_plan* plan, const double* f, double* df, int64_t nx, do
 int pii_step(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, const int* inner_steps,
              const double* inner_dt, int levels, double dx, const double* v1, int bc_lower, int bc_upper,
              double kn, int with_loss, int mass_fix, int use_graph, void* stream);
+
+/*
+ * One convex-splitting step of size dt, updating f in place (FP64):
+ *   CONSP   (src/boltzmann.py:86-94):  f += dt / (kn + P dt) Q(f);  f += transport(f, dt)
+ *   CONSP_M (src/boltzmann.py:96-118): as CONSP plus the penalised Maxwellian
+ *           term P dt / (kn + P dt) (M[rho, u1, T_new] - M[rho, u1, T]) with
+ *           T_new = (T - 8 tau / (1 - e^2)) exp(-(1 - e^2) rho dt / (4 kn)) + 8 tau / (1 - e^2),
+ *           rho, u1 (first velocity component) and T from the FP64 moments of f.
+ *           The reference implements it for 2D velocity only; this is the 3D-velocity
+ *           form (Maxwellian in 3D, bulk velocity (u1, 0, 0) as in the reference).
+ * penalty: P; e, tau: CONSP_M only.  dx <= 0: no transport (homogeneous cells).
+ */
+int pii_step_splitting(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, double dx,
+                       const double* v1, int bc_lower, int bc_upper, double kn, double penalty, double e,
+                       double tau, int with_loss, int mass_fix, int use_graph, void* stream);
+
+/*
+ * FP64 guard on the state (no reference counterpart; the reference has no
+ * failure detection): computes the per-cell moments of f into out[cells * 5]
+ * (device, as pii_moments) and checks every value of f for NaN / Inf.
+ * Synchronises the stream.  Returns PII_ERR_NONFINITE if any value is not
+ * finite, PII_OK otherwise.
+ */
+int pii_state_check(pii_plan* plan, const double* f, double* out, int64_t cells, const double* v, double delta,
+                    void* stream);
 
 /*
  * FP64 moments per cell: out[c*5 + {0,1,2,3,4}] = sum f, sum f v1, sum f v2,

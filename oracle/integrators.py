@@ -60,6 +60,36 @@ def tel_proj_step3(f, dt, df, inner_steps, inner_dt):
     f += M2 * d2
 
 
+def convex_splitting_step(f, dt, collision, kn, penalty, advection=None):
+    """CONSP (src/boltzmann.py:86-94): collision update, then transport of the updated f."""
+    f += dt / (kn + penalty * dt) * collision(f)
+    if advection is not None:
+        f += advection(f, dt)
+
+
+def convex_splitting_maxwellian_step(f, dt, collision, kn, penalty, e, tau, v, delta, advection=None):
+    """CONSP_M (src/boltzmann.py:96-118) in 3D velocity.
+
+    The reference writes it for 2D velocity only; this restatement uses the 3D
+    Maxwellian with bulk velocity (u1, 0, 0) and the 3D temperature, the same
+    cooling law T_new = (T - 8 tau/(1-e^2)) exp(-(1-e^2) rho dt / (4 kn)) + 8 tau/(1-e^2).
+    """
+    mo = moments(f, v, delta)
+    rho, u1, T = mo["rho"], mo["u"][..., 0], mo["T"]
+    T_new = (T - 8 * tau / (1 - e**2)) * np.exp(-(1 - e**2) / kn / 4 * rho * dt) + 8 * tau / (1 - e**2)
+    V = np.meshgrid(v, v, v, indexing="ij")
+
+    def maxw(T_):
+        sh = (slice(None),) + (None,) * 3 if np.ndim(rho) else ()
+        r, uu, tt = (np.asarray(x)[sh] for x in (rho, u1, T_))
+        return r / (2 * np.pi * tt) ** 1.5 * np.exp(-((V[0] - uu) ** 2 + V[1] ** 2 + V[2] ** 2) / (2 * tt))
+
+    dm = maxw(T_new) - maxw(T)
+    f += dt / (kn + penalty * dt) * collision(f) + penalty * dt / (kn + penalty * dt) * dm
+    if advection is not None:
+        f += advection(f, dt)
+
+
 STEPS = {
     "Euler": lambda f, dt, df, K, h: euler_step(f, dt, df),
     "PFE": proj_euler_step,

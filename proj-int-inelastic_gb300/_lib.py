@@ -25,6 +25,8 @@ INT_EULER = 0
 INT_PFE = 1
 INT_TPI2 = 2
 INT_TPI3 = 3
+INT_CONSP = 4
+INT_CONSP_M = 5
 
 _c_int, _c_i64, _c_dbl, _vp = ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
 _pdbl = ctypes.POINTER(ctypes.c_double)
@@ -45,6 +47,9 @@ SIGNATURES = {
                                   _c_int, _vp]),
     "pii_step": (_c_int, [_vp, _c_int, _vp, _c_i64, _c_dbl, _pint, _pdbl, _c_int, _c_dbl, _pdbl, _c_int, _c_int,
                           _c_dbl, _c_int, _c_int, _c_int, _vp]),
+    "pii_step_splitting": (_c_int, [_vp, _c_int, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _c_dbl, _c_dbl,
+                                    _c_dbl, _c_dbl, _c_int, _c_int, _c_int, _vp]),
+    "pii_state_check": (_c_int, [_vp, _vp, _vp, _c_i64, _pdbl, _c_dbl, _vp]),
     "pii_moments": (_c_int, [_vp, _vp, _vp, _c_i64, _pdbl, _c_dbl, _vp]),
     "pii_axpby": (_c_int, [_vp, _vp, _c_dbl, _c_dbl, _c_i64, _vp]),
     "pii_collide_noalloc": (_c_int, [_vp, _vp, _c_i64, _c_int, _c_int, _c_int, _pdbl, _pdbl, _pdbl, _c_dbl, _c_dbl,
@@ -90,6 +95,8 @@ def check(status, what):
     msg = f"{what}: {last_error()}"
     if status in (PII_ERR_ARG, PII_ERR_SIZE):
         raise ValueError(msg)
+    if status == PII_ERR_NONFINITE:
+        raise FloatingPointError(msg)
     raise RuntimeError(msg)
 
 

@@ -111,6 +111,9 @@ struct pii_plan {
   double* d1 = nullptr;
   double* d2 = nullptr;
   double* v1dev = nullptr;  // n first-axis velocities (device)
+  double* mom = nullptr;    // batch_max * 5 FP64 moment sums (CONSP_M)
+  int* flag = nullptr;      // device flag of pii_state_check
+  double delta3 = 0;        // velocity cell volume of the last splitting step
   // fused 2-CTA-cluster gain kernel (n = 32, FP32): 1 = use it, 0 = column/plane pipeline
   int gain_path = 0;
   int gc_clusters = 0;
@@ -155,6 +158,10 @@ int mass_fix_impl(pii_plan* p, double* q, int64_t cells, int64_t N, cudaStream_t
 int axpy3_impl(pii_plan* p, double* f, const double* d, double s0, double s1, double s2, int64_t count,
                cudaStream_t s);
 int upload_v1(pii_plan* p, const double* v1, cudaStream_t s);
+int consp_m_impl(pii_plan* p, double* f, const double* q, int64_t cells, double c, double c2, double dt, double kn,
+                 double e, double tau, cudaStream_t s);
+int axpy3_impl(pii_plan* p, double* f, const double* d, double s0, double s1, double s2, int64_t count,
+               cudaStream_t s);
 
 // per-precision, per-size kernels (collide_kernels_*.cu)
 template <typename T, int NV>

@@ -145,7 +145,7 @@ static void free_plan(pii_plan* p) {
   }
   void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
-                  p->gc_maps,    p->gc_hpart};
+                  p->gc_maps,    p->gc_hpart,   p->mom,       p->flag};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -208,7 +208,9 @@ static int create(pii_plan** out, int n, int nr, int ns, const double* r, const 
       (s2 = alloc(p, &p->buf, size_t(p->chunk_items) * N * cs)) != PII_OK ||
       (s2 = alloc(p, (void**)&p->q, size_t(batch_max) * N * 8)) != PII_OK ||
       (s2 = alloc(p, (void**)&p->d0, size_t(batch_max) * N * 8)) != PII_OK ||
-      (s2 = alloc(p, (void**)&p->v1dev, size_t(n) * 8)) != PII_OK) {
+      (s2 = alloc(p, (void**)&p->v1dev, size_t(n) * 8)) != PII_OK ||
+      (s2 = alloc(p, (void**)&p->mom, size_t(batch_max) * 5 * 8)) != PII_OK ||
+      (s2 = alloc(p, (void**)&p->flag, sizeof(int))) != PII_OK) {
     free_plan(p);
     return s2;
   }

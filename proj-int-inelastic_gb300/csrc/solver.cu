@@ -111,9 +111,93 @@ static int validate(pii_plan* p, int integrator, double* f, int64_t nx, const in
   return PII_OK;
 }
 
+// CONSP / CONSP_M (src/boltzmann.py:86-118): collision update, then transport of the updated f
+static int splitting_body(const StepCtx& c, int integrator, double dt, double penalty, double e, double tau) {
+  PII_TRY(collide_impl(c.p, c.f, c.p->q, c.nx, c.with_loss, 0.0, c.mass_fix, c.s));
+  const double cq = dt / (c.kn + penalty * dt);
+  if (integrator == PII_INT_CONSP) {
+    PII_TRY(axpy3_impl(c.p, c.f, c.p->q, cq, 1, 1, c.nx * c.p->N, c.s));
+  } else {
+    const double cm = penalty * dt / (c.kn + penalty * dt);
+    PII_TRY(consp_m_impl(c.p, c.f, c.p->q, c.nx, cq, cm, dt, c.kn, e, tau, c.s));
+  }
+  if (c.dx > 0) {
+    PII_TRY(transport_impl(c.p, c.f, nullptr, c.p->d0, c.nx, dt, c.dx, c.bc_lo, c.bc_hi, 1.0, c.s));
+    PII_TRY(add(c, 1, 1, 1));
+  }
+  return PII_OK;
+}
+
 }  // namespace pii
 
 extern "C" {
+
+int pii_step_splitting(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, double dx,
+                       const double* v1, int bc_lower, int bc_upper, double kn, double penalty, double e,
+                       double tau, int with_loss, int mass_fix, int use_graph, void* stream) {
+  if (!plan || !f || nx <= 0 || !v1 || !(kn > 0) || !(dt > 0)) {
+    pii::set_error("pii_step_splitting: invalid arguments");
+    return PII_ERR_ARG;
+  }
+  if (integrator != PII_INT_CONSP && integrator != PII_INT_CONSP_M) {
+    pii::set_error("This time integrator is not implemented.");
+    return PII_ERR_ARG;
+  }
+  if (!penalty) {
+    pii::set_error("The penalty parameter is not given. Please specify it!");
+    return PII_ERR_ARG;
+  }
+  if (integrator == PII_INT_CONSP_M && (!e || !(e * e < 1.0))) {
+    pii::set_error("The penalty parameter, e or tau are not given. Please specify it!");
+    return PII_ERR_ARG;
+  }
+  if (nx > plan->batch_max) {
+    pii::set_error("pii_step_splitting: nx beyond batch_max");
+    return PII_ERR_SIZE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PII_CUDA(cudaSetDevice(plan->device));
+  if (dx > 0) PII_TRY(pii::check_bcs(bc_lower, bc_upper));
+  PII_TRY(pii::upload_v1(plan, v1, s));
+  const double delta = v1[1] - v1[0];
+  plan->delta3 = delta * delta * delta;
+  pii::StepCtx c{plan, f, nx, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, s};
+  if (!use_graph || s == nullptr || plan->prof) return pii::splitting_body(c, integrator, dt, penalty, e, tau);
+  pii::GraphKey key{integrator, f, nx, dt, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, 0,
+                    {0, 0, 0}, {penalty, e, tau}, stream};
+  auto it = plan->graphs.find(key);
+  if (it == plan->graphs.end()) {
+    PII_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = pii::g_launches.load();
+    int st = pii::splitting_body(c, integrator, dt, penalty, e, tau);
+    const int64_t captured = pii::g_launches.load() - before;
+    pii::g_launches.fetch_sub(captured);
+    cudaGraph_t g = nullptr;
+    cudaError_t er = cudaStreamEndCapture(s, &g);
+    if (st != PII_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (er != cudaSuccess) {
+      pii::set_error("graph capture: %s", cudaGetErrorString(er));
+      return PII_ERR_CUDA;
+    }
+    pii::GraphEntry ge;
+    ge.graph = g;
+    ge.kernels = captured;
+    er = cudaGraphInstantiate(&ge.exec, g, 0);
+    if (er != cudaSuccess) {
+      cudaGraphDestroy(g);
+      pii::set_error("graph instantiate: %s", cudaGetErrorString(er));
+      return PII_ERR_CUDA;
+    }
+    it = plan->graphs.emplace(key, ge).first;
+  }
+  PII_CUDA(cudaGraphLaunch(it->second.exec, s));
+  pii::g_launches.fetch_add(it->second.kernels);
+  return PII_OK;
+}
+
 
 int pii_boltzmann_df(pii_plan* plan, const double* f, double* df, int64_t nx, double dt, double dx,
                      const double* v1, int bc_lower, int bc_upper, double kn, int with_loss, int mass_fix,

@@ -8,6 +8,8 @@
 //   * k_massfix   : per-cell FP64 mean removal of Q (k = 0 mode; not in the reference)
 //   * k_moments   : per-cell FP64 sums of f, f v, f |v|^2 / 2
 // The state f and every increment are FP64 in every precision mode.
+#include <algorithm>
+
 #include "pii_internal.cuh"
 
 namespace pii {
@@ -126,6 +128,56 @@ __global__ void __launch_bounds__(256) k_moments(const double* f, double* out, c
   }
 }
 
+// CONSP_M update: f += c Q + c2 (M[rho, u1, T_new] - M[rho, u1, T]) per cell, moments from mom
+__global__ void __launch_bounds__(256) k_consp_m(double* f, const double* q, const double* mom, const double* v, int n,
+                                                  int64_t count, double c, double c2, double dt, double kn, double e,
+                                                  double tau) {
+  const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= count) return;
+  const int64_t N = int64_t(n) * n * n;
+  const int64_t cell = gid / N;
+  const int64_t j = gid - cell * N;
+  const double* m = mom + cell * 5;
+  const double rho = m[0];
+  const double u = m[1] / rho;
+  const double ux = m[1] / rho, uy = m[2] / rho, uz = m[3] / rho;
+  const double T = (2.0 / 3.0) * (m[4] / rho - 0.5 * (ux * ux + uy * uy + uz * uz));
+  const double ee = 1.0 - e * e;
+  const double Tinf = 8.0 * tau / ee;
+  const double Tn = (T - Tinf) * exp(-ee / kn / 4.0 * rho * dt) + Tinf;
+  const double v1 = v[j / (int64_t(n) * n)], v2 = v[(j / n) % n], v3 = v[j % n];
+  const double d2 = (v1 - u) * (v1 - u) + v2 * v2 + v3 * v3;
+  const double pi = 3.141592653589793238462643383279502884;
+  const double Mn = rho / pow(2.0 * pi * Tn, 1.5) * exp(-d2 / (2.0 * Tn));
+  const double Mo = rho / pow(2.0 * pi * T, 1.5) * exp(-d2 / (2.0 * T));
+  f[gid] += c * q[gid] + c2 * (Mn - Mo);
+}
+
+__global__ void __launch_bounds__(256) k_nonfinite(const double* f, int64_t count, int* flag) {
+  int bad = 0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x)
+    bad |= !isfinite(f[i]);
+  bad = __syncthreads_or(bad);
+  if (bad && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+int consp_m_impl(pii_plan* p, double* f, const double* q, int64_t cells, double c, double c2, double dt, double kn,
+                 double e, double tau, cudaStream_t s) {
+  const int64_t count = cells * p->N;
+  {
+    StageTimer st(p, ST_AXPY, s);
+    k_moments<<<unsigned(cells), 256, 0, s>>>(f, p->mom, p->v1dev, p->n, p->delta3);
+  }
+  PII_CHECK_LAUNCH();
+  {
+    StageTimer st(p, ST_AXPY, s);
+    k_consp_m<<<unsigned((count + 255) / 256), 256, 0, s>>>(f, q, p->mom, p->v1dev, p->n, count, c, c2, dt, kn, e,
+                                                            tau);
+  }
+  PII_CHECK_LAUNCH();
+  return PII_OK;
+}
+
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt, double dx,
                    int bc_lo, int bc_hi, double kn, cudaStream_t s) {
   DfArgs a{};
@@ -220,6 +272,32 @@ int pii_moments(pii_plan* plan, const double* f, double* out, int64_t cells, con
   PII_TRY(pii::upload_v1(plan, v, s));
   pii::k_moments<<<unsigned(cells), 256, 0, s>>>(f, out, plan->v1dev, plan->n, delta * delta * delta);
   PII_CHECK_LAUNCH();
+  return PII_OK;
+}
+
+int pii_state_check(pii_plan* plan, const double* f, double* out, int64_t cells, const double* v, double delta,
+                    void* stream) {
+  if (!plan || !f || !out || !v || cells <= 0) {
+    pii::set_error("pii_state_check: invalid arguments");
+    return PII_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PII_CUDA(cudaSetDevice(plan->device));
+  PII_TRY(pii::upload_v1(plan, v, s));
+  pii::k_moments<<<unsigned(cells), 256, 0, s>>>(f, out, plan->v1dev, plan->n, delta * delta * delta);
+  PII_CHECK_LAUNCH();
+  PII_CUDA(cudaMemsetAsync(plan->flag, 0, sizeof(int), s));
+  const int64_t count = cells * plan->N;
+  const int64_t blocks = std::min<int64_t>((count + 255) / 256, 4096);
+  pii::k_nonfinite<<<unsigned(blocks), 256, 0, s>>>(f, count, plan->flag);
+  PII_CHECK_LAUNCH();
+  int h = 0;
+  PII_CUDA(cudaMemcpyAsync(&h, plan->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PII_CUDA(cudaStreamSynchronize(s));
+  if (h) {
+    pii::set_error("pii_state_check: f holds NaN or Inf values");
+    return PII_ERR_NONFINITE;
+  }
   return PII_OK;
 }
 

@@ -242,6 +242,9 @@ class BoltzmannSolver(Solver):
         self.with_loss = None
         self.mass_fix = None
         self.use_graph = True
+        self.check_every = 0
+        self.mass_drift_tol = None
+        self._mass0 = None
         self._stream = None
         super().__init__(riemann_solver, collision_operator)
 
@@ -252,6 +255,7 @@ class BoltzmannSolver(Solver):
         n = f.shape[-1]
         cells = f.numel() // n**3
         return cells, 0.0, np.ascontiguousarray(state.v, np.float64), _lib.BC_EXTRAP, _lib.BC_EXTRAP
+
 
     def _wl(self):
         if self.with_loss is not None:
@@ -272,15 +276,70 @@ class BoltzmannSolver(Solver):
     def step(self, solution, take_one_step, tstart, tend):
         """``BoltzmannSolver.step`` (src/boltzmann.py:46-80)."""
         ti = self.time_integrator
-        if ti in ("CONSP", "CONSP_M"):
-            raise NotImplementedError("convex-splitting integrators are not implemented on the GPU")
-        if ti not in _INTEGRATORS:
-            raise NotImplementedError("This time integrator is not implemented.")
         state = solution.state
+        if ti == "CONSP":
+            if not self.penalty:
+                raise ValueError("The penalty parameter is not given. Please specify it!")
+        elif ti == "CONSP_M":
+            if not (self.penalty and self.e and (self.tau is not None)):
+                raise ValueError("The penalty parameter, e or tau are not given. Please specify it!")
+        elif ti not in _INTEGRATORS:
+            raise NotImplementedError("This time integrator is not implemented.")
         if isinstance(self.collision, FSInelasticVHSCollision):
-            self._fused_step(state, ti)
+            if ti in ("CONSP", "CONSP_M"):
+                self._fused_splitting(state, ti)
+            else:
+                self._fused_step(state, ti)
         else:
+            if ti == "CONSP_M":
+                raise NotImplementedError("CONSP_M needs the GB300 collision operator")
             self._generic_step(state, ti)
+        self._steps_done = getattr(self, "_steps_done", 0) + 1
+        if self.check_every and self._steps_done % self.check_every == 0:
+            self.check_state(state)
+
+    def check_state(self, state):
+        """FP64 guard: raise FloatingPointError if f holds NaN / Inf, and
+        RuntimeError if the total mass drifted by more than ``mass_drift_tol``
+        (relative) since the first check.  Returns (rho, u, T) per cell."""
+        f = state.f
+        n = f.shape[-1]
+        cells = f.numel() // n**3
+        out = torch.empty((cells, 5), dtype=torch.float64, device=f.device)
+        plan = _moment_plan(n, f.device.index or 0)
+        v = np.ascontiguousarray(state.v, np.float64)
+        st = plan._lib.pii_state_check(plan.handle, f.contiguous().data_ptr(), out.data_ptr(), cells, _lib.dptr(v),
+                                       float(state.dv), torch.cuda.current_stream(f.device).cuda_stream)
+        _lib.check(st, "pii_state_check")
+        m = out.cpu().numpy()
+        mass = float(m[:, 0].sum())
+        if self._mass0 is None:
+            self._mass0 = mass
+        elif self.mass_drift_tol is not None and abs(mass - self._mass0) > self.mass_drift_tol * abs(self._mass0):
+            raise RuntimeError(f"total mass drifted from {self._mass0:.12g} to {mass:.12g}")
+        rho = m[:, 0]
+        u = m[:, 1:4] / rho[:, None]
+        T = (2.0 / 3.0) * (m[:, 4] / rho - 0.5 * (u**2).sum(-1))
+        return rho, u, T
+
+    def _fused_splitting(self, state, ti):
+        f = state.f
+        if not (f.is_cuda and f.dtype == torch.float64 and f.is_contiguous()):
+            raise ValueError("state.f must be a contiguous CUDA float64 tensor")
+        nx, dx, v1, lo, hi = self._transport_args(state)
+        plan = self.collision._ensure_plan(nx)
+        cur = torch.cuda.current_stream(f.device)
+        s = self._get_stream(f.device) if self.use_graph else cur
+        if s is not cur:
+            s.wait_stream(cur)
+        code = _lib.INT_CONSP if ti == "CONSP" else _lib.INT_CONSP_M
+        st = plan._lib.pii_step_splitting(plan.handle, code, f.data_ptr(), nx, float(self.dt), float(dx), _lib.dptr(v1),
+                                          int(lo), int(hi), float(self.kn), float(self.penalty or 0.0),
+                                          float(self.e or 0.0), float(self.tau or 0.0), int(self._wl()),
+                                          int(self._mf()), int(bool(self.use_graph)), s.cuda_stream)
+        _lib.check(st, "pii_step_splitting")
+        if s is not cur:
+            cur.wait_stream(s)
 
     def _fused_step(self, state, ti):
         f = state.f
@@ -307,7 +366,10 @@ class BoltzmannSolver(Solver):
         """Same nesting as src/boltzmann.py:82-158 for an arbitrary collision callable."""
         f = state.f
         dt, K, h = self.dt, self.inner_steps, self.inner_dt
-        if ti == "Euler":
+        if ti == "CONSP":
+            f += dt / (self.kn + self.penalty * dt) * self._q(state)
+            f += self.df_advection(state, dt)
+        elif ti == "Euler":
             f += self.df(state, dt)
         elif ti == "PFE":
             M = dt / h[0] - K[0]
@@ -340,14 +402,17 @@ class BoltzmannSolver(Solver):
                 f += d2
             f += M2 * d2
 
+    def _q(self, state):
+        q = self.collision(state.f)
+        if not isinstance(q, torch.Tensor):
+            q = torch.as_tensor(q, device=state.f.device)
+        return q
+
     def df(self, state, dt):
         """``BoltzmannSolver.df`` (src/boltzmann.py:160-164)."""
         deltaf = self.df_advection(state, dt)
         if self.collision is not None:
-            q = self.collision(state.f)
-            if not isinstance(q, torch.Tensor):
-                q = torch.as_tensor(q, device=state.f.device)
-            deltaf += dt * q / self.kn
+            deltaf += dt * self._q(state) / self.kn
         return deltaf
 
     def df_advection(self, state, dt):

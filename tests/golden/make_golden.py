@@ -173,6 +173,7 @@ def make_solver1d(ref):
         ("tpi2", "TPI2", ref.solver.BC.periodic, "per", [2, 2], [5e-4, 2e-3], 6e-3, 6e-3, "gain"),
         ("tpi3", "TPI3", ref.solver.BC.periodic, "per", [2, 2, 2], [2e-4, 6e-4, 2e-3], 6e-3, 1.2e-2, "full"),
         ("euler", "Euler", ref.solver.BC.extrap, "sod", [3], [1e-3], 5e-4, 2e-3, "gain"),
+        ("consp", "CONSP", ref.solver.BC.periodic, "per", [3], [1e-3], 1e-3, 3e-3, "full"),
     ]
     for name, integ, bc, init, K, h, dt, tend, which in runs:
         sol = _solution(ref, nx, nv, sm.L)
@@ -192,6 +193,7 @@ def make_solver1d(ref):
         solver.inner_steps = list(K)
         solver.inner_dt = list(h)
         solver.dt = dt
+        solver.penalty = 5.0
         solver.evolve_to_time(sol, tend)
         out[f"{name}_f0"] = f0
         out[f"{name}_f"] = sol.state.f.copy()

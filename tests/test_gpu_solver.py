@@ -158,3 +158,88 @@ def test_pfe_c2_full_size_mass_and_parity():
     rho0, rho1 = out["mixed"][1], out["mixed"][2]
     # total mass changes only by the boundary fluxes; interior cells far from x = 0.5 keep rho
     assert abs(rho1[:20].mean() - rho0[:20].mean()) / rho0[:20].mean() < 1e-6
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_consp_golden(golden, precision, use_graph):
+    """Convex splitting (src/boltzmann.py:86-94) against the reference run."""
+    pkg = _pkg()
+    d = golden("solver1d.npz")
+    nv, nr, ns, e, e0, g, s, nx = d["params"]
+    cfg = op_config(nv, s, nr, ns, e, e0, g)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, with_loss=True)
+    dt, tend, kn, dx = d["consp_meta"]
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": int(nx), "nv": int(nv)})
+    sol.state.f.copy_(torch.as_tensor(d["consp_f0"]))
+    solver = pkg.BoltzmannSolver1D(float(kn), collision_operator=col)
+    solver.all_bcs = pkg.BC.periodic
+    solver.time_integrator = "CONSP"
+    solver.penalty = 5.0
+    solver.dt = float(dt)
+    solver.use_graph = use_graph
+    solver.evolve_to_time(sol, float(tend))
+    tol = 1e-11 if precision == "double" else 1e-5
+    assert rel_linf(sol.f.cpu().numpy(), d["consp_f"]) < tol
+
+
+def test_consp_maxwellian_3d_vs_oracle():
+    """CONSP_M in its 3D-velocity form against the oracle restatement."""
+    pkg = _pkg()
+    from oracle import fs_inelastic as fo
+    from oracle import integrators as it
+    from oracle import transport as tr
+
+    nv, nr, ns, e = 8, 4, 6, 0.6
+    cfg = op_config(nv, L8_S, nr, ns, e, e, 0.0)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", with_loss=True)
+    nx = 6
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": nx, "nv": nv})
+    v = sol.state.v
+    f0 = np.stack([maxwellian(v, 1 + 0.1 * i, (0.3 * i - 0.5, 0.2, 0.0), 1 + 0.05 * i) for i in range(nx)])
+    sol.state.f.copy_(torch.as_tensor(f0))
+    solver = pkg.BoltzmannSolver1D(0.5, collision_operator=col)
+    solver.all_bcs = pkg.BC.extrap
+    solver.time_integrator = "CONSP_M"
+    solver.penalty, solver.e, solver.tau, solver.dt = 3.0, e, 0.05, 1e-3
+    solver.evolve_to_time(sol, 3e-3)
+    m = fo.Mesh(nv, L8_S, nr, ns)
+    op = fo.FSInelasticVHS(m, e, e, 0.0)
+    f = f0.copy()
+    dx = 1.0 / nx
+    for _ in range(3):
+        it.convex_splitting_maxwellian_step(f, 1e-3, lambda x: op.collide(x, with_loss=True), 0.5, 3.0, e, 0.05,
+                                            m.v, m.delta, lambda x, h: tr.df_advection(x, m.v, h, dx))
+    assert rel_linf(sol.f.cpu().numpy(), f) < 1e-11
+
+
+def test_state_guard_detects_nonfinite_and_mass_drift():
+    """Failures injected on the host: a NaN written into f, and a mass change."""
+    pkg = _pkg()
+    cfg = op_config(8, L8_S, 4, 6, 0.9, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, mass_fix=True)
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": 4, "nv": 8})
+    v = sol.state.v
+    sol.state.f.copy_(torch.as_tensor(np.stack([maxwellian(v, 1.0, (0, 0, 0), 1.0)] * 4)))
+    solver = pkg.BoltzmannSolver1D(1.0, collision_operator=col)
+    solver.all_bcs = pkg.BC.periodic
+    solver.time_integrator = "PFE"
+    solver.inner_steps, solver.inner_dt, solver.dt = [2], [1e-3], 4e-3
+    solver.check_every, solver.mass_drift_tol = 1, 1e-9
+    solver.evolve_to_time(sol, 8e-3)  # healthy: periodic transport + mass-fixed collisions conserve mass
+    rho, u, T = solver.check_state(sol.state)
+    assert np.all(np.isfinite(T))
+    sol.state.f[2, 3, 4, 5] += 1.0  # host-side injection: mass changes
+    with pytest.raises(RuntimeError, match="mass drifted"):
+        solver.check_state(sol.state)
+    sol.state.f[1, 0, 0, 0] = float("nan")  # host-side injection: a NaN
+    with pytest.raises(FloatingPointError):
+        solver.check_state(sol.state)
+    # the library and the plan stay usable after the guard fired
+    sol.state.f.copy_(torch.as_tensor(np.stack([maxwellian(v, 1.0, (0, 0, 0), 1.0)] * 4)))
+    solver._mass0 = None
+    solver.evolve_to_time(sol, sol.t + 4e-3)
+    assert torch.isfinite(sol.f).all()

@@ -65,6 +65,19 @@ def test_solver1d(golden, name, integ):
     assert rel_linf(f, d[f"{name}_f"]) < 1e-11
 
 
+def test_consp_reference_run(golden):
+    """CONSP (convex splitting, penalty 5) of the reference solver, gain - loss."""
+    d = golden("solver1d.npz")
+    nv, nr, ns, e, e0, g, s, nx = d["params"]
+    m, op = _op((nv, nr, ns, e, e0, g, s))
+    dt, tend, kn, dx = d["consp_meta"]
+    f = d["consp_f0"].copy()
+    adv = lambda x, hh: tr.df_advection(x, m.v, hh, dx, "periodic", "periodic")
+    for _ in range(int(round(tend / dt))):
+        it.convex_splitting_step(f, dt, lambda x: op.collide(x, with_loss=True), kn, 5.0, adv)
+    assert rel_linf(f, d["consp_f"]) < 1e-11
+
+
 def test_euler_history_c32(golden):
     """First steps of the 100-step forward-Euler run (full run checked on the GPU)."""
     d = golden("euler_c32.npz")
