@@ -327,8 +327,10 @@ int gain_cluster_prepare(pii_plan* p) {
     return PII_ERR_CUDA;
   }
   p->gc_clusters = nclus;
-  // per-part Hermitian slots: at most (6 * clusters + batch_max) work items
-  const int64_t max_items = int64_t(6) * nclus + p->batch_max;
+  // per-part Hermitian slots: at most (6 * clusters + batch_max) work items, and
+  // never more than batch_max cells x Q / 8 parts
+  const int64_t max_items =
+      std::min<int64_t>(int64_t(6) * nclus + p->batch_max, p->batch_max * std::max(1, p->Q / 8));
   PII_CUDA(cudaMalloc(&p->gc_hpart, size_t(max_items) * 2 * 16 * HSLOTS * sizeof(float2)));
   p->bytes += max_items * 2 * 16 * HSLOTS * int64_t(sizeof(float2));
   p->gc_max_items = max_items;

@@ -1,0 +1,98 @@
+"""Ensembles of independent space-homogeneous problems stepped as one graph.
+
+Each instance has its own velocity grid (n may differ), restitution law and
+state f of shape (n, n, n).  Instances sharing (config, precision) share one
+operator plan; the macro-steps of all instances (Euler or projective forward
+Euler, src/boltzmann.py:82-84,120-128, with df = dt Q(f) / kn) are captured
+into one CUDA graph on the first call of :meth:`Ensemble.step` and replayed as a
+single launch afterwards.
+
+This generalises the reference's per-problem driver loop to a batch; the
+reference has no ensemble driver of its own.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from .collision import FSInelasticVHSCollision, SpectralMesh
+
+_INT = {"Euler": _lib.INT_EULER, "PFE": _lib.INT_PFE}
+
+
+def _key(config):
+    vm, sd, cm = config["velocity-mesh"], config["spherical-design-rule"], config["collision-model"]
+    return (int(vm["nv"]), float(vm["s"]), int(vm.get("nr", int(vm["nv"]) // 2)), int(sd["nsphr"]),
+            float(cm.get("e", 1.0)), float(cm.get("e0", 1.0)), float(cm.get("gamma", 0.0)))
+
+
+class Ensemble:
+    def __init__(self, configs, f0s, dt, kn=1.0, integrator="PFE", inner_steps=(2,), inner_dt=None,
+                 precision="mixed", with_loss=True, mass_fix=False, device=0):
+        if len(configs) != len(f0s):
+            raise ValueError("one initial state per configuration")
+        if integrator not in _INT:
+            raise NotImplementedError("This time integrator is not implemented.")
+        self.device = int(device)
+        self.dt, self.kn = float(dt), float(kn)
+        self.integrator = integrator
+        self.K = np.ascontiguousarray(list(inner_steps) + [0, 0], np.int32)[:3]
+        self.h = np.ascontiguousarray(list(inner_dt or [dt]) + [0.0, 0.0], np.float64)[:3]
+        self.with_loss, self.mass_fix = bool(with_loss), bool(mass_fix)
+        self.meshes, self.ops, self.f = [], [], []
+        ops = {}
+        for cfg, f0 in zip(configs, f0s):
+            k = _key(cfg)
+            if k not in ops:
+                sm = SpectralMesh(cfg)
+                ops[k] = (sm, FSInelasticVHSCollision(cfg, sm, precision=precision, with_loss=with_loss,
+                                                       mass_fix=mass_fix, batch_max=1, device=device))
+            sm, op = ops[k]
+            f = torch.as_tensor(np.asarray(f0, np.float64), device=f"cuda:{self.device}").contiguous()
+            if tuple(f.shape) != (sm.nv,) * 3:
+                raise ValueError(f"initial state of shape {tuple(f.shape)} for a {sm.nv}^3 grid")
+            self.meshes.append(sm)
+            self.ops.append(op)
+            self.f.append(f)
+        for op in {id(o): o for o in self.ops}.values():
+            op.plan  # build every plan (and its kernel attributes) before any capture
+        self._graph = None
+        self._stream = torch.cuda.Stream(device=self.device)
+
+    def _launch_all(self, stream):
+        v1 = np.zeros(1)
+        for op, f in zip(self.ops, self.f):
+            plan = op.plan
+            st = plan._lib.pii_step(plan.handle, _INT[self.integrator], f.data_ptr(), 1, self.dt, _lib.iptr(self.K),
+                                    _lib.dptr(self.h), 1, 0.0, _lib.dptr(v1), _lib.BC_EXTRAP, _lib.BC_EXTRAP, self.kn,
+                                    int(self.with_loss), int(self.mass_fix), 0, stream)
+            _lib.check(st, "pii_step")
+
+    def step(self, use_graph=True):
+        """One macro-step of every instance (one CUDA-graph launch after the first call)."""
+        cur = torch.cuda.current_stream(self.device)
+        self._stream.wait_stream(cur)
+        with torch.cuda.stream(self._stream):
+            if not use_graph:
+                self._launch_all(self._stream.cuda_stream)
+            else:
+                if self._graph is None:
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g, stream=self._stream):
+                        self._launch_all(torch.cuda.current_stream(self.device).cuda_stream)
+                    self._graph = g
+                self._graph.replay()
+        cur.wait_stream(self._stream)
+
+    def moments(self):
+        """FP64 (rho, u[3], T) of every instance."""
+        out = []
+        for sm, f in zip(self.meshes, self.f):
+            v = sm.v_center
+            V = np.meshgrid(v, v, v, indexing="ij")
+            Vt = [torch.as_tensor(x, device=f.device) for x in V]
+            dv = sm.delta**3
+            rho = float(f.sum()) * dv
+            u = np.array([float((f * Vt[d]).sum()) * dv / rho for d in range(3)])
+            E = 0.5 * float((f * (Vt[0] ** 2 + Vt[1] ** 2 + Vt[2] ** 2)).sum()) * dv
+            out.append((rho, u, (2.0 / 3.0) * (E / rho - 0.5 * float((u**2).sum()))))
+        return out
