@@ -320,6 +320,7 @@ def main():
     cfg = op_config()
     sm = pkg.SpectralMesh(cfg)
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=NX, device=local)
+    tune_ms, tuning = col.plan.autotune(NX)  # kernel choices for this batch, timed on the device
     f0_host = sod_state(sm.v_center)
     sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": NX, "nv": NV},
                        device=local)
@@ -446,7 +447,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "cells": NX, "n_v": NV, "n_r": NR, "n_sigma": NS,
                    "cell_evals_per_step": CELL_EVALS_PER_STEP, "l2": "flushed (256 MB write) between timed steps",
-                   "graph": "each macro-step replayed as one CUDA graph", "parallelism": f"replicas x{world}"},
+                   "graph": "each macro-step replayed as one CUDA graph", "parallelism": f"replicas x{world}",
+                   "tuning": tuning},
         "clocks": ck, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
         "kernels": stages, "hbm_peak_gbs": hbm_peak,
     }

@@ -90,6 +90,18 @@ int64_t pii_plan_workspace_bytes(const pii_plan* plan);
 int pii_plan_set_gain_path(pii_plan* plan, int path);
 
 /*
+ * Autotuner (no reference counterpart): times, for `cells` cells, every
+ * candidate of the plan's kernel choices -- gain path (cluster / pipeline),
+ * work items per resident cluster (2, 4, 6, 8), pipeline chunk size (64K to
+ * 512K velocity points) -- on scratch inputs it allocates and frees itself,
+ * keeps the fastest and drops captured step graphs.  best_ms (may be NULL)
+ * receives the best time of one Q evaluation.  Synchronises the stream.
+ * pii_plan_get_tuning reads the current choices.
+ */
+int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stream);
+int pii_plan_get_tuning(const pii_plan* plan, int* gain_path, int* items_per_cluster, int64_t* chunk_points);
+
+/*
  * q = Q+(f,f) [- Q-(f,f) if with_loss] [+ heat_bath * Lap_v f], per cell.
  * Replaces BaseCollision.__call__ (src/collision/base.py:32-58) and
  * FSInelasticVHSCollision.collide / laplacian

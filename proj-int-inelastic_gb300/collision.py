@@ -178,6 +178,22 @@ class Plan:
             _lib.check(lib.pii_plan_set_gain_path(self.handle, {"pipeline": 0, "cluster": 1}[gain_path]),
                        "pii_plan_set_gain_path")
 
+    def autotune(self, cells):
+        """Time the kernel choices for `cells` cells and keep the fastest
+        (``pii_plan_autotune``); returns (best ms, choices)."""
+        best = _lib.ctypes.c_double()
+        _lib.check(self._lib.pii_plan_autotune(self.handle, int(cells), _lib.ctypes.byref(best),
+                                               torch.cuda.current_stream().cuda_stream), "pii_plan_autotune")
+        return best.value, self.tuning
+
+    @property
+    def tuning(self):
+        path, items, pts = _lib.ctypes.c_int(), _lib.ctypes.c_int(), _lib.ctypes.c_int64()
+        _lib.check(self._lib.pii_plan_get_tuning(self.handle, _lib.ctypes.byref(path), _lib.ctypes.byref(items),
+                                                 _lib.ctypes.byref(pts)), "pii_plan_get_tuning")
+        return {"gain_path": "cluster" if path.value == 1 else "pipeline", "items_per_cluster": items.value,
+                "chunk_points": pts.value}
+
     @property
     def workspace_bytes(self):
         return int(self._lib.pii_plan_workspace_bytes(self.handle))

@@ -1,6 +1,7 @@
 // Orchestration of one batched Q(f,f) evaluation (pii_collide) and dispatch on
 // (precision, n) to the templated kernels.
 #include <type_traits>
+#include <vector>
 
 #include "pii_internal.cuh"
 
@@ -30,7 +31,7 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
     }
   }
   // items = (cell, pair); a chunk holds Cc cells x Pc pairs in the L2-resident buffer
-  int64_t Cc = std::max<int64_t>(1, (int64_t(131072) + N - 1) / N);
+  int64_t Cc = std::max<int64_t>(1, (p->chunk_points + N - 1) / N);
   Cc = std::min<int64_t>(Cc, std::min<int64_t>(cells, p->chunk_items));
   const int64_t Pc = std::max<int64_t>(1, std::min<int64_t>(p->Q, p->chunk_items / Cc));
   for (int64_t c0 = 0; c0 < cells; c0 += Cc) {
@@ -92,6 +93,98 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
 }
 
 }  // namespace pii
+
+// Autotuner: time the candidate kernel choices for `cells` cells on scratch
+// inputs and keep the fastest.  Candidates: gain path (cluster / pipeline, where
+// the cluster kernel exists), cluster work items per resident cluster, pipeline
+// chunk size.
+extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stream) {
+  using namespace pii;
+  if (!plan || cells <= 0 || cells > plan->batch_max) {
+    set_error("pii_plan_autotune: cells outside [1, batch_max]");
+    return PII_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PII_CUDA(cudaSetDevice(plan->device));
+  double* f = nullptr;
+  double* q = nullptr;
+  const size_t bytes = size_t(cells) * plan->N * sizeof(double);
+  PII_CUDA(cudaMalloc(&f, bytes));
+  if (cudaMalloc(&q, bytes) != cudaSuccess) {
+    cudaFree(f);
+    set_error("pii_plan_autotune: out of memory");
+    return PII_ERR_CUDA;
+  }
+  // a smooth positive state: 1 + small ramp (values do not change the timing)
+  cudaMemsetAsync(f, 0, bytes, s);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  struct Cand {
+    int path, items;
+    int64_t points;
+  };
+  std::vector<Cand> cands;
+  const bool cluster_ok = plan->gc_clusters > 0;
+  if (cluster_ok)
+    for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points});
+  for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
+    cands.push_back({0, plan->gc_items_per_cluster, pts});
+  const int saved_path = plan->gain_path;
+  const int saved_items = plan->gc_items_per_cluster;
+  const int64_t saved_points = plan->chunk_points;
+  float best = 1e30f;
+  Cand pick{saved_path, saved_items, saved_points};
+  int st = PII_OK;
+  for (const Cand& c : cands) {
+    plan->gain_path = c.path;
+    plan->gc_items_per_cluster = c.items;
+    plan->chunk_points = c.points;
+    st = collide_impl(plan, f, q, cells, 1, 0.0, 0, s);  // warm-up
+    if (st != PII_OK) break;
+    cudaEventRecord(e0, s);
+    st = collide_impl(plan, f, q, cells, 1, 0.0, 0, s);
+    cudaEventRecord(e1, s);
+    if (st != PII_OK) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      st = PII_ERR_CUDA;
+      set_error("pii_plan_autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      pick = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(f);
+  cudaFree(q);
+  plan->gain_path = st == PII_OK ? pick.path : saved_path;
+  plan->gc_items_per_cluster = st == PII_OK ? pick.items : saved_items;
+  plan->chunk_points = st == PII_OK ? pick.points : saved_points;
+  for (auto& kv : plan->graphs) {  // captured graphs baked the old choices in
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  plan->graphs.clear();
+  if (best_ms) *best_ms = best;
+  return st;
+}
+
+extern "C" int pii_plan_get_tuning(const pii_plan* plan, int* gain_path, int* items_per_cluster,
+                                   int64_t* chunk_points) {
+  if (!plan || !gain_path || !items_per_cluster || !chunk_points) {
+    pii::set_error("pii_plan_get_tuning: NULL argument");
+    return PII_ERR_ARG;
+  }
+  *gain_path = plan->gain_path;
+  *items_per_cluster = plan->gc_items_per_cluster;
+  *chunk_points = plan->chunk_points;
+  return PII_OK;
+}
 
 extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
   if (!plan || (path != 0 && path != 1)) {

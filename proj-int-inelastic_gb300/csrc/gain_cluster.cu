@@ -327,10 +327,10 @@ int gain_cluster_prepare(pii_plan* p) {
     return PII_ERR_CUDA;
   }
   p->gc_clusters = nclus;
-  // per-part Hermitian slots: at most (6 * clusters + batch_max) work items, and
+  // per-part Hermitian slots: at most (8 * clusters + batch_max) work items, and
   // never more than batch_max cells x Q / 8 parts
   const int64_t max_items =
-      std::min<int64_t>(int64_t(6) * nclus + p->batch_max, p->batch_max * std::max(1, p->Q / 8));
+      std::min<int64_t>(int64_t(8) * nclus + p->batch_max, p->batch_max * std::max(1, p->Q / 8));
   PII_CUDA(cudaMalloc(&p->gc_hpart, size_t(max_items) * 2 * 16 * HSLOTS * sizeof(float2)));
   p->bytes += max_items * 2 * 16 * HSLOTS * int64_t(sizeof(float2));
   p->gc_max_items = max_items;
@@ -340,7 +340,7 @@ int gain_cluster_prepare(pii_plan* p) {
 int gain_cluster_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   using namespace gc;
   const int nclus = p->gc_clusters;
-  int parts = int(std::max<int64_t>(1, (int64_t(6) * nclus + cells - 1) / cells));
+  int parts = int(std::max<int64_t>(1, (int64_t(p->gc_items_per_cluster) * nclus + cells - 1) / cells));
   parts = std::min(parts, std::max(1, p->Q / 8));
   while (cells * parts > p->gc_max_items && parts > 1) --parts;
   parts = (p->Q + (p->Q + parts - 1) / parts - 1) / ((p->Q + parts - 1) / parts);  // no empty parts

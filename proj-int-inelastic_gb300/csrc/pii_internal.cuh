@@ -116,6 +116,10 @@ struct pii_plan {
   double delta3 = 0;        // velocity cell volume of the last splitting step
   // fused 2-CTA-cluster gain kernel (n = 32, FP32): 1 = use it, 0 = column/plane pipeline
   int gain_path = 0;
+  // tunables (pii_plan_autotune): work items per resident cluster, and the
+  // points per chunk of the pipeline path (cells per chunk = this / n^3)
+  int gc_items_per_cluster = 6;
+  int64_t chunk_points = 131072;
   int gc_clusters = 0;
   int64_t gc_max_items = 0;
   void* gc_maps = nullptr;   // int2 thread -> columns [512], column -> slot [1024]

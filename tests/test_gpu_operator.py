@@ -140,6 +140,23 @@ def test_cluster_kernel_matches_pipeline_and_fp64(cells):
             assert rel_linf(qc[c].cpu().numpy(), qp[c].cpu().numpy()) < 1e-5, (wl, c)
 
 
+def test_autotuner_keeps_results():
+    """pii_plan_autotune picks a kernel configuration; results stay within tolerance."""
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 16, 32, 0.8, 0.8, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=8)
+    best, choice = col.plan.autotune(8)
+    assert best > 0 and choice["gain_path"] in ("cluster", "pipeline")
+    assert choice["items_per_cluster"] in (2, 4, 6, 8)
+    v = sm.v_center
+    f = torch.as_tensor(np.stack([maxwellian(v, 1.0, (0.3 * c, 0, 0), 1.0) for c in range(8)]), device="cuda:0")
+    ref = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=8).collide(f, with_loss=True)
+    q = col.collide(f, with_loss=True)
+    for c in range(8):
+        assert rel_linf(q[c].cpu().numpy(), ref[c].cpu().numpy()) < 1e-5
+
+
 def test_mass_fix_conserves_mass_fp32():
     pkg = _pkg()
     cfg = op_config(32, L8_S, 32, 32, 0.9, 0.9, 1.0)
