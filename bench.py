@@ -183,7 +183,7 @@ def time_torch_fp64(mesh, f_dev, cells, device):
 # ---------------------------------------------------------------------------
 # CPU baseline (the oracle restatement of the reference operator, host cores)
 # ---------------------------------------------------------------------------
-def cpu_baseline(budget_s=15.0, max_cells=16):
+def cpu_baseline(budget_s=15.0, max_cells=64):
     import numpy as np
 
     from oracle import fs_inelastic as fo
@@ -299,6 +299,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the plan's default kernel choices")
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: run 3 Q(f,f) evaluations on this many cells of the workload and exit")
     args = ap.parse_args()
@@ -320,7 +321,10 @@ def main():
     cfg = op_config()
     sm = pkg.SpectralMesh(cfg)
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=NX, device=local)
-    tune_ms, tuning = col.plan.autotune(NX)  # kernel choices for this batch, timed on the device
+    if args.no_autotune:
+        tuning = col.plan.tuning
+    else:
+        tune_ms, tuning = col.plan.autotune(NX)  # kernel choices for this batch, timed on the device
     f0_host = sod_state(sm.v_center)
     sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": NX, "nv": NV},
                        device=local)
