@@ -83,16 +83,18 @@ int64_t pii_plan_workspace_bytes(const pii_plan* plan);
 
 /*
  * Kernel choice for the gain term of n = 32 FP32 plans (tuning knob, no
- * reference counterpart): 1 = the fused 2-CTA-cluster kernel (the default
- * where it exists), 0 = the column / plane pass pipeline used for every other
- * size and for FP64.  Both compute the same operator.
+ * reference counterpart): 2 = the fused a-parity kernel with its accumulator in
+ * tensor memory (the default where it exists), 1 = the fused 2-CTA-cluster
+ * kernel, 0 = the column / plane pass pipeline used for every other size and
+ * for FP64.  All compute the same operator.
  */
 int pii_plan_set_gain_path(pii_plan* plan, int path);
 
 /*
  * Autotuner (no reference counterpart): times, for `cells` cells, every
- * candidate of the plan's kernel choices -- gain path (cluster / pipeline),
- * work items per resident cluster (2, 4, 6, 8), pipeline chunk size (64K to
+ * candidate of the plan's kernel choices -- gain path (a-parity / cluster /
+ * pipeline), work items per resident cluster or CTA (2, 4, 6, 8), pipeline
+ * chunk size (64K to
  * 512K velocity points) -- on scratch inputs it allocates and frees itself,
  * keeps the fastest and drops captured step graphs.  best_ms (may be NULL)
  * receives the best time of one Q evaluation.  Synchronises the stream.
@@ -100,6 +102,9 @@ int pii_plan_set_gain_path(pii_plan* plan, int path);
  */
 int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stream);
 int pii_plan_get_tuning(const pii_plan* plan, int* gain_path, int* items_per_cluster, int64_t* chunk_points);
+/* Restores choices read by pii_plan_get_tuning (e.g. saved from an earlier
+ * autotune); drops captured step graphs.  items_per_cluster in [1, 64]. */
+int pii_plan_set_tuning(pii_plan* plan, int gain_path, int items_per_cluster, int64_t chunk_points);
 
 /*
  * q = Q+(f,f) [- Q-(f,f) if with_loss] [+ heat_bath * Lap_v f], per cell.

@@ -151,6 +151,9 @@ def _precision_of(config, precision):
     raise ValueError(f"precision must be 'mixed'/'fp32' or 'double'/'fp64', got {precision!r}")
 
 
+GAIN_PATHS = {"pipeline": 0, "cluster": 1, "parity": 2}
+
+
 class Plan:
     """Owner of one ``pii_plan`` (device tables + workspace for batch_max cells)."""
 
@@ -175,8 +178,7 @@ class Plan:
         self.handle = h.value
         self._lib = lib
         if gain_path is not None:
-            _lib.check(lib.pii_plan_set_gain_path(self.handle, {"pipeline": 0, "cluster": 1}[gain_path]),
-                       "pii_plan_set_gain_path")
+            _lib.check(lib.pii_plan_set_gain_path(self.handle, GAIN_PATHS[gain_path]), "pii_plan_set_gain_path")
 
     def autotune(self, cells):
         """Time the kernel choices for `cells` cells and keep the fastest
@@ -186,12 +188,17 @@ class Plan:
                                                torch.cuda.current_stream().cuda_stream), "pii_plan_autotune")
         return best.value, self.tuning
 
+    def set_tuning(self, gain_path, items_per_cluster, chunk_points, **_):
+        """Restore choices (as returned by :attr:`tuning`), ``pii_plan_set_tuning``."""
+        _lib.check(self._lib.pii_plan_set_tuning(self.handle, GAIN_PATHS[gain_path], int(items_per_cluster),
+                                                 int(chunk_points)), "pii_plan_set_tuning")
+
     @property
     def tuning(self):
         path, items, pts = _lib.ctypes.c_int(), _lib.ctypes.c_int(), _lib.ctypes.c_int64()
         _lib.check(self._lib.pii_plan_get_tuning(self.handle, _lib.ctypes.byref(path), _lib.ctypes.byref(items),
                                                  _lib.ctypes.byref(pts)), "pii_plan_get_tuning")
-        return {"gain_path": "cluster" if path.value == 1 else "pipeline", "items_per_cluster": items.value,
+        return {"gain_path": {v: k for k, v in GAIN_PATHS.items()}[path.value], "items_per_cluster": items.value,
                 "chunk_points": pts.value}
 
     @property
@@ -229,9 +236,10 @@ class FSInelasticVHSCollision:
     * ``mass_fix``   -- subtract the per-cell mean of Q in FP64 (k = 0 mode);
     * ``batch_max``  -- initial cell capacity of the plan (grown on demand);
     * ``device``     -- CUDA device index;
-    * ``gain_path``  -- "cluster" (fused 2-CTA-cluster kernel, the default for
-      n = 32 in mixed precision) or "pipeline" (column / plane passes, every
-      other case); both evaluate the same operator.
+    * ``gain_path``  -- "parity" (fused a-parity kernel with a tensor-memory
+      accumulator, the default for n = 32 in mixed precision), "cluster" (fused
+      2-CTA-cluster kernel, n = 32 mixed) or "pipeline" (column / plane passes,
+      every case); all evaluate the same operator.
     """
 
     collision_model = "vhs"

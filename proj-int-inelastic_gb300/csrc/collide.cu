@@ -25,8 +25,8 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
   const int64_t N = p->N;
   PII_TRY(K::fwd(p, f, 0, cells, s));
   if constexpr (std::is_same<T, float>::value && NV == 32) {
-    if (p->gain_path == 1) {
-      PII_TRY(gain_cluster_run(p, cells, s));
+    if (p->gain_path == 1 || p->gain_path == 2) {
+      PII_TRY(p->gain_path == 1 ? gain_cluster_run(p, cells, s) : gain_parity_run(p, cells, s));
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
   }
@@ -95,9 +95,9 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
 }  // namespace pii
 
 // Autotuner: time the candidate kernel choices for `cells` cells on scratch
-// inputs and keep the fastest.  Candidates: gain path (cluster / pipeline, where
-// the cluster kernel exists), cluster work items per resident cluster, pipeline
-// chunk size.
+// inputs and keep the fastest.  Candidates: gain path (a-parity / cluster /
+// pipeline, where the fused kernels exist), work items per resident cluster or
+// CTA, pipeline chunk size.
 extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stream) {
   using namespace pii;
   if (!plan || cells <= 0 || cells > plan->batch_max) {
@@ -127,7 +127,8 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
   std::vector<Cand> cands;
   const bool cluster_ok = plan->gc_clusters > 0;
   if (cluster_ok)
-    for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points});
+    for (int path : {1, 2})
+      for (int items : {2, 4, 6, 8}) cands.push_back({path, items, plan->chunk_points});
   for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
     cands.push_back({0, plan->gc_items_per_cluster, pts});
   const int saved_path = plan->gain_path;
@@ -186,13 +187,30 @@ extern "C" int pii_plan_get_tuning(const pii_plan* plan, int* gain_path, int* it
   return PII_OK;
 }
 
-extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
-  if (!plan || (path != 0 && path != 1)) {
-    pii::set_error("pii_plan_set_gain_path: path must be 0 (pipeline) or 1 (cluster)");
+extern "C" int pii_plan_set_tuning(pii_plan* plan, int gain_path, int items_per_cluster, int64_t chunk_points) {
+  if (!plan || items_per_cluster < 1 || items_per_cluster > 64 || chunk_points < 1) {
+    pii::set_error("pii_plan_set_tuning: items_per_cluster must be in [1, 64] and chunk_points positive");
     return PII_ERR_ARG;
   }
-  if (path == 1 && (plan->gc_clusters <= 0 || plan->precision != PII_PREC_FP32 || plan->n != 32)) {
-    pii::set_error("pii_plan_set_gain_path: the cluster kernel exists for n = 32, FP32 plans only");
+  const int st = pii_plan_set_gain_path(plan, gain_path);
+  if (st != PII_OK) return st;
+  plan->gc_items_per_cluster = items_per_cluster;
+  plan->chunk_points = chunk_points;
+  for (auto& kv : plan->graphs) {  // captured graphs baked the old choices in
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  plan->graphs.clear();
+  return PII_OK;
+}
+
+extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
+  if (!plan || path < 0 || path > 2) {
+    pii::set_error("pii_plan_set_gain_path: path must be 0 (pipeline), 1 (cluster) or 2 (a-parity)");
+    return PII_ERR_ARG;
+  }
+  if (path != 0 && (plan->gc_clusters <= 0 || plan->gp_ctas <= 0)) {
+    pii::set_error("pii_plan_set_gain_path: the fused kernels exist for n = 32, FP32 plans only");
     return PII_ERR_ARG;
   }
   plan->gain_path = path;

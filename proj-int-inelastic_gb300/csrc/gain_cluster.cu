@@ -29,26 +29,16 @@
 
 #include <algorithm>
 
-#include "fft_reg.cuh"
-#include "pii_internal.cuh"
+#include "gain_common.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace pii {
 
 namespace gc {
-constexpr int NV = 32, N2 = 1024, N3 = 32768;
-constexpr int THREADS = 512;
-constexpr int PLANES = 16;
-constexpr int HSLOTS = 514;
 constexpr size_t SMEM = size_t(PLANES) * N2 * sizeof(float2) + size_t(16) * HSLOTS * sizeof(float2);
-
-__host__ __device__ constexpr int neg_col(int j) {
-  return (((NV - (j >> 5)) & 31) << 5) | ((NV - (j & 31)) & 31);
-}
 // index of k_a = -(2 m + par) within the parity half
 __host__ __device__ constexpr int neg_m(int m, int par) { return par == 0 ? ((16 - m) & 15) : (15 - m); }
-__device__ __forceinline__ int widx(int plane, int b, int c) { return plane * N2 + b * 32 + (c ^ b); }
 }  // namespace gc
 
 struct GainClusterArgs {
@@ -186,39 +176,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_cluster(GainClusterArgs
       }
       __syncthreads();
       // ---- B: warp `warp` owns plane `warp`; lane = row / column index
-      {
-        float2 x[32];
-        float2* P = W + warp * N2;
-#pragma unroll
-        for (int c = 0; c < 32; ++c) x[c] = P[lane * 32 + (c ^ lane)];
-        fft_line<32, +1>(x);
-        static_for<0, 32>([&](auto ci) {
-          constexpr int c = decltype(ci)::value;
-          P[lane * 32 + (c ^ lane)] = x[pos(32, c)];
-        });
-        __syncwarp();
-#pragma unroll
-        for (int b = 0; b < 32; ++b) x[b] = P[b * 32 + (lane ^ b)];
-        fft_line<32, +1>(x);
-        float2 y[32];
-        static_for<0, 32>([&](auto bi) {
-          constexpr int b = decltype(bi)::value;
-          y[b] = cscale(x[pos(32, b)], fr[b * 32]);
-        });
-        fft_line<32, -1>(y);
-        static_for<0, 32>([&](auto ki) {
-          constexpr int k = decltype(ki)::value;
-          P[k * 32 + (lane ^ k)] = y[pos(32, k)];
-        });
-        __syncwarp();
-#pragma unroll
-        for (int c = 0; c < 32; ++c) x[c] = P[lane * 32 + (c ^ lane)];
-        fft_line<32, -1>(x);
-        static_for<0, 32>([&](auto ki) {
-          constexpr int k = decltype(ki)::value;
-          P[lane * 32 + (k ^ lane)] = x[pos(32, k)];
-        });
-      }
+      plane_pass(W + warp * N2, fr, lane);
       cluster.sync();  // both CTAs' planes are final for this pair
       // ---- C
       if (crank == 0)
@@ -263,15 +221,10 @@ __global__ void __launch_bounds__(256) k_herm_expand(float2* G, const float2* hp
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-int gain_cluster_prepare(pii_plan* p) {
+bool gc::build_column_map(std::vector<int4>& uc, std::vector<int2>& cs) {
   using namespace gc;
-  PII_CUDA(cudaFuncSetAttribute(k_gain_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM)));
-  // Stage-C work of each thread: a column pair {j, -j} (one slot) or two
-  // self-conjugate columns (two slots).  Warps 0..14 take rows 1..15 (every
-  // column); warp 15 takes rows 0 and 16, one row per half-warp, so its
-  // shared-memory accesses are conflict-free like the other warps'.
-  std::vector<int4> uc(THREADS);
-  std::vector<int2> cs(N2, make_int2(-1, -1));
+  uc.assign(THREADS, make_int4(0, 0, 0, 0));
+  cs.assign(N2, make_int2(-1, -1));
   int slot = 0;
   auto pair_unit = [&](int t, int j) {
     const int nj = neg_col(j);
@@ -292,12 +245,17 @@ int gain_cluster_prepare(pii_plan* p) {
     slot += 2;
   }
   for (int j = 0; j < N2; ++j)
-    if (cs[j].x < 0) {
-      set_error("gain_cluster_prepare: column %d has no slot", j);
-      return PII_ERR_ARG;
-    }
-  if (slot != HSLOTS) {
-    set_error("gain_cluster_prepare: %d slots, expected %d", slot, HSLOTS);
+    if (cs[j].x < 0) return false;
+  return slot == HSLOTS;
+}
+
+int gain_cluster_prepare(pii_plan* p) {
+  using namespace gc;
+  PII_CUDA(cudaFuncSetAttribute(k_gain_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM)));
+  std::vector<int4> uc;
+  std::vector<int2> cs;
+  if (!build_column_map(uc, cs)) {
+    set_error("gain_cluster_prepare: column map does not cover the %d columns", N2);
     return PII_ERR_ARG;
   }
   void* d = nullptr;

@@ -57,9 +57,15 @@ enum Stage {
 //   lossk  [M+1] real        : sum_r 4 pi r^{gamma+2} w_r sinc(pi r sqrt(m) / L)
 //   lapl   [M+1] real        : -pi^2 m / L^2
 // with k the signed spectral index of the storage position and m = |k|^2 <= M = 3 (n/2)^2.
+// For n = 32 in FP32 the a-parity kernel also keeps, per pair and parity p
+// (W = exp(-2 pi i / 32), e_a / g_a the d = 0 rows above):
+//   epar [Q][2][32] complex  : W^{-p k} e_a[k] (k < 16), (-1)^p W^{-p k} e_a[k + 16]
+//   gpar [Q][2][32] complex  : W^{p k} g_a[k]
 struct Tables {
   void* ephase = nullptr;
   void* gphase = nullptr;
+  void* epar = nullptr;
+  void* gpar = nullptr;
   void* gsinc = nullptr;
   void* lossk = nullptr;
   void* lapl = nullptr;
@@ -114,7 +120,8 @@ struct pii_plan {
   double* mom = nullptr;    // batch_max * 5 FP64 moment sums (CONSP_M)
   int* flag = nullptr;      // device flag of pii_state_check
   double delta3 = 0;        // velocity cell volume of the last splitting step
-  // fused 2-CTA-cluster gain kernel (n = 32, FP32): 1 = use it, 0 = column/plane pipeline
+  // gain kernel for n = 32, FP32: 0 = column/plane pipeline, 1 = fused
+  // 2-CTA-cluster kernel, 2 = fused a-parity kernel (tensor-memory accumulator)
   int gain_path = 0;
   // tunables (pii_plan_autotune): work items per resident cluster, and the
   // points per chunk of the pipeline path (cells per chunk = this / n^3)
@@ -124,6 +131,9 @@ struct pii_plan {
   int64_t gc_max_items = 0;
   void* gc_maps = nullptr;   // int2 thread -> columns [512], column -> slot [1024]
   void* gc_hpart = nullptr;  // per-part Hermitian slots
+  int gp_ctas = 0;           // resident CTAs of the a-parity kernel
+  int64_t gp_max_items = 0;
+  void* gp_hpart = nullptr;  // its per-item Hermitian slots
   int64_t bytes = 0;
   std::map<pii::GraphKey, pii::GraphEntry> graphs;
   // per-stage CUDA-event profiling (pii_plan_profile)
@@ -155,6 +165,9 @@ int prepare_impl(pii_plan* p);
 // gain_cluster.cu
 int gain_cluster_prepare(pii_plan* p);
 int gain_cluster_run(pii_plan* p, int64_t cells, cudaStream_t s);
+// gain_parity.cu
+int gain_parity_prepare(pii_plan* p);
+int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // transport.cu
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
                    double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "pii_internal.cuh"
 
@@ -111,6 +112,42 @@ static int upload_tables(pii_plan* p) {
       }
     }
   }
+  if (std::is_same<T, float>::value && n == 32) {
+    // a-parity rows: the first-axis rows with the radix-2 twiddles of the
+    // parity split folded in, evaluated in FP64 (angles reduced exactly)
+    std::vector<T> ep2(size_t(Q) * 2 * 32 * 2), gp2(size_t(Q) * 2 * 32 * 2);
+    for (int ir = 0; ir < nr; ++ir) {
+      const double r = p->r[ir];
+      const double er = 0.5 * (p->e0 - p->e) * std::tanh(r - 0.5 * p->R) + 0.5 * (p->e0 + p->e);
+      const double afac = 0.25 * pi * (1.0 + er) / p->L;
+      for (int is = 0; is < ns; ++is) {
+        const int pair = ir * ns + is;
+        const double sd = p->sigma[size_t(is) * 3];
+        for (int par = 0; par < 2; ++par)
+          for (int k = 0; k < 32; ++k) {
+            const size_t o = ((size_t(pair) * 2 + par) * 32 + k) * 2;
+            // epar: k < 16 pairs e_a[k], k >= 16 pairs e_a[k] with the sign (-1)^p
+            const int kk = k & 15;
+            const int ks = k < 16 ? k : k - 32;
+            const double th_e = -pi * r * sd * double(ks) / p->L + 2.0 * pi * double(par * kk) / 32.0 +
+                                (k >= 16 && par ? pi : 0.0);
+            ep2[o] = T(invN * std::cos(th_e));
+            ep2[o + 1] = T(invN * std::sin(th_e));
+            const double th_g = afac * r * sd * double(ks) - 2.0 * pi * double(par * k) / 32.0;
+            gp2[o] = T(std::cos(th_g));
+            gp2[o + 1] = T(std::sin(th_g));
+          }
+      }
+    }
+    auto up2 = [&](void** dst, const std::vector<T>& v) -> int {
+      PII_CUDA(cudaMalloc(dst, v.size() * sizeof(T)));
+      PII_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+      p->bytes += int64_t(v.size() * sizeof(T));
+      return PII_OK;
+    };
+    PII_TRY(up2(&p->tab.epar, ep2));
+    PII_TRY(up2(&p->tab.gpar, gp2));
+  }
   for (int m = 0; m <= M; ++m) {
     lk[m] = T(lk_d[m]);
     lp[m] = T(-pi * pi / (p->L * p->L) * double(m));  // (:69)
@@ -143,9 +180,9 @@ static void free_plan(pii_plan* p) {
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
   }
-  void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
+  void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
-                  p->gc_maps,    p->gc_hpart,   p->mom,       p->flag};
+                  p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->mom,       p->flag};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -219,11 +256,11 @@ static int create(pii_plan** out, int n, int nr, int ns, const double* r, const 
     return s2;
   }
   if (n == 32 && precision == PII_PREC_FP32) {
-    if ((s2 = gain_cluster_prepare(p)) != PII_OK) {
+    if ((s2 = gain_cluster_prepare(p)) != PII_OK || (s2 = gain_parity_prepare(p)) != PII_OK) {
       free_plan(p);
       return s2;
     }
-    p->gain_path = 1;
+    p->gain_path = 2;
   }
   *out = p;
   return PII_OK;

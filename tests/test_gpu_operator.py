@@ -118,10 +118,12 @@ def test_full_size_properties_c2():
     assert float((q7[0] - q[7]).abs().max() / q[7].abs().max()) < 1e-6
 
 
+@pytest.mark.parametrize("path", ["cluster", "parity"])
 @pytest.mark.parametrize("cells", [1, 3, 128])
-def test_cluster_kernel_matches_pipeline_and_fp64(cells):
-    """n = 32 mixed precision: the fused 2-CTA-cluster gain kernel against the
-    column / plane pipeline and against the FP64 path, gain and gain - loss."""
+def test_fused_kernel_matches_pipeline_and_fp64(cells, path):
+    """n = 32 mixed precision: the fused gain kernels (2-CTA cluster, a-parity)
+    against the column / plane pipeline and against the FP64 path, gain and
+    gain - loss."""
     pkg = _pkg()
     cfg = op_config(32, L8_S, 32, 32, 0.7, 0.9, 1.0)
     sm = pkg.SpectralMesh(cfg)
@@ -130,7 +132,7 @@ def test_cluster_kernel_matches_pipeline_and_fp64(cells):
     f = np.stack([maxwellian(v, 1.0 + 0.2 * rng.random(), rng.uniform(-2, 2, 3), rng.uniform(0.5, 2.0))
                   + 0.3 * maxwellian(v, 1.0, rng.uniform(-2, 2, 3), rng.uniform(0.5, 2.0)) for _ in range(cells)])
     f = torch.as_tensor(f, device="cuda:0")
-    clus = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=cells, gain_path="cluster")
+    clus = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=cells, gain_path=path)
     pipe = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=cells, gain_path="pipeline")
     dbl = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=cells)
     for wl in (False, True):
@@ -140,6 +142,24 @@ def test_cluster_kernel_matches_pipeline_and_fp64(cells):
             assert rel_linf(qc[c].cpu().numpy(), qp[c].cpu().numpy()) < 1e-5, (wl, c)
 
 
+@pytest.mark.parametrize("path", ["cluster", "parity"])
+def test_fused_kernel_rough_input(path):
+    """Uniform random f (spectrum up to the Nyquist planes, where exp_rs f^ is
+    not Hermitian): fused kernels against the FP64 path, with and without loss,
+    with heat bath, and with pair ranges of every length."""
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 3, 12, 0.5, 0.8, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    f = torch.as_tensor(np.random.default_rng(11).random((5, 32, 32, 32)), device="cuda:0")
+    fused = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=5, gain_path=path)
+    dbl = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=5)
+    for wl in (False, True):
+        qf, qd = fused.collide(f, with_loss=wl), dbl.collide(f, with_loss=wl)
+        assert rel_linf(qf.cpu().numpy(), qd.cpu().numpy()) < 1e-5, wl
+    qf, qd = fused(f, heat_bath=0.2), dbl(f, heat_bath=0.2)
+    assert rel_linf(np.asarray(qf.cpu()), np.asarray(qd.cpu())) < 1e-5
+
+
 def test_autotuner_keeps_results():
     """pii_plan_autotune picks a kernel configuration; results stay within tolerance."""
     pkg = _pkg()
@@ -147,7 +167,7 @@ def test_autotuner_keeps_results():
     sm = pkg.SpectralMesh(cfg)
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=8)
     best, choice = col.plan.autotune(8)
-    assert best > 0 and choice["gain_path"] in ("cluster", "pipeline")
+    assert best > 0 and choice["gain_path"] in ("parity", "cluster", "pipeline")
     assert choice["items_per_cluster"] in (2, 4, 6, 8)
     v = sm.v_center
     f = torch.as_tensor(np.stack([maxwellian(v, 1.0, (0.3 * c, 0, 0), 1.0) for c in range(8)]), device="cuda:0")
