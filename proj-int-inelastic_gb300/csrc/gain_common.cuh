@@ -23,7 +23,10 @@ __device__ __forceinline__ int widx(int plane, int b, int c) { return plane * N2
 // One warp transforms one 32 x 32 plane in place (src/collision/
 // inelastic_collisions.py:212-214 restricted to the plane's two axes):
 //   IFFT_c, IFFT_b, multiply by f(a, b, c), FFT_b, FFT_c.
-// `fr` points at f[a][0][lane] (row stride 32).
+// F_ROW = false: `fr` points at f[a][0][lane] in global memory (row stride 32);
+// F_ROW = true: `fr` points at this lane's 32 values f[a][0..31][lane],
+// contiguous and 16-byte aligned (shared memory).
+template <bool F_ROW = false>
 __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane) {
   float2 x[32];
 #pragma unroll
@@ -38,10 +41,21 @@ __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane)
   for (int b = 0; b < 32; ++b) x[b] = P[b * 32 + (lane ^ b)];
   fft_line<32, +1>(x);
   float2 y[32];
-  static_for<0, 32>([&](auto bi) {
-    constexpr int b = decltype(bi)::value;
-    y[b] = cscale(x[pos(32, b)], fr[b * 32]);
-  });
+  if constexpr (F_ROW) {
+    static_for<0, 8>([&](auto qi) {
+      constexpr int q = decltype(qi)::value;
+      const float4 fv = reinterpret_cast<const float4*>(fr)[q];
+      y[4 * q] = cscale(x[pos(32, 4 * q)], fv.x);
+      y[4 * q + 1] = cscale(x[pos(32, 4 * q + 1)], fv.y);
+      y[4 * q + 2] = cscale(x[pos(32, 4 * q + 2)], fv.z);
+      y[4 * q + 3] = cscale(x[pos(32, 4 * q + 3)], fv.w);
+    });
+  } else {
+    static_for<0, 32>([&](auto bi) {
+      constexpr int b = decltype(bi)::value;
+      y[b] = cscale(x[pos(32, b)], fr[b * 32]);
+    });
+  }
   fft_line<32, -1>(y);
   static_for<0, 32>([&](auto ki) {
     constexpr int k = decltype(ki)::value;

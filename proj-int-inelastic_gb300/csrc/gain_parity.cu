@@ -34,7 +34,12 @@ namespace pii {
 namespace gpar {
 using namespace gc;
 constexpr int TMEM_COLS = 512;
-constexpr size_t SMEM = size_t(PLANES) * N2 * sizeof(float2) + 16;
+// f of the CTA's 16 planes, transposed per plane to [c][b] with a 36-float row
+// pitch: each lane of the plane pass reads its 32 values in 16-byte loads
+// without bank conflicts
+constexpr int FPITCH = 36;
+constexpr size_t FS_OFF = size_t(PLANES) * N2 * sizeof(float2);
+constexpr size_t SMEM = FS_OFF + size_t(PLANES) * 32 * FPITCH * sizeof(float) + 16;
 }  // namespace gpar
 
 // ---- tensor-memory access (PTX tcgen05, CTA group 1)
@@ -60,8 +65,7 @@ __device__ __forceinline__ void tm_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       "%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr)
-      : "memory");
+      : "r"(taddr));
 }
 // completes the loads above; the registers are tied to it so that no use is
 // scheduled before the wait
@@ -69,19 +73,16 @@ __device__ __forceinline__ void tm_wait_ld(uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
                : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
                  "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
-                 "+r"(r[15])
-               :
-               : "memory");
+                 "+r"(r[15]));
 }
 __device__ __forceinline__ void tm_st16(uint32_t taddr, const uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
       "%14, %15, %16};" ::"r"(taddr),
       "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-      : "memory");
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]));
 }
-__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;"); }
 
 struct GainParityArgs {
   const float2* fhat;    // [cells][N3] spectra of f
@@ -90,62 +91,96 @@ struct GainParityArgs {
   const float2* gphase;  // [Q][3][32]
   const float2* epar;    // [Q][2][32]
   const float2* gpar;    // [Q][2][32]
-  const float* gsinc;    // [n_r][M + 1]
-  int M, ns, Q;
+  const float* gsx;      // [n_r][513][20]
+  int ns, Q;
   int64_t cells;
-  int parts;          // pair ranges per cell
-  float2* hpart;      // [cells * parts * 2][32][HSLOTS]
+  float2* hpart;      // [CTAs + 2 cells][32][HSLOTS]
   const int4* ucols;  // [THREADS] (column, column, first slot, 1 if two self-conjugate columns)
 };
 
-// stage A for column j: parity-PAR outputs of the inverse transform along a
+// stage A for the adjacent columns j0 = 2 t, j0 + 1 of one row: parity-PAR
+// outputs of the inverse transform along a.  Both columns come in one 16-byte
+// load per k_a and leave as one 16-byte store per plane (with the row swizzle
+// (c ^ b) the two columns stay neighbours).
 template <int PAR>
-__device__ __forceinline__ void par_stage_a(float2* W, const float2* fh, const float2* ep, const float2* epp, int j) {
+__device__ __forceinline__ void par_stage_a(float2* W, const float2* fh, const float2* ep, const float2* epp, int j0) {
   using namespace gc;
-  const int jb = j >> 5, jc = j & 31;
-  const float2 ebc = cmul(ep[32 + jb], ep[64 + jc]);
-  float2 u[16];
+  const int jb = j0 >> 5, jc = j0 & 31;
+  const float2 eb = ep[32 + jb];
+  const float4 ec = *reinterpret_cast<const float4*>(ep + 64 + jc);
+  const float2 ebc0 = cmul(eb, make_float2(ec.x, ec.y)), ebc1 = cmul(eb, make_float2(ec.z, ec.w));
+  const float4* f4 = reinterpret_cast<const float4*>(fh + j0);
+  const float4* e4 = reinterpret_cast<const float4*>(epp);
+  float2 u0[16], u1[16];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const float2 lo = fh[k * N2 + j], hi = fh[(k + 16) * N2 + j];
-    u[k] = cmul(cfma(hi, epp[16 + k], cmul(lo, epp[k])), ebc);
+  for (int k = 0; k < 16; k += 2) {
+    const float4 ea = e4[k >> 1], eb2 = e4[8 + (k >> 1)];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const float4 lo = f4[(k + d) * (N2 / 2)], hi = f4[(k + d + 16) * (N2 / 2)];
+      const float2 wa = d ? make_float2(ea.z, ea.w) : make_float2(ea.x, ea.y);
+      const float2 wb = d ? make_float2(eb2.z, eb2.w) : make_float2(eb2.x, eb2.y);
+      u0[k + d] = cmul(cfma(make_float2(hi.x, hi.y), wb, cmul(make_float2(lo.x, lo.y), wa)), ebc0);
+      u1[k + d] = cmul(cfma(make_float2(hi.z, hi.w), wb, cmul(make_float2(lo.z, lo.w), wa)), ebc1);
+    }
   }
-  fft_line<16, +1>(u);
+  fft_line<16, +1>(u0);
+  fft_line<16, +1>(u1);
+  float4* W4 = reinterpret_cast<float4*>(W);
   static_for<0, 16>([&](auto mi) {
     constexpr int m = decltype(mi)::value;
-    W[widx(m, jb, jc)] = u[pos(16, m)];
+    const float2 v0 = u0[pos(16, m)], v1 = u1[pos(16, m)];
+    // columns jc, jc + 1 share the 16-byte slot widx >> 1, swapped when the row is odd
+    W4[widx(m, jb, jc) >> 1] = (jb & 1) ? make_float4(v1.x, v1.y, v0.x, v0.y) : make_float4(v0.x, v0.y, v1.x, v1.y);
   });
 }
 
 // stage C for one column of the thread's pair: PASS 0 adds gain * X(k) to
 // region 0, PASS 1 adds conj(gain * X(-k)) to region 1, for all 32 k_a.
+// gsr = the pair's radial row of gsx: the column's 17 sinc values |k_a| = 0..16
+// come in five 16-byte loads instead of 32 scattered ones.
 template <int PASS>
 __device__ __forceinline__ void par_stage_c(const float2* W, int j, const float2* gp, const float2* gpp,
-                                            const float* gs, uint32_t treg) {
+                                            const float* gsr, uint32_t treg) {
   using namespace gc;
   const int jb = j >> 5, jc = j & 31;
+  uint32_t r[16];
+  tm_ld16(treg, r);  // chunk 0 of the accumulator, in flight during the transform
   float2 z[16];
 #pragma unroll
   for (int m = 0; m < 16; ++m) z[m] = W[widx(m, jb, jc)];
   fft_line<16, -1>(z);
   const int kb = kval(jb, 32), kc = kval(jc, 32);
-  const int mbc = kb * kb + kc * kc;
+  const float4* grow = reinterpret_cast<const float4*>(gsr + (kb * kb + kc * kc) * 20);
+  float g[20];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const float4 v = grow[i];
+    g[4 * i] = v.x;
+    g[4 * i + 1] = v.y;
+    g[4 * i + 2] = v.z;
+    g[4 * i + 3] = v.w;
+  }
   const float2 gbc = cmul(gp[32 + jb], gp[64 + jc]);
 #pragma unroll
   for (int m = 0; m < 16; ++m) z[m] = cmul(z[m], gbc);
+  const float4* gpp4 = reinterpret_cast<const float4*>(gpp);
   static_for<0, 4>([&](auto ci) {
     constexpr int c = decltype(ci)::value;
-    uint32_t r[16];
-    tm_ld16(treg + 16 * c, r);
+    if constexpr (c > 0) tm_ld16(treg + 16 * c, r);
     tm_wait_ld(r);
     static_for<0, 8>([&](auto ii) {
       constexpr int i = decltype(ii)::value;
       constexpr int k = 8 * c + i;
       constexpr int src = PASS == 0 ? k : ((32 - k) & 31);
-      constexpr int ka = kval(src, 32);
-      const float2 x = cscale(cmul(z[pos(16, src & 15)], gpp[src]), gs[mbc + ka * ka]);
-      r[2 * i] = __float_as_uint(__uint_as_float(r[2 * i]) + x.x);
-      r[2 * i + 1] = __float_as_uint(__uint_as_float(r[2 * i + 1]) + (PASS == 0 ? x.y : -x.y));
+      constexpr int q = kval(src, 32) < 0 ? -kval(src, 32) : kval(src, 32);
+      const float4 w4 = gpp4[src >> 1];
+      const float2 w = (src & 1) ? make_float2(w4.z, w4.w) : make_float2(w4.x, w4.y);
+      const float2 zz = z[pos(16, src & 15)];
+      const float re = zz.x * w.x - zz.y * w.y;
+      const float im = zz.x * w.y + zz.y * w.x;
+      r[2 * i] = __float_as_uint(fmaf(g[q], re, __uint_as_float(r[2 * i])));
+      r[2 * i + 1] = __float_as_uint(fmaf(PASS == 0 ? g[q] : -g[q], im, __uint_as_float(r[2 * i + 1])));
     });
     tm_st16(treg + 16 * c, r);
   });
@@ -155,7 +190,8 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
   using namespace gpar;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* W = reinterpret_cast<float2*>(smem_raw);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + size_t(PLANES) * N2 * sizeof(float2));
+  float* fS = reinterpret_cast<float*>(smem_raw + FS_OFF);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + SMEM - 16);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (warp == 0) {
     tm_alloc(tslot, TMEM_COLS);
@@ -168,16 +204,20 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
   // this thread's lane (32 (warp mod 4) + lane) and columns [128 (warp / 4), + 128)
   const uint32_t treg0 = tbase + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(128 * (warp >> 2));
 
-  const int64_t items = a.cells * a.parts * 2;
-  const int per_part = (a.Q + a.parts - 1) / a.parts;
+  // Work units = (cell, parity, pair) flattened with the pair fastest; CTA b takes
+  // the contiguous range [T b / G, T (b + 1) / G) of the T = 2 cells Q units,
+  // split into segments of constant (cell, parity); segment (b, cp) writes
+  // Hermitian slot set b + cp.
+  const int64_t total = a.cells * 2 * a.Q;
+  const int64_t w0 = total * blockIdx.x / gridDim.x, w1 = total * (blockIdx.x + 1) / gridDim.x;
 
-  for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
-    const int par = int(it & 1);
-    const int64_t cp = it >> 1;
-    const int64_t cell = cp / a.parts;
-    const int part = int(cp - cell * a.parts);
-    const int p0 = part * per_part;
-    const int p1 = min(a.Q, p0 + per_part);
+  for (int64_t w = w0; w < w1;) {
+    const int64_t cp = w / a.Q;
+    const int par = int(cp & 1);
+    const int64_t cell = cp >> 1;
+    const int p0 = int(w - cp * a.Q);
+    const int p1 = int(min(int64_t(a.Q), w1 - cp * a.Q));
+    w = cp * a.Q + p1;
     {
       uint32_t zr[16];
 #pragma unroll
@@ -189,36 +229,42 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       }
     }
     const float2* fh = a.fhat + cell * N3;
-    const float* fr = a.fT + cell * N3 + int64_t(2 * warp + par) * N2 + lane;  // f[cell][a][b][c = lane]
+    {
+      // fS[m][c][b] = f[cell][2 m + par][b][c] (read before the first plane pass:
+      // the stage-A barrier orders it)
+      const float* fc = a.fT + cell * N3;
+#pragma unroll 4
+      for (int i = t; i < PLANES * N2; i += THREADS) {
+        const int m = i >> 10, b = (i >> 5) & 31, c = i & 31;
+        fS[(m * 32 + c) * FPITCH + b] = fc[(2 * m + par) * N2 + b * 32 + c];
+      }
+    }
 
     for (int p = p0; p < p1; ++p) {
       // (per-pair pointers are formed inside each stage so that none stays
       // live across the register-heavy plane pass)
-      // ---- A: columns t and t + 512
+      // ---- A: columns 2 t and 2 t + 1
       {
         const float2* ep = a.ephase + int64_t(p) * 96;
         const float2* epp = a.epar + (int64_t(p) * 2 + par) * 32;
-#pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-          if (par == 0)
-            par_stage_a<0>(W, fh, ep, epp, t + 512 * h);
-          else
-            par_stage_a<1>(W, fh, ep, epp, t + 512 * h);
-        }
+        if (par == 0)
+          par_stage_a<0>(W, fh, ep, epp, 2 * t);
+        else
+          par_stage_a<1>(W, fh, ep, epp, 2 * t);
       }
       __syncthreads();
       // ---- B: warp `warp` owns local plane `warp` (a = 2 warp + par)
-      plane_pass(W + warp * N2, fr, lane);
+      plane_pass<true>(W + warp * N2, fS + (warp * 32 + lane) * FPITCH, lane);
       __syncthreads();
       // ---- C: the thread's two columns (the previous pair's TMEM stores are complete first)
       {
         const float2* gp = a.gphase + int64_t(p) * 96;
         const float2* gpp = a.gpar + (int64_t(p) * 2 + par) * 32;
-        const float* gs = a.gsinc + int64_t(p / a.ns) * (a.M + 1);
+        const float* gsr = a.gsx + int64_t(p / a.ns) * (513 * 20);
         const int4 uc = a.ucols[t];
         tm_wait_st();
-        par_stage_c<0>(W, uc.x, gp, gpp, gs, treg0);
-        par_stage_c<1>(W, uc.y, gp, gpp, gs, treg0 + 64);
+        par_stage_c<0>(W, uc.x, gp, gpp, gsr, treg0);
+        par_stage_c<1>(W, uc.y, gp, gpp, gsr, treg0 + 64);
       }
       __syncthreads();  // the next pair's stage A overwrites the planes
     }
@@ -227,7 +273,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
     // parked in the thread's own entries S[k][t] of the (now free) plane buffer.
     tm_wait_st();
     const int4 uc = a.ucols[t];
-    float2* out = a.hpart + it * 32 * HSLOTS;
+    float2* out = a.hpart + (int64_t(blockIdx.x) + cp) * 32 * HSLOTS;
     float2* S = W;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -266,7 +312,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       }
     }
     if (uc.w) self_conj(1);
-    __syncthreads();  // the parked slots are read before the next item's stage A
+    __syncthreads();  // the parked slots are read before the next segment's stage A
   }
   // every thread's TMEM traffic is complete before the columns are released
   tm_wait_st();
@@ -278,10 +324,10 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
   }
 }
 
-// G[cell][a][j] = sum over pair ranges and parities of the Hermitian slots,
-// expanded to all k (conjugate-mirrored for the negated partner columns)
+// G[cell][a][j] = sum over the segments of both parities of the Hermitian
+// slots, expanded to all k (conjugate-mirrored for the negated partner columns)
 __global__ void __launch_bounds__(256) k_herm_expand_par(float2* G, const float2* hpart, const int2* colslot,
-                                                          int64_t cells, int parts) {
+                                                          int64_t cells, int Q, int ctas) {
   using namespace gc;
   const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (gid >= cells * N3) return;
@@ -290,13 +336,18 @@ __global__ void __launch_bounds__(256) k_herm_expand_par(float2* G, const float2
   const int a = e >> 10, j = e & 1023;
   const int2 cs = colslot[j];  // (slot, kind): 0 representative, 1 negated partner, 2 self-conjugate
   const int aa = cs.y == 1 ? ((32 - a) & 31) : a;
+  const int64_t W = cells * 2 * Q;
   float2 s = make_float2(0.f, 0.f);
-  const int64_t n_it = int64_t(parts) * 2;
-  const float2* h = hpart + (cell * n_it * 32 + aa) * HSLOTS + cs.x;
-  for (int64_t i = 0; i < n_it; ++i) {
-    const float2 v = h[i * 32 * HSLOTS];
-    s.x += v.x;
-    s.y += v.y;
+  for (int par = 0; par < 2; ++par) {
+    const int64_t cp = 2 * cell + par, lo = cp * Q, hi = lo + Q;
+    for (int64_t b = lo * ctas / W; b < ctas; ++b) {
+      const int64_t wb0 = W * b / ctas, wb1 = W * (b + 1) / ctas;
+      if (wb0 >= hi) break;
+      if (wb1 <= lo) continue;  // this CTA's range ends where the segment starts
+      const float2 v = hpart[((b + cp) * 32 + aa) * HSLOTS + cs.x];
+      s.x += v.x;
+      s.y += v.y;
+    }
   }
   if (cs.y == 1) s.y = -s.y;
   G[gid] = s;
@@ -307,7 +358,7 @@ __global__ void __launch_bounds__(256) k_herm_expand_par(float2* G, const float2
 // ---------------------------------------------------------------------------
 int gain_parity_prepare(pii_plan* p) {
   using namespace gpar;
-  if (!p->tab.epar || !p->tab.gpar || !p->gc_maps) {
+  if (!p->tab.epar || !p->tab.gpar || !p->tab.gsx || !p->gc_maps) {
     set_error("gain_parity_prepare: parity tables or column map missing");
     return PII_ERR_ARG;
   }
@@ -321,10 +372,8 @@ int gain_parity_prepare(pii_plan* p) {
     return PII_ERR_CUDA;
   }
   p->gp_ctas = sms;
-  // Hermitian slots per work item: at most (8 * CTAs + 2 batch_max) items and
-  // never more than 2 batch_max x Q / 8
-  const int64_t max_items =
-      std::min<int64_t>(int64_t(8) * sms + 2 * p->batch_max, 2 * p->batch_max * std::max(1, p->Q / 8));
+  // Hermitian slot sets: one per (CTA, cell-parity) segment, at most CTAs + 2 batch_max
+  const int64_t max_items = int64_t(sms) + 2 * p->batch_max;
   const size_t bytes = size_t(max_items) * 32 * HSLOTS * sizeof(float2);
   PII_CUDA(cudaMalloc(&p->gp_hpart, bytes));
   p->bytes += int64_t(bytes);
@@ -334,13 +383,9 @@ int gain_parity_prepare(pii_plan* p) {
 
 int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   using namespace gpar;
-  const int nct = p->gp_ctas;
-  // pair ranges per cell: about `items per CTA` work items per resident CTA
-  int parts = int(std::max<int64_t>(1, (int64_t(p->gc_items_per_cluster) * nct + 2 * cells - 1) / (2 * cells)));
-  parts = std::min(parts, std::max(1, p->Q / 8));
-  while (2 * cells * parts > p->gp_max_items && parts > 1) --parts;
-  parts = (p->Q + (p->Q + parts - 1) / parts - 1) / ((p->Q + parts - 1) / parts);  // no empty ranges
-  if (2 * cells * parts > p->gp_max_items) {
+  // one CTA per SM, each with an equal share of the (cell, parity, pair) work
+  const int nct = int(std::min<int64_t>(p->gp_ctas, cells * 2 * p->Q));
+  if (nct + 2 * cells > p->gp_max_items) {
     set_error("gain_parity_run: %lld cells beyond the plan's capacity", (long long)cells);
     return PII_ERR_SIZE;
   }
@@ -351,26 +396,23 @@ int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.gphase = static_cast<const float2*>(p->tab.gphase);
   a.epar = static_cast<const float2*>(p->tab.epar);
   a.gpar = static_cast<const float2*>(p->tab.gpar);
-  a.gsinc = static_cast<const float*>(p->tab.gsinc);
-  a.M = p->tab.M;
+  a.gsx = static_cast<const float*>(p->tab.gsx);
   a.ns = p->ns;
   a.Q = p->Q;
   a.cells = cells;
-  a.parts = parts;
   a.hpart = static_cast<float2*>(p->gp_hpart);
   a.ucols = static_cast<const int4*>(p->gc_maps);
-  const int64_t items = 2 * cells * parts;
-  const unsigned grid = unsigned(std::min<int64_t>(items, nct));
   {
     StageTimer st(p, ST_GAIN_CLUSTER, s);
-    k_gain_parity<<<grid, THREADS, SMEM, s>>>(a);
+    k_gain_parity<<<unsigned(nct), THREADS, SMEM, s>>>(a);
   }
   PII_CHECK_LAUNCH();
   {
     StageTimer st(p, ST_REDUCE, s);
     k_herm_expand_par<<<unsigned((cells * N3 + 255) / 256), 256, 0, s>>>(
         static_cast<float2*>(p->G), a.hpart,
-        reinterpret_cast<const int2*>(static_cast<const char*>(p->gc_maps) + THREADS * sizeof(int4)), cells, parts);
+        reinterpret_cast<const int2*>(static_cast<const char*>(p->gc_maps) + THREADS * sizeof(int4)), cells, p->Q,
+        nct);
   }
   PII_CHECK_LAUNCH();
   return PII_OK;

@@ -61,11 +61,14 @@ enum Stage {
 // (W = exp(-2 pi i / 32), e_a / g_a the d = 0 rows above):
 //   epar [Q][2][32] complex  : W^{-p k} e_a[k] (k < 16), (-1)^p W^{-p k} e_a[k + 16]
 //   gpar [Q][2][32] complex  : W^{p k} g_a[k]
+//   gsx  [n_r][513][20] real : gsinc[r][m_bc + q^2] for q = |k_a| <= 16 (0-padded),
+//                              m_bc = k_b^2 + k_c^2: one 80-byte row per column
 struct Tables {
   void* ephase = nullptr;
   void* gphase = nullptr;
   void* epar = nullptr;
   void* gpar = nullptr;
+  void* gsx = nullptr;
   void* gsinc = nullptr;
   void* lossk = nullptr;
   void* lapl = nullptr;

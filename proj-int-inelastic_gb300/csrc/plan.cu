@@ -147,6 +147,13 @@ static int upload_tables(pii_plan* p) {
     };
     PII_TRY(up2(&p->tab.epar, ep2));
     PII_TRY(up2(&p->tab.gpar, gp2));
+    // per-column rows of the radial sinc table: gsinc[r][m_bc + q^2], q = |k_a| <= 16
+    std::vector<T> gsx(size_t(nr) * 513 * 20, T(0));
+    for (int ir = 0; ir < nr; ++ir)
+      for (int mbc = 0; mbc <= 512; ++mbc)
+        for (int q = 0; q <= 16 && mbc + q * q <= M; ++q)
+          gsx[(size_t(ir) * 513 + mbc) * 20 + q] = gs[size_t(ir) * (M + 1) + mbc + q * q];
+    PII_TRY(up2(&p->tab.gsx, gsx));
   }
   for (int m = 0; m <= M; ++m) {
     lk[m] = T(lk_d[m]);
@@ -180,7 +187,7 @@ static void free_plan(pii_plan* p) {
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
   }
-  void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
+  void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
                   p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->mom,       p->flag};
   for (void* q : ptrs)
