@@ -98,40 +98,55 @@ struct GainParityArgs {
   const int4* ucols;  // [THREADS] (column, column, first slot, 1 if two self-conjugate columns)
 };
 
-// stage A for the adjacent columns j0 = 2 t, j0 + 1 of one row: parity-PAR
-// outputs of the inverse transform along a.  Both columns come in one 16-byte
-// load per k_a and leave as one 16-byte store per plane (with the row swizzle
-// (c ^ b) the two columns stay neighbours).
+// stage A, parity-PAR outputs of the inverse transform along a, for the
+// thread's column pair (j, -j).  f is real, so f^(k, -j) = conj f^(-k, j): the
+// 32 values of column j give both columns (half the bytes of reading both):
+//   u_j[k]  = e_bc(j)  (F[k] eA[k] + F[k + 16] eB[k])
+//   u_-j[k] = e_bc(-j) (conj F[-k] eA[k] + conj F[-k - 16] eB[k])   (indices mod 32)
+// so the loaded pair (F[k], F[k + 16]) also serves u_-j[(16 - k) mod 16].
 template <int PAR>
-__device__ __forceinline__ void par_stage_a(float2* W, const float2* fh, const float2* ep, const float2* epp, int j0) {
+__device__ __forceinline__ void par_stage_a_pair(float2* W, const float2* fh, const float2* ep, const float2* epp,
+                                                 int j) {
   using namespace gc;
-  const int jb = j0 >> 5, jc = j0 & 31;
-  const float2 eb = ep[32 + jb];
-  const float4 ec = *reinterpret_cast<const float4*>(ep + 64 + jc);
-  const float2 ebc0 = cmul(eb, make_float2(ec.x, ec.y)), ebc1 = cmul(eb, make_float2(ec.z, ec.w));
-  const float4* f4 = reinterpret_cast<const float4*>(fh + j0);
-  const float4* e4 = reinterpret_cast<const float4*>(epp);
+  const int jb = j >> 5, jc = j & 31;
+  const int nb = (32 - jb) & 31, nc = (32 - jc) & 31;
+  const float2 ebc0 = cmul(ep[32 + jb], ep[64 + jc]), ebc1 = cmul(ep[32 + nb], ep[64 + nc]);
   float2 u0[16], u1[16];
-#pragma unroll
-  for (int k = 0; k < 16; k += 2) {
-    const float4 ea = e4[k >> 1], eb2 = e4[8 + (k >> 1)];
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      const float4 lo = f4[(k + d) * (N2 / 2)], hi = f4[(k + d + 16) * (N2 / 2)];
-      const float2 wa = d ? make_float2(ea.z, ea.w) : make_float2(ea.x, ea.y);
-      const float2 wb = d ? make_float2(eb2.z, eb2.w) : make_float2(eb2.x, eb2.y);
-      u0[k + d] = cmul(cfma(make_float2(hi.x, hi.y), wb, cmul(make_float2(lo.x, lo.y), wa)), ebc0);
-      u1[k + d] = cmul(cfma(make_float2(hi.z, hi.w), wb, cmul(make_float2(lo.z, lo.w), wa)), ebc1);
-    }
-  }
+  static_for<0, 16>([&](auto ki) {
+    constexpr int k = decltype(ki)::value;
+    constexpr int k1 = (16 - k) & 15;
+    const float2 lo = fh[k * N2 + j], hi = fh[(k + 16) * N2 + j];
+    u0[k] = cmul(cfma(hi, epp[16 + k], cmul(lo, epp[k])), ebc0);
+    const float2 clo = make_float2(lo.x, -lo.y), chi = make_float2(hi.x, -hi.y);
+    if constexpr (k == 0)
+      u1[0] = cmul(cfma(chi, epp[16], cmul(clo, epp[0])), ebc1);
+    else
+      u1[k1] = cmul(cfma(clo, epp[16 + k1], cmul(chi, epp[k1])), ebc1);
+  });
   fft_line<16, +1>(u0);
   fft_line<16, +1>(u1);
-  float4* W4 = reinterpret_cast<float4*>(W);
   static_for<0, 16>([&](auto mi) {
     constexpr int m = decltype(mi)::value;
-    const float2 v0 = u0[pos(16, m)], v1 = u1[pos(16, m)];
-    // columns jc, jc + 1 share the 16-byte slot widx >> 1, swapped when the row is odd
-    W4[widx(m, jb, jc) >> 1] = (jb & 1) ? make_float4(v1.x, v1.y, v0.x, v0.y) : make_float4(v0.x, v0.y, v1.x, v1.y);
+    W[widx(m, jb, jc)] = u0[pos(16, m)];
+    W[widx(m, nb, nc)] = u1[pos(16, m)];
+  });
+}
+
+// stage A for one column j from its own 32 values (the warp holding the
+// self-conjugate columns)
+template <int PAR>
+__device__ __forceinline__ void par_stage_a_col(float2* W, const float2* fh, const float2* ep, const float2* epp,
+                                                int j) {
+  using namespace gc;
+  const int jb = j >> 5, jc = j & 31;
+  const float2 ebc = cmul(ep[32 + jb], ep[64 + jc]);
+  float2 u[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) u[k] = cmul(cfma(fh[(k + 16) * N2 + j], epp[16 + k], cmul(fh[k * N2 + j], epp[k])), ebc);
+  fft_line<16, +1>(u);
+  static_for<0, 16>([&](auto mi) {
+    constexpr int m = decltype(mi)::value;
+    W[widx(m, jb, jc)] = u[pos(16, m)];
   });
 }
 
@@ -243,14 +258,25 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
     for (int p = p0; p < p1; ++p) {
       // (per-pair pointers are formed inside each stage so that none stays
       // live across the register-heavy plane pass)
-      // ---- A: columns 2 t and 2 t + 1
+      // ---- A: the thread's two columns (those it also takes in stage C)
       {
         const float2* ep = a.ephase + int64_t(p) * 96;
         const float2* epp = a.epar + (int64_t(p) * 2 + par) * 32;
-        if (par == 0)
-          par_stage_a<0>(W, fh, ep, epp, 2 * t);
-        else
-          par_stage_a<1>(W, fh, ep, epp, 2 * t);
+        const int4 uc = a.ucols[t];
+        if (warp < 15) {  // column pairs {j, -j}: rows 1..15 and 31..17
+          if (par == 0)
+            par_stage_a_pair<0>(W, fh, ep, epp, uc.x);
+          else
+            par_stage_a_pair<1>(W, fh, ep, epp, uc.x);
+        } else {  // rows 0 and 16 (with the self-conjugate columns): each column from its own values
+#pragma unroll 1
+          for (int h = 0; h < 2; ++h) {
+            if (par == 0)
+              par_stage_a_col<0>(W, fh, ep, epp, h ? uc.y : uc.x);
+            else
+              par_stage_a_col<1>(W, fh, ep, epp, h ? uc.y : uc.x);
+          }
+        }
       }
       __syncthreads();
       // ---- B: warp `warp` owns local plane `warp` (a = 2 warp + par)
