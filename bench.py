@@ -127,7 +127,7 @@ class ClockSampler:
 # the reference's broadcast evaluation (src/collision/inelastic_collisions.py:208-227)
 # ---------------------------------------------------------------------------
 class TorchFP64Operator:
-    def __init__(self, mesh, device):
+    def __init__(self, mesh, device, e=E, gamma=1.0):
         import numpy as np
         import torch
 
@@ -141,13 +141,13 @@ class TorchFP64Operator:
         sig = t(sigma)
         kdots = sig[:, 0, None, None, None] * kx + sig[:, 1, None, None, None] * ky + sig[:, 2, None, None, None] * kz
         rr = t(r)[:, None, None, None, None]
-        er = 0.5 * (E - E) * np.tanh(r - 0.5 * mesh.R) + 0.5 * (E + E)
+        er = 0.5 * (e - e) * np.tanh(r - 0.5 * mesh.R) + 0.5 * (e + e)
         a = t(0.25 * math.pi * (1 + er) / mesh.L)[:, None, None, None, None]
-        pre = 4 * math.pi * rr ** 3.0
+        pre = 4 * math.pi * rr ** (gamma + 2.0)
         sinc = lambda x: torch.where(x == 0, torch.ones_like(x), torch.sin(x) / torch.where(x == 0, torch.ones_like(x), x))
         self.gain = pre * torch.exp(1j * a * rr * kdots) * sinc(a * rr * knorm) * t(wr)[:, None, None, None, None] * wsig
         self.exp = torch.exp(-1j * math.pi * rr * kdots / mesh.L)
-        loss = 4 * math.pi * t(r) ** 3.0 * t(wr)
+        loss = 4 * math.pi * t(r) ** (gamma + 2.0) * t(wr)
         self.loss = loss[:, None, None, None]
         self.sp = sinc(math.pi * t(r)[:, None, None, None] * knorm / mesh.L)
 
@@ -178,6 +178,72 @@ def time_torch_fp64(mesh, f_dev, cells, device):
     e1.record()
     torch.cuda.synchronize()
     return cells / (e0.elapsed_time(e1) / 1e3)
+
+
+# ---------------------------------------------------------------------------
+# the 64^3 configuration: n = 64 on [-10, 10]^3, 48 GL radial nodes x the
+# 70-point symmetric design (no 64-point design exists), e = e0 = 0.7, hard
+# spheres, 3-Maxwellian mixtures (means in [-3, 3]^3, T in [0.5, 3])
+# ---------------------------------------------------------------------------
+N64, NR64, NS64, E64 = 64, 48, 70, 0.7
+S_L10 = 20.0 / (3.0 + math.sqrt(2.0))
+
+
+def mixture_states(v, cells, seed):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(cells):
+        f = sum(maxwellian(v, rng.uniform(0.5, 1.5), rng.uniform(-3, 3, 3), rng.uniform(0.5, 3.0)) for _ in range(3))
+        out.append(f / (f.sum() * (v[1] - v[0]) ** 3))
+    return np.stack(out)
+
+
+def measure_n64(pkg, device, cells=16, cells_fp64=2):
+    """Q(f,f) (gain - loss) at 64^3: mixed-precision throughput on `cells`
+    cells, the plain FP64 GPU method (torch.fft complex128) on `cells_fp64`,
+    and the relative L-inf error of the mixed path against it."""
+    import torch
+
+    cfg = {"velocity-mesh": {"nv": N64, "s": S_L10, "nr": NR64},
+           "spherical-design-rule": {"ssrule": "womersley", "nsphr": NS64},
+           "collision-model": {"dim": 3, "type": "vhs", "e": E64, "e0": E64, "gamma": 1.0}}
+    sm = pkg.SpectralMesh(cfg)
+    f = torch.as_tensor(mixture_states(sm.v_center, cells, 64), device=device).contiguous()
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=cells, device=device.index)
+    col.plan.autotune(cells)
+    q = col.collide(f, with_loss=True)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(2):
+        q = col.collide(f, with_loss=True)
+    b.record()
+    torch.cuda.synchronize()
+    mixed = 2 * cells / (a.elapsed_time(b) / 1e3)
+    out = {"config": f"n_v={N64}^3 on [-10,10]^3, {NR64} GL radial x {NS64}-point symmetric design, "
+                     f"hard spheres, e=e0={E64}, 3-Maxwellian mixtures", "cells": cells,
+           "mixed": mixed, "unit": UNIT, "tuning": col.plan.tuning}
+    try:
+        op = TorchFP64Operator(sm, device, e=E64, gamma=1.0)
+        fc = f[:cells_fp64].to(torch.complex128)
+        q64 = [op.collide(fc[0])]
+        torch.cuda.synchronize()
+        a.record()
+        q64 = [op.collide(fc[c]) for c in range(cells_fp64)]
+        b.record()
+        torch.cuda.synchronize()
+        out["fp64_torch"] = cells_fp64 / (a.elapsed_time(b) / 1e3)
+        out["speedup_vs_fp64_gpu"] = mixed / out["fp64_torch"]
+        errs = [float((q[c] - q64[c]).abs().max() / q64[c].abs().max()) for c in range(cells_fp64)]
+        out["rel_linf_err_vs_fp64"] = max(errs)
+        del op
+    except Exception as ex:  # noqa: BLE001
+        out["fp64_torch_error"] = str(ex)[:200]
+    col.close()
+    torch.cuda.empty_cache()
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -300,6 +366,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's default kernel choices")
+    ap.add_argument("--no-n64", action="store_true", help="skip the 64^3 configuration measurement")
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: run 3 Q(f,f) evaluations on this many cells of the workload and exit")
     args = ap.parse_args()
@@ -411,7 +478,8 @@ def main():
     # per (cell, pair) item; the fused kernel does the whole pair (survey's per-pair term 2*5N log2 N + 16 N)
     per_item = {"pair_plane": 4 * pass_flops + 2 * N, "col_pstart": pass_flops + 12 * N,
                 "col_pend": pass_flops + 14 * N, "reduce": 2 * N,
-                "gain_cluster": 2 * 5.0 * N * math.log2(N) + 16 * N}
+                "gain_cluster": 2 * 5.0 * N * math.log2(N) + 16 * N,
+                "gain_parity": 2 * 5.0 * N * math.log2(N) + 16 * N}
     collides = K_INNER
     if dom in per_item:
         flops_total = per_item[dom] * items_per_collide * collides
@@ -504,6 +572,8 @@ def main():
         line["mixed_collide_only"] = collide_rate
         if torch64:
             line["speedup_vs_fp64_gpu"] = collide_rate / torch64
+    if rank == 0 and not args.no_n64:
+        line["n64"] = measure_n64(pkg, device)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if rank == 0:

@@ -214,9 +214,9 @@ int pii_collide_noalloc(const double* f, double* q, int64_t cells, int n, int n_
  * pii_plan_profile_read fills ms[PII_NSTAGES] (summed device time) and
  * launches[PII_NSTAGES] after synchronising, and resets the counters.
  */
-#define PII_NSTAGES 12
+#define PII_NSTAGES 13
 /* stage order: fwd_plane, col_fwd, col_pstart, pair_plane, col_pend, reduce,
- * col_iprep, finish, df, axpy, massfix, gain_cluster */
+ * col_iprep, finish, df, axpy, massfix, gain_cluster, gain_parity */
 int64_t pii_kernel_launches(void);
 int pii_plan_profile(pii_plan* plan, int enable);
 int pii_plan_profile_read(pii_plan* plan, double* ms, int64_t* launches);

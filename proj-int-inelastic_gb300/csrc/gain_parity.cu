@@ -429,7 +429,7 @@ int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.hpart = static_cast<float2*>(p->gp_hpart);
   a.ucols = static_cast<const int4*>(p->gc_maps);
   {
-    StageTimer st(p, ST_GAIN_CLUSTER, s);
+    StageTimer st(p, ST_GAIN_PARITY, s);
     k_gain_parity<<<unsigned(nct), THREADS, SMEM, s>>>(a);
   }
   PII_CHECK_LAUNCH();

@@ -20,7 +20,7 @@ extern std::atomic<int64_t> g_launches;
 
 enum Stage {
   ST_FWD_PLANE = 0, ST_COL_FWD, ST_COL_PSTART, ST_PAIR_PLANE, ST_COL_PEND, ST_REDUCE,
-  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_COUNT
+  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_GAIN_PARITY, ST_COUNT
 };
 
 #define PII_CUDA(call)                                                                    \

@@ -17,6 +17,8 @@
 
 namespace pii {
 
+static_assert(ST_COUNT == PII_NSTAGES, "profiling stages out of step with the C ABI");
+
 static thread_local char g_err[1024] = "";
 std::atomic<int64_t> g_launches{0};
 
