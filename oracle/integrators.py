@@ -90,6 +90,53 @@ def convex_splitting_maxwellian_step(f, dt, collision, kn, penalty, e, tau, v, d
         f += advection(f, dt)
 
 
+def maxwellian_2d(vx, vy, rho, u, T):
+    """``maxwellian`` of the reference solver (``src/boltzmann.py:9-13``): 2D
+    velocity, bulk velocity (u, 0); rho, u, T per cell."""
+    rho = np.asarray(rho)[:, None, None]
+    u = np.asarray(u)[:, None, None]
+    T = np.asarray(T)[:, None, None]
+    return rho / (2 * np.pi * T) * np.exp(-((vx - u) ** 2 + vy**2) / (2 * T))
+
+
+def convex_splitting_maxwellian_step_2d(f, dt, collision, kn, penalty, e, tau, v, delta, advection=None):
+    """CONSP_M exactly as the reference writes it for 2D velocity
+    (``src/boltzmann.py:96-118``), with the 2D moments of ``State``
+    (``src/state.py:31-52,91-92``)."""
+    mo = moments(f, v, delta, dim=2)
+    rho, u, T = mo["rho"], mo["u"][..., 0], mo["T"]
+    vx, vy = np.meshgrid(v, v, indexing="ij")
+    T_new = (T - 8 * tau / (1 - e**2)) * np.exp(-(1 - e**2) / kn / 4 * rho * dt) + 8 * tau / (1 - e**2)
+    dm = maxwellian_2d(vx, vy, rho, u, T_new) - maxwellian_2d(vx, vy, rho, u, T)
+    f += dt / (kn + penalty * dt) * collision(f) + penalty * dt / (kn + penalty * dt) * dm
+    if advection is not None:
+        f += advection(f, dt)
+
+
+def fast_sweep_step(f, v1, dx, kn, collision, delta, dim):
+    """One ``BoltzmannFastSweep.step`` (``src/iter_solver.py:38-62``): the
+    collision term and the density of the current state, then a Gauss-Seidel
+    upwind sweep in x for v1 > 0 (left to right) and v1 < 0 (right to left) over
+    the interior cells; returns max |f_new - f_old|.  The reference writes it
+    for 2D velocity; with ``dim = 3`` the same sweep runs over the other two
+    velocity axes."""
+    f_old = f.copy()
+    nx = f.shape[0]
+    v = np.asarray(v1, np.float64)
+    vdx = v / dx
+    nu = 1 / np.sqrt(np.pi / 2) / kn
+    rho = moments(f, v, delta, dim=dim)["rho"]
+    rho = rho.reshape((nx,) + (1,) * dim)
+    gain = collision(f)
+    pos, neg = v > 0, v < 0
+    ext = (slice(None),) + (None,) * (dim - 1)
+    for i in range(1, nx - 1):
+        f[i, pos] = (nu * gain[i, pos] + vdx[pos][ext] * f[i - 1, pos]) / (nu * rho[i] + vdx[pos][ext])
+    for j in range(1, nx - 1):
+        f[-j - 1, neg] = (nu * gain[-j - 1, neg] - vdx[neg][ext] * f[-j, neg]) / (nu * rho[-j - 1] - vdx[neg][ext])
+    return np.max(np.abs(f - f_old))
+
+
 STEPS = {
     "Euler": lambda f, dt, df, K, h: euler_step(f, dt, df),
     "PFE": proj_euler_step,
@@ -109,20 +156,22 @@ def evolve(f, t0, tend, dt, df, integrator="Euler", inner_steps=(3, 3, 3), inner
     return f
 
 
-def moments(f, v, delta):
-    """FP64 density, bulk velocity (3), energy density and temperature per cell.
+def moments(f, v, delta, dim=3):
+    """FP64 density, bulk velocity, energy density and temperature per cell.
 
-    The reference's ``State.rho/u/T`` reduce over two velocity axes only
-    (``src/state.py:31-52,91-92``); this is the 3D-velocity form:
-    ``rho = sum f dv``, ``u = sum f v dv / rho``, ``E = 1/2 sum f |v|^2 dv`` and
+    ``dim = 2`` is the reference's ``State.rho/u/T`` (``src/state.py:31-52,91-92``):
+    sums over the two velocity axes times delta^2, ``T = E / rho - |u|^2 / 2``.
+    ``dim = 3`` is the 3D-velocity form: ``rho = sum f dv``,
+    ``u = sum f v dv / rho``, ``E = 1/2 sum f |v|^2 dv`` and
     ``T = (2/3) (E / rho - |u|^2 / 2)``.
     """
     f = np.asarray(f, np.float64)
-    V = np.meshgrid(v, v, v, indexing="ij")
-    dv = delta**3
-    rho = f.sum(axis=(-3, -2, -1)) * dv
-    mom = np.stack([(f * V[d]).sum(axis=(-3, -2, -1)) * dv for d in range(3)], axis=-1)
-    E = 0.5 * (f * (V[0] ** 2 + V[1] ** 2 + V[2] ** 2)).sum(axis=(-3, -2, -1)) * dv
+    V = np.meshgrid(*([v] * dim), indexing="ij")
+    ax = tuple(range(-dim, 0))
+    dv = delta**dim
+    rho = f.sum(axis=ax) * dv
+    mom = np.stack([(f * V[d]).sum(axis=ax) * dv for d in range(dim)], axis=-1)
+    E = 0.5 * (f * sum(V[d] ** 2 for d in range(dim))).sum(axis=ax) * dv
     u = mom / rho[..., None]
-    T = (2.0 / 3.0) * (E / rho - 0.5 * (u**2).sum(-1))
+    T = (2.0 / dim) * (E / rho - 0.5 * (u**2).sum(-1))
     return {"rho": rho, "u": u, "E": E, "T": T}

@@ -8,9 +8,10 @@ correction and two ghost cells, as in
 * ``advection_1D`` (``src/riemann/advection_1D.py:4-21``),
 * ``tvd.limit`` / ``tvd.minmod`` (``src/limiters/tvd.py:6-40``).
 
-The state is ``f`` with shape ``(n_x, n, n, n)``; the advection speed is the
-first velocity coordinate ``v1`` (``src/solution.py:55``), broadcast over the
-other two velocity axes.
+The state is ``f`` with shape ``(n_x, n, n, n)`` (3D velocity) or
+``(n_x, n, n)`` (2D velocity); the advection speed is the first velocity
+coordinate ``v1`` (``src/solution.py:55``), broadcast over the other velocity
+axes.
 
 The reference slices the speed array as ``s[LL-1:UL-1]`` on its *velocity*
 axis (``src/boltzmann.py:200``); that slice is the whole array whenever
@@ -80,7 +81,8 @@ def df_advection(f, v1, dt, dx, bc_lower=EXTRAP, bc_upper=EXTRAP, order=2):
     """
     f = np.asarray(f, np.float64)
     n = f.shape[1]
-    s = np.broadcast_to(np.asarray(v1, np.float64)[:, None, None], (n,) + f.shape[2:]).copy()
+    vv = np.asarray(v1, np.float64).reshape((n,) + (1,) * (f.ndim - 2))
+    s = np.broadcast_to(vv, (n,) + f.shape[2:]).copy()
     fb = ghosted(f, bc_lower, bc_upper)
     dtdx = dt / dx
     df = np.zeros(fb.shape)

@@ -15,8 +15,17 @@ vectors, so parity is pinned by executing its own code under the shims in
   (extrapolation and periodic ghost cells);
 * ``solver1d.npz``   -- short PFE / TPI2 / TPI3 runs of ``BoltzmannSolver1D``
   (reference default collision call = gain only, plus a gain - loss run).
+* ``op2d.npz``       -- the 2D-velocity operator (``J_0`` kernel, circle
+  quadrature) at n = 8 / 16 / 32: gain, gain - loss, heat bath;
+* ``solver2d.npz``   -- ``BoltzmannSolver1D`` on 2D velocity (its native
+  setting): PFE, Euler and CONSP_M runs (the convex splitting with the
+  Maxwellian penalty exists only in 2D in the reference);
+* ``sweep2d.npz``    -- ``BoltzmannFastSweep`` iterations (state after each
+  step and the returned errors).
 
-Run from the repository root:  ``python tests/golden/make_golden.py``.
+Run from the repository root:  ``python tests/golden/make_golden.py [stem ...]``
+(all fixtures, or only the named ones; the full set reproduces the committed
+files, the transport fixture drawing from the same generator after op_small).
 Needs the reference checkout (``PII_REFERENCE_ROOT``, default
 /root/reference); the GPU machine never runs this script.
 """
@@ -204,16 +213,158 @@ def make_solver1d(ref):
     np.savez_compressed(os.path.join(HERE, "solver1d.npz"), **out)
 
 
-def main():
+def op_config_2d(nv, s, nr, nphi, e, e0, gamma):
+    return {
+        "velocity-mesh": {"nv": nv, "s": s, "nr": nr},
+        "circle-quad-rule": {"nphi": nphi},
+        "collision-model": {"dim": 2, "type": "vhs", "e": e, "e0": e0, "gamma": gamma},
+    }
+
+
+def maxwellian_2d(v, rho, u, T):
+    V = np.meshgrid(v, v, indexing="ij")
+    return rho / (2 * math.pi * T) * np.exp(-((V[0] - u[0]) ** 2 + (V[1] - u[1]) ** 2) / (2 * T))
+
+
+OP2D_CASES = [
+    # nv, nr, nphi, e, e0, gamma, cells
+    (8, 4, 8, 0.9, 0.9, 0.0, 3),
+    (16, 8, 16, 0.5, 1.0, 1.0, 2),
+    (16, 5, 12, 0.7, 0.7, 0.0, 2),
+    (32, 16, 16, 0.8, 0.8, 1.0, 2),
+]
+
+
+def make_op2d(ref, rng):
+    out = {}
+    for i, (nv, nr, nphi, e, e0, g, cells) in enumerate(OP2D_CASES):
+        cfg = op_config_2d(nv, L8_S, nr, nphi, e, e0, g)
+        sm = ref.spectral_mesh.SpectralMesh(cfg)
+        col = ref.inelastic.FSInelasticVHSCollision(cfg, sm)
+        if i == 3:
+            v = sm.v_center
+            f = np.stack([maxwellian_2d(v, 1.0 + 0.1 * c, (0.5 * c, -0.3), 1.0 + 0.2 * c)
+                          + 0.5 * maxwellian_2d(v, 1.0, (-1.5, 1.0), 0.7) for c in range(cells)])
+        else:
+            f = rng.random((cells, nv, nv)) + 0.1
+        out[f"case{i}_params"] = np.array([nv, nr, nphi, e, e0, g, L8_S])
+        out[f"case{i}_f"] = f
+        out[f"case{i}_gain"] = col(f)
+        out[f"case{i}_full"] = col.collide(f, with_loss=True)
+        out[f"case{i}_heat"] = col(f, heat_bath=0.3)
+    np.savez_compressed(os.path.join(HERE, "op2d.npz"), **out)
+
+
+def _solution_2d(ref, nx, nv, L, xmin=0.0, xmax=1.0):
+    Solution = __import__("src.solution", fromlist=["Solution"]).Solution
+    cfg = types.SimpleNamespace(dim_x=1, dim_v=2, xmin=xmin, xmax=xmax, l=L, nx=nx, nv=nv)
+    return Solution(cfg)
+
+
+def sod_f0_2d(v, nx):
+    x = (np.arange(nx) + 0.5) / nx
+    left = maxwellian_2d(v, 1.0, (0.0, 0.0), 1.0)
+    right = maxwellian_2d(v, 0.125, (0.0, 0.0), 0.8)
+    return np.stack([left if xi < 0.5 else right for xi in x])
+
+
+def periodic_f0_2d(v, nx):
+    x = (np.arange(nx) + 0.5) / nx
+    return np.stack([maxwellian_2d(v, 1 + 0.2 * math.sin(2 * math.pi * xi), (0.3 * math.cos(2 * math.pi * xi), 0.0),
+                                   1 + 0.1 * math.cos(2 * math.pi * xi)) for xi in x])
+
+
+def make_solver2d(ref):
+    out = {}
+    # n_x + 2 >= n_v: the reference's transport slices its speed array on the
+    # velocity axis (src/boltzmann.py:200) and fails to broadcast otherwise
+    nv, nr, nphi, nx = 16, 8, 16, 16
+    kn, e, tau, penalty = 1e-2, 0.8, 0.05, 5.0
+    cfg = op_config_2d(nv, L8_S, nr, nphi, e, e, 0.0)
+    sm = ref.spectral_mesh.SpectralMesh(cfg)
+    col = ref.inelastic.FSInelasticVHSCollision(cfg, sm)
+    runs = [
+        # name, integrator, bc, f0, inner_steps, inner_dt, dt, tend, collision
+        ("pfe", "PFE", ref.solver.BC.extrap, "sod", [2], [5e-4], 2e-3, 4e-3, "full"),
+        ("euler", "Euler", ref.solver.BC.periodic, "per", [3], [1e-3], 5e-4, 1.5e-3, "gain"),
+        ("consp_m", "CONSP_M", ref.solver.BC.periodic, "per", [3], [1e-3], 1e-3, 3e-3, "full"),
+    ]
+    for name, integ, bc, init, K, h, dt, tend, which in runs:
+        sol = _solution_2d(ref, nx, nv, sm.L)
+        v = sol.state.grid.dimensions[1].centers
+        f0 = sod_f0_2d(v, nx) if init == "sod" else periodic_f0_2d(v, nx)
+        sol.state.f[:] = f0
+        if which == "gain":
+            operator = col
+        else:
+            def operator(f, _c=col):
+                _c(f)
+                return _c.collide(f, with_loss=True)
+        solver = ref.boltzmann.BoltzmannSolver1D(kn, riemann_solver=ref.advection_1D.advection_1D,
+                                                 collision_operator=operator)
+        solver.all_bcs = bc
+        solver.time_integrator = integ
+        solver.inner_steps = list(K)
+        solver.inner_dt = list(h)
+        solver.dt = dt
+        solver.penalty = penalty
+        solver.e = e
+        solver.tau = tau
+        solver.evolve_to_time(sol, tend)
+        out[f"{name}_f0"] = f0
+        out[f"{name}_f"] = sol.state.f.copy()
+        out[f"{name}_meta"] = np.array([dt, tend, kn, sol.state.grid.delta[0]])
+        out[f"{name}_K"] = np.array(K)
+        out[f"{name}_h"] = np.array(h)
+    out["params"] = np.array([nv, nr, nphi, e, e, 0.0, L8_S, nx])
+    out["consp_m_coeffs"] = np.array([penalty, e, tau])
+    np.savez_compressed(os.path.join(HERE, "solver2d.npz"), **out)
+
+
+def make_sweep2d(ref):
+    import tempfile
+
+    nv, nr, nphi, nx = 16, 8, 16, 10
+    kn = 0.5
+    cfg = op_config_2d(nv, L8_S, nr, nphi, 0.9, 0.9, 0.0)
+    sm = ref.spectral_mesh.SpectralMesh(cfg)
+    col = ref.inelastic.FSInelasticVHSCollision(cfg, sm)
+    sol = _solution_2d(ref, nx, nv, sm.L)
+    v = sol.state.grid.dimensions[1].centers
+    f0 = periodic_f0_2d(v, nx)
+    sol.state.f[:] = f0
+    log = os.path.join(tempfile.mkdtemp(), "sweep.log")
+    sweep = ref.iter_solver.BoltzmannFastSweep(log, collision=col, kn=kn, tol=1e-12)
+    fs, errs = [], []
+    for _ in range(3):
+        errs.append(sweep.step(sol.state))
+        fs.append(sol.state.f.copy())
+    np.savez_compressed(os.path.join(HERE, "sweep2d.npz"), params=np.array([nv, nr, nphi, 0.9, 0.9, 0.0, L8_S, nx]),
+                        kn=kn, dx=sol.state.grid.delta[0], v=v, f0=f0, f=np.stack(fs), err=np.array(errs))
+
+
+def main(which=None):
+    """Write every fixture, or only those named in ``which`` (file stems)."""
     ref = load_reference()
+    want = set(which or ["op_small", "op_c32", "euler_c32", "transport", "solver1d", "op2d", "solver2d", "sweep2d"])
     rng = np.random.default_rng(20261203)
-    make_op_small(ref, rng)
-    cfg, sm, col, f = make_op_c32(ref)
-    make_euler_c32(ref, cfg, sm, col, f)
-    make_transport(ref, rng)
-    make_solver1d(ref)
+    if "op_small" in want:
+        make_op_small(ref, rng)
+    if want & {"op_c32", "euler_c32"}:
+        cfg, sm, col, f = make_op_c32(ref)
+        make_euler_c32(ref, cfg, sm, col, f)
+    if "transport" in want:
+        make_transport(ref, np.random.default_rng(1) if "op_small" not in want else rng)
+    if "solver1d" in want:
+        make_solver1d(ref)
+    if "op2d" in want:
+        make_op2d(ref, np.random.default_rng(20261204))
+    if "solver2d" in want:
+        make_solver2d(ref)
+    if "sweep2d" in want:
+        make_sweep2d(ref)
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -17,6 +17,9 @@ reference tree itself is never modified):
   ``src/collision/spherical_design/__init__.py:39-40``.
 * ``tqdm.tnrange = range`` -- the notebook progress bar breaks under current
   tqdm (``src/solver.py:131``, ``src/boltzmann.py:124-149``).
+* ``matplotlib`` -- an empty stub; ``src/utility.py:5`` imports pyplot for
+  plotting helpers that the iterative solver (``src/iter_solver.py:6``) does
+  not call.
 """
 import os
 import sys
@@ -68,6 +71,15 @@ def _install_shims(workers=None):
 
     tqdm.tnrange = lambda n, *a, **k: range(n)
 
+    try:
+        import matplotlib  # noqa: F401
+    except ImportError:
+        mpl = types.ModuleType("matplotlib")
+        plt = types.ModuleType("matplotlib.pyplot")
+        mpl.pyplot = plt
+        sys.modules["matplotlib"] = mpl
+        sys.modules["matplotlib.pyplot"] = plt
+
 
 def load_reference(workers=None):
     """Return a namespace with the reference modules used by the fixtures."""
@@ -86,4 +98,5 @@ def load_reference(workers=None):
     ns.solver = importlib.import_module("src.solver")
     ns.advection_1D = importlib.import_module("src.riemann.advection_1D")
     ns.tvd = importlib.import_module("src.limiters.tvd")
+    ns.iter_solver = importlib.import_module("src.iter_solver")
     return ns

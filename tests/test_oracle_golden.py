@@ -118,3 +118,55 @@ def test_mass_mode_correction():
     qc = fo.mass_mode_correction(q)
     assert np.abs(qc.sum(axis=(1, 2, 3))).max() < 1e-12
     assert rel_linf(qc - q, -q.mean(axis=(1, 2, 3), keepdims=True) + 0 * q) < 1e-14
+
+
+# ---------------------------------------------------------------------------
+# 2D velocity (J_0 kernel, circle quadrature): the reference's native setting
+# ---------------------------------------------------------------------------
+def _op2d(params):
+    nv, nr, nphi, e, e0, g, s = params
+    m = fo.Mesh(int(nv), s, int(nr), dim=2, nphi=int(nphi))
+    return m, fo.FSInelasticVHS(m, e, e0, g)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_operator_2d(golden, case):
+    d = golden("op2d.npz")
+    m, op = _op2d(d[f"case{case}_params"])
+    f = d[f"case{case}_f"]
+    assert rel_linf(op.collide(f), d[f"case{case}_gain"]) < TOL
+    assert rel_linf(op.collide(f, with_loss=True), d[f"case{case}_full"]) < TOL
+    assert rel_linf(op(f, heat_bath=0.3), d[f"case{case}_heat"]) < TOL
+
+
+@pytest.mark.parametrize("name", ["pfe", "euler", "consp_m"])
+def test_solver2d(golden, name):
+    d = golden("solver2d.npz")
+    nv, nr, nphi, e, e0, g, s, nx = d["params"]
+    m, op = _op2d((nv, nr, nphi, e, e0, g, s))
+    dt, tend, kn, dx = d[f"{name}_meta"]
+    bc = "extrap" if name == "pfe" else "periodic"
+    with_loss = name != "euler"
+    coll = lambda x: op.collide(x, with_loss=with_loss)
+    adv = lambda x, hh: tr.df_advection(x, m.v, hh, dx, bc, bc)
+    f = d[f"{name}_f0"].copy()
+    if name == "consp_m":
+        penalty, e_s, tau = d["consp_m_coeffs"]
+        for _ in range(int(round(tend / dt))):
+            it.convex_splitting_maxwellian_step_2d(f, dt, coll, kn, penalty, e_s, tau, m.v, m.delta, adv)
+    else:
+        integ = {"pfe": "PFE", "euler": "Euler"}[name]
+        it.evolve(f, 0.0, tend, dt, lambda x, h: it.boltzmann_df(x, h, coll, kn, adv), integ,
+                  list(d[f"{name}_K"]), list(d[f"{name}_h"]))
+    assert rel_linf(f, d[f"{name}_f"]) < 1e-11
+
+
+def test_fast_sweep_2d(golden):
+    d = golden("sweep2d.npz")
+    nv, nr, nphi, e, e0, g, s, nx = d["params"]
+    m, op = _op2d((nv, nr, nphi, e, e0, g, s))
+    f = d["f0"].copy()
+    for k in range(3):
+        err = it.fast_sweep_step(f, d["v"], float(d["dx"]), float(d["kn"]), op, m.delta, dim=2)
+        assert rel_linf(f, d["f"][k]) < 1e-12, k
+        assert abs(err - d["err"][k]) <= 1e-12 * abs(d["err"][k]), k
