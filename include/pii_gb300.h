@@ -74,6 +74,20 @@ int pii_plan_create(pii_plan** out, int n, int n_r, int n_sigma, const double* r
                     const double* sigma, double w_sigma, double L, double R, double e, double e0,
                     double gamma, int precision, int64_t batch_max, int device);
 
+/*
+ * The same for velocity dimension dim = 2 or 3 (config["collision-model"]["dim"],
+ * src/collision/spectral_mesh.py:17-23, inelastic_collisions.py:42-52).  In 2D
+ * the grid is n^2 per cell, sigma holds n_sigma x 2 circle directions
+ * (cos phi, sin phi) with weight w_sigma = 2 pi / n_phi
+ * (src/collision/spectral_mesh.py:51-56,94-97), the radial kernel is J_0 and
+ * the circle constant 2 pi.  pii_plan_create is the dim = 3 case;
+ * pii_plan_dim returns a plan's dimension (-1 for NULL).
+ */
+int pii_plan_create_nd(pii_plan** out, int dim, int n, int n_r, int n_sigma, const double* r, const double* w_r,
+                       const double* sigma, double w_sigma, double L, double R, double e, double e0, double gamma,
+                       int precision, int64_t batch_max, int device);
+int pii_plan_dim(const pii_plan* plan);
+
 /* Free the plan, its tables and workspace (no reference counterpart: the
  * reference's numpy/cupy arrays are garbage collected). */
 int pii_plan_destroy(pii_plan* plan);
@@ -156,8 +170,9 @@ int pii_step(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, c
  *           term P dt / (kn + P dt) (M[rho, u1, T_new] - M[rho, u1, T]) with
  *           T_new = (T - 8 tau / (1 - e^2)) exp(-(1 - e^2) rho dt / (4 kn)) + 8 tau / (1 - e^2),
  *           rho, u1 (first velocity component) and T from the FP64 moments of f.
- *           The reference implements it for 2D velocity only; this is the 3D-velocity
- *           form (Maxwellian in 3D, bulk velocity (u1, 0, 0) as in the reference).
+ *           2D plans: the reference's form (2D Maxwellian, T = E / rho - |u|^2 / 2);
+ *           3D plans: its 3D-velocity form (Maxwellian in 3D, bulk velocity
+ *           (u1, 0, 0), T = (2/3)(E / rho - |u|^2 / 2)).
  * penalty: P; e, tau: CONSP_M only.  dx <= 0: no transport (homogeneous cells).
  */
 int pii_step_splitting(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, double dx,
@@ -176,12 +191,27 @@ int pii_state_check(pii_plan* plan, const double* f, double* out, int64_t cells,
 
 /*
  * FP64 moments per cell: out[c*5 + {0,1,2,3,4}] = sum f, sum f v1, sum f v2,
- * sum f v3, sum f |v|^2 / 2, each times delta^3 (3D-velocity form of
- * State.rho / u / T, src/state.py:31-52,91-92).  v: n velocity centres (host).
+ * sum f v3, sum f |v|^2 / 2, each times delta^dim (State.rho / u / T,
+ * src/state.py:31-52,91-92; 2D plans: the reference's form, v3 term 0).
+ * v: n velocity centres (host).
  * out is a device array of cells*5 doubles.
  */
 int pii_moments(pii_plan* plan, const double* f, double* out, int64_t cells, const double* v, double delta,
                 void* stream);
+
+/*
+ * One iteration of BoltzmannFastSweep.step (src/iter_solver.py:38-62), FP64, in
+ * place on the device state f (nx cells): with q = the collision term of the
+ * current f (device, as the operator's __call__ returns it) and rho the
+ * cells' densities, a Gauss-Seidel upwind sweep in x
+ *   v1 > 0: f[i] = (nu q[i] + (v1/dx) f[i-1]) / (nu rho[i] + v1/dx),  i = 1 .. nx-2
+ *   v1 < 0: f[i] = (nu q[i] - (v1/dx) f[i+1]) / (nu rho[i] - v1/dx),  i = nx-2 .. 1
+ * with nu = 1 / sqrt(pi/2) / kn.  *err (host) receives max |f_new - f_old|.
+ * v1: n first-axis velocity centres (host).  The reference writes the sweep for
+ * 2D velocity; 3D plans sweep every (v2, v3) the same way.  Synchronises the stream.
+ */
+int pii_fast_sweep(pii_plan* plan, double* f, const double* q, int64_t nx, double dx, double kn, const double* v1,
+                   double* err, void* stream);
 
 /* f[i] += a * (b * d[i]) for i < count, FP64 (the projective extrapolation
  * f += M_l * df_l, src/boltzmann.py:128,138-140,154-158). */

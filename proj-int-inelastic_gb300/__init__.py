@@ -8,10 +8,10 @@ sm_103a CUDA kernels in ``libpii_gb300.so`` (C ABI: ``include/pii_gb300.h``).
 from . import _lib
 from .collision import FSInelasticVHSCollision, Plan, SpectralMesh, get_sphrquadrule
 from .ensemble import Ensemble
-from .solver import (BC, BoltzmannSolver, BoltzmannSolver0D, BoltzmannSolver1D, IterativeBoltzmannSolver,
-                     Solution, Solver, State)
+from .solver import (BC, BoltzmannFastSweep, BoltzmannSolver, BoltzmannSolver0D, BoltzmannSolver1D,
+                     IterativeBoltzmannSolver, Solution, Solver, State)
 
 __all__ = [
-    "BC", "BoltzmannSolver", "Ensemble", "BoltzmannSolver0D", "BoltzmannSolver1D", "FSInelasticVHSCollision",
+    "BC", "BoltzmannFastSweep", "BoltzmannSolver", "Ensemble", "BoltzmannSolver0D", "BoltzmannSolver1D", "FSInelasticVHSCollision",
     "IterativeBoltzmannSolver", "Plan", "Solution", "Solver", "SpectralMesh", "State", "get_sphrquadrule",
 ]

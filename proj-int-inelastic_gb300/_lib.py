@@ -38,6 +38,9 @@ SIGNATURES = {
     "pii_version": (ctypes.c_char_p, []),
     "pii_plan_create": (_c_int, [ctypes.POINTER(_vp), _c_int, _c_int, _c_int, _pdbl, _pdbl, _pdbl, _c_dbl, _c_dbl,
                                  _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_i64, _c_int]),
+    "pii_plan_create_nd": (_c_int, [ctypes.POINTER(_vp), _c_int, _c_int, _c_int, _c_int, _pdbl, _pdbl, _pdbl, _c_dbl,
+                                    _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_i64, _c_int]),
+    "pii_plan_dim": (_c_int, [_vp]),
     "pii_plan_destroy": (_c_int, [_vp]),
     "pii_plan_workspace_bytes": (_c_i64, [_vp]),
     "pii_plan_set_gain_path": (_c_int, [_vp, _c_int]),
@@ -54,6 +57,7 @@ SIGNATURES = {
                                     _c_dbl, _c_dbl, _c_int, _c_int, _c_int, _vp]),
     "pii_state_check": (_c_int, [_vp, _vp, _vp, _c_i64, _pdbl, _c_dbl, _vp]),
     "pii_moments": (_c_int, [_vp, _vp, _vp, _c_i64, _pdbl, _c_dbl, _vp]),
+    "pii_fast_sweep": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _pdbl, _vp]),
     "pii_axpby": (_c_int, [_vp, _vp, _c_dbl, _c_dbl, _c_i64, _vp]),
     "pii_collide_noalloc": (_c_int, [_vp, _vp, _c_i64, _c_int, _c_int, _c_int, _pdbl, _pdbl, _pdbl, _c_dbl, _c_dbl,
                                      _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _vp]),

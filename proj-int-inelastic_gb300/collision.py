@@ -3,7 +3,8 @@
 * ``SpectralMesh(config)`` -- velocity mesh and quadratures
   (src/collision/spectral_mesh.py:8-132);
 * ``FSInelasticVHSCollision(config, spectral_mesh)`` -- the fast
-  Fourier-spectral inelastic VHS operator with ``__call__(input_f,
+  Fourier-spectral inelastic VHS operator (3D velocity: sinc kernel on a
+  spherical design; 2D velocity: J_0 kernel on the circle quadrature) with ``__call__(input_f,
   heat_bath=None, device=...)``, ``collide(input_f, with_loss=False)`` and
   ``laplacian(input_f)`` (src/collision/base.py:7-58,
   src/collision/inelastic_collisions.py:116-230).
@@ -78,14 +79,18 @@ class SpectralMesh:
         self._wr = 0.5 * self._R * w
         self._ndim = int(config["collision-model"]["dim"])
         if self._ndim == 2:
-            raise NotImplementedError("the GB300 operator implements the 3D-velocity model only")
-        if self._ndim != 3:
+            # circle quadrature (src/collision/spectral_mesh.py:51-56)
+            self._nphi = int(config["circle-quad-rule"]["nphi"])
+            self._wphi = 2 * math.pi / self._nphi
+            self._phi = np.arange(0, 2 * math.pi, self._wphi)
+        elif self._ndim == 3:
+            sp = config["spherical-design-rule"]
+            self._ssrule = sp.get("ssrule", "womersley")
+            self._nsphr = int(sp["nsphr"])
+            self._spts = get_sphrquadrule("symmetric", rule=sp.get("points", self._ssrule), npts=self._nsphr)
+            self._wspts = 4 * math.pi / self._nsphr
+        else:
             raise ValueError("Dimension must be 2 or 3.")
-        sp = config["spherical-design-rule"]
-        self._ssrule = sp.get("ssrule", "womersley")
-        self._nsphr = int(sp["nsphr"])
-        self._spts = get_sphrquadrule("symmetric", rule=sp.get("points", self._ssrule), npts=self._nsphr)
-        self._wspts = 4 * math.pi / self._nsphr
         self._v_center = None
         self._v_centers = None
 
@@ -104,9 +109,13 @@ class SpectralMesh:
 
     @property
     def ncirc_or_nsphr(self):
-        return self._nsphr
+        return self._nphi if self._ndim == 2 else self._nsphr
 
     def circ_or_sphr_quad(self):
+        """(directions, weight): (cos phi, sin phi) and 2 pi / n_phi in 2D, the
+        spherical design and 4 pi / n_sigma in 3D (src/collision/spectral_mesh.py:94-101)."""
+        if self._ndim == 2:
+            return np.stack((np.cos(self._phi), np.sin(self._phi)), axis=-1), self._wphi
         return self._spts, self._wspts
 
     @property
@@ -168,13 +177,14 @@ class Plan:
         self._r = np.ascontiguousarray(r, np.float64)
         self._wr = np.ascontiguousarray(wr, np.float64)
         self._sigma = np.ascontiguousarray(sigma, np.float64)
+        self.dim = int(mesh.ndim)
         h = _lib._vp()
         torch.cuda.init()
-        st = lib.pii_plan_create(
-            _lib.ctypes.byref(h), int(mesh.nv), int(len(self._r)), int(len(self._sigma)), _lib.dptr(self._r),
-            _lib.dptr(self._wr), _lib.dptr(self._sigma), float(wsigma), float(mesh.L), float(mesh.R), float(e),
-            float(e0), float(gamma), int(precision), self.batch_max, self.device)
-        _lib.check(st, "pii_plan_create")
+        st = lib.pii_plan_create_nd(
+            _lib.ctypes.byref(h), self.dim, int(mesh.nv), int(len(self._r)), int(len(self._sigma)),
+            _lib.dptr(self._r), _lib.dptr(self._wr), _lib.dptr(self._sigma), float(wsigma), float(mesh.L),
+            float(mesh.R), float(e), float(e0), float(gamma), int(precision), self.batch_max, self.device)
+        _lib.check(st, "pii_plan_create_nd")
         self.handle = h.value
         self._lib = lib
         if gain_path is not None:
@@ -270,7 +280,7 @@ class FSInelasticVHSCollision:
         self._e = float(cm.get("e", 1.0))
         self._e0 = float(cm.get("e0", 1.0))
         self._gamma = float(cm.get("gamma", 0.0))
-        if self.ndim != 3:
+        if self.ndim not in (2, 3):
             raise ValueError("Dimension must be 2 or 3.")
         self._sphr_fac = 2 * math.pi ** (0.5 * self.ndim) / math.gamma(0.5 * self.ndim)
 
@@ -299,9 +309,9 @@ class FSInelasticVHSCollision:
     # -- evaluation --------------------------------------------------------
     def _as_device(self, input_f):
         """(device FP64 contiguous tensor, was_numpy)."""
-        n = self.sm.nv
-        if tuple(input_f.shape[-3:]) != (n, n, n):
-            raise ValueError(f"input_f must end with ({n}, {n}, {n}), got {tuple(input_f.shape)}")
+        n, d = self.sm.nv, self.ndim
+        if tuple(input_f.shape[-d:]) != (n,) * d or len(input_f.shape) < d:
+            raise ValueError(f"input_f must end with {(n,) * d}, got {tuple(input_f.shape)}")
         if isinstance(input_f, torch.Tensor):
             t = input_f
             if not t.is_cuda:
@@ -319,7 +329,7 @@ class FSInelasticVHSCollision:
 
     def _run(self, input_f, with_loss, heat_bath):
         f, was_np = self._as_device(input_f)
-        lead = f.shape[:-3]
+        lead = f.shape[:-self.ndim]
         cells = int(np.prod(lead)) if len(lead) else 1
         plan = self._ensure_plan(cells)
         q = torch.empty_like(f)

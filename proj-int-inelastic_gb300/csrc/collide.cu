@@ -58,6 +58,7 @@ static int collide_n(pii_plan* p, const double* f, double* q, int64_t cells, int
 }
 
 int prepare_impl(pii_plan* p) {
+  if (p->dim == 2) return PII_OK;  // the 2D kernels set their attributes on first use
   const bool f32 = p->precision == PII_PREC_FP32;
   switch (p->n) {
     case 8: return f32 ? CollideKernels<float, 8>::prepare() : CollideKernels<double, 8>::prepare();
@@ -85,8 +86,13 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
     set_error("pii_collide: f and q must not alias");
     return PII_ERR_ARG;
   }
-  int st = p->precision == PII_PREC_FP32 ? collide_n<float>(p, f, q, cells, with_loss, hb, s)
-                                         : collide_n<double>(p, f, q, cells, with_loss, hb, s);
+  int st = PII_OK;
+  if (p->dim == 2)
+    st = p->precision == PII_PREC_FP32 ? collide2d_f32(p, f, q, cells, with_loss, hb, s)
+                                       : collide2d_f64(p, f, q, cells, with_loss, hb, s);
+  else
+    st = p->precision == PII_PREC_FP32 ? collide_n<float>(p, f, q, cells, with_loss, hb, s)
+                                       : collide_n<double>(p, f, q, cells, with_loss, hb, s);
   if (st != PII_OK) return st;
   if (mass_fix) PII_TRY(mass_fix_impl(p, q, cells, p->N, s));
   return PII_OK;

@@ -50,13 +50,16 @@ enum Stage {
 
 // Device tables, all in the plan's working precision (float or double).
 //   ephase [Q][3][n] complex : exp(-i pi r sigma_d k / L); the d = 0 row also
-//                              carries the 1/n^3 of the first inverse FFT
+//                              carries the 1/n^dim of the first inverse FFT
 //   gphase [Q][3][n] complex : exp(+i a(r) r sigma_d k)
-//   gsinc  [n_r][M+1] real   : r^{gamma+2} w_r w_sigma sinc(a(r) r sqrt(m))
-//                              (the 4 pi prefactor cancels the 1/(4 pi) of collide)
-//   lossk  [M+1] real        : sum_r 4 pi r^{gamma+2} w_r sinc(pi r sqrt(m) / L)
+//   gsinc  [n_r][M+1] real   : r^{gamma+dim-1} w_r w_sigma K(a(r) r sqrt(m))
+//                              (the sphere constant cancels the 1/(4 pi) or
+//                              1/(2 pi) of collide)
+//   lossk  [M+1] real        : sum_r S r^{gamma+dim-1} w_r K(pi r sqrt(m) / L)
 //   lapl   [M+1] real        : -pi^2 m / L^2
-// with k the signed spectral index of the storage position and m = |k|^2 <= M = 3 (n/2)^2.
+// with k the signed spectral index of the storage position, m = |k|^2 <= M =
+// dim (n/2)^2, K = sinc and S = 4 pi in 3D, K = J_0 and S = 2 pi in 2D (the
+// third row of the per-axis tables is unused in 2D).
 // For n = 32 in FP32 the a-parity kernel also keeps, per pair and parity p
 // (W = exp(-2 pi i / 32), e_a / g_a the d = 0 rows above):
 //   epar [Q][2][32] complex  : W^{-p k} e_a[k] (k < 16), (-1)^p W^{-p k} e_a[k + 16]
@@ -101,6 +104,7 @@ struct ProfEvent {
 }  // namespace pii
 
 struct pii_plan {
+  int dim = 3;  // velocity dimension (2: J_0 kernel on a circle, 3: sinc on a sphere)
   int n = 0, nr = 0, ns = 0, Q = 0;
   int64_t N = 0;
   int precision = 0;
@@ -121,7 +125,7 @@ struct pii_plan {
   double* d2 = nullptr;
   double* v1dev = nullptr;  // n first-axis velocities (device)
   double* mom = nullptr;    // batch_max * 5 FP64 moment sums (CONSP_M)
-  int* flag = nullptr;      // device flag of pii_state_check
+  int* flag = nullptr;      // 16 device bytes: pii_state_check flag (0), pii_fast_sweep error word (8)
   double delta3 = 0;        // velocity cell volume of the last splitting step
   // gain kernel for n = 32, FP32: 0 = column/plane pipeline, 1 = fused
   // 2-CTA-cluster kernel, 2 = fused a-parity kernel (tensor-memory accumulator)
@@ -168,6 +172,9 @@ int prepare_impl(pii_plan* p);
 // gain_cluster.cu
 int gain_cluster_prepare(pii_plan* p);
 int gain_cluster_run(pii_plan* p, int64_t cells, cudaStream_t s);
+// collide2d_f32.cu / collide2d_f64.cu: the 2D-velocity operator
+int collide2d_f32(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb, cudaStream_t s);
+int collide2d_f64(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb, cudaStream_t s);
 // gain_parity.cu
 int gain_parity_prepare(pii_plan* p);
 int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s);

@@ -75,31 +75,50 @@ bool GraphKey::operator<(const GraphKey& o) const {
 
 static double sinc(double x) { return x == 0.0 ? 1.0 : std::sin(x) / x; }
 
+// J_0(x) = (1/pi) int_0^pi cos(x sin t) dt by the trapezoidal rule, which
+// converges geometrically for this periodic integrand once the node count
+// exceeds ~x (64 + 2 ceil|x| nodes: |error| < 3e-15 up to x = 200 against
+// scipy.special.jv(0, x), the reference's kernel, inelastic_collisions.py:42-43)
+static double bessel_j0(double x) {
+  const double pi = 3.141592653589793238462643383279502884;
+  x = std::fabs(x);
+  const int nodes = 64 + 2 * int(std::ceil(x));
+  const double h = pi / nodes;
+  double s = 1.0;  // (f(0) + f(pi)) / 2, f(0) = f(pi) = 1
+  for (int k = 1; k < nodes; ++k) s += std::cos(x * std::sin(k * h));
+  return s / nodes;
+}
+
 template <typename T>
 static int upload_tables(pii_plan* p) {
-  const int n = p->n, nr = p->nr, ns = p->ns, Q = p->Q;
-  const int M = 3 * (n / 2) * (n / 2);
+  const int n = p->n, nr = p->nr, ns = p->ns, Q = p->Q, dim = p->dim;
+  const int M = dim * (n / 2) * (n / 2);
   p->tab.M = M;
   const double pi = 3.141592653589793238462643383279502884;
-  std::vector<T> eph(size_t(Q) * 3 * n * 2), gph(size_t(Q) * 3 * n * 2);
+  // per-axis rows: always 3 per pair (the 2D operator leaves the third unused)
+  std::vector<T> eph(size_t(Q) * 3 * n * 2, T(0)), gph(size_t(Q) * 3 * n * 2, T(0));
   std::vector<T> gs(size_t(nr) * (M + 1)), lk(M + 1), lp(M + 1);
   const double invN = 1.0 / double(p->N);
+  // sphere (circle) constant 2 pi^{d/2} / Gamma(d/2): 4 pi in 3D, 2 pi in 2D (:50-52)
+  const double sphr = dim == 3 ? 4.0 * pi : 2.0 * pi;
+  // radial kernel sp_func: sin(x)/x in 3D, J_0 in 2D (:42-45)
+  auto kern = [dim](double x) { return dim == 3 ? sinc(x) : bessel_j0(x); };
   std::vector<double> lk_d(M + 1, 0.0);
   for (int ir = 0; ir < nr; ++ir) {
     const double r = p->r[ir], wr = p->wr[ir];
     // restitution law and exponential factor (inelastic_collisions.py:77-80)
     const double er = 0.5 * (p->e0 - p->e) * std::tanh(r - 0.5 * p->R) + 0.5 * (p->e0 + p->e);
     const double afac = 0.25 * pi * (1.0 + er) / p->L;
-    const double rg = std::pow(r, p->gamma + 2.0);  // pre_fac(r) / (4 pi)  (:54-55)
+    const double rg = std::pow(r, p->gamma + dim - 1.0);  // pre_fac(r) / sphr  (:54-55)
     for (int m = 0; m <= M; ++m) {
       const double kn = std::sqrt(double(m));
-      gs[size_t(ir) * (M + 1) + m] = T(rg * wr * p->wsigma * sinc(afac * r * kn));
-      lk_d[m] += 4.0 * pi * rg * wr * sinc(pi * r * kn / p->L);  // loss (:109-114)
+      gs[size_t(ir) * (M + 1) + m] = T(rg * wr * p->wsigma * kern(afac * r * kn));
+      lk_d[m] += sphr * rg * wr * kern(pi * r * kn / p->L);  // loss (:109-114)
     }
     for (int is = 0; is < ns; ++is) {
       const int pair = ir * ns + is;
-      for (int d = 0; d < 3; ++d) {
-        const double sd = p->sigma[size_t(is) * 3 + d];
+      for (int d = 0; d < dim; ++d) {
+        const double sd = p->sigma[size_t(is) * dim + d];
         for (int i = 0; i < n; ++i) {
           const int k = i < n / 2 ? i : i - n;
           const double th_e = -pi * r * sd * double(k) / p->L;
@@ -114,7 +133,7 @@ static int upload_tables(pii_plan* p) {
       }
     }
   }
-  if (std::is_same<T, float>::value && n == 32) {
+  if (std::is_same<T, float>::value && n == 32 && dim == 3) {
     // a-parity rows: the first-axis rows with the radix-2 twiddles of the
     // parity split folded in, evaluated in FP64 (angles reduced exactly)
     std::vector<T> ep2(size_t(Q) * 2 * 32 * 2), gp2(size_t(Q) * 2 * 32 * 2);
@@ -197,14 +216,18 @@ static void free_plan(pii_plan* p) {
   delete p;
 }
 
-static int create(pii_plan** out, int n, int nr, int ns, const double* r, const double* wr, const double* sigma,
-                  double wsigma, double L, double R, double e, double e0, double gamma, int precision,
-                  int64_t batch_max, int device) {
+static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* r, const double* wr,
+                  const double* sigma, double wsigma, double L, double R, double e, double e0, double gamma,
+                  int precision, int64_t batch_max, int device) {
   if (!out) {
     set_error("pii_plan_create: out is NULL");
     return PII_ERR_ARG;
   }
   *out = nullptr;
+  if (dim != 2 && dim != 3) {
+    set_error("pii_plan_create: Dimension must be 2 or 3.");
+    return PII_ERR_ARG;
+  }
   if (!(n == 8 || n == 16 || n == 24 || n == 32 || n == 48 || n == 64)) {
     set_error("pii_plan_create: n = %d unsupported (8, 16, 24, 32, 48, 64)", n);
     return PII_ERR_ARG;
@@ -223,7 +246,8 @@ static int create(pii_plan** out, int n, int nr, int ns, const double* r, const 
   p->nr = nr;
   p->ns = ns;
   p->Q = nr * ns;
-  p->N = int64_t(n) * n * n;
+  p->dim = dim;
+  p->N = dim == 3 ? int64_t(n) * n * n : int64_t(n) * n;
   p->precision = precision;
   p->device = device;
   p->L = L;
@@ -235,7 +259,7 @@ static int create(pii_plan** out, int n, int nr, int ns, const double* r, const 
   p->batch_max = batch_max;
   p->r.assign(r, r + nr);
   p->wr.assign(wr, wr + nr);
-  p->sigma.assign(sigma, sigma + size_t(ns) * 3);
+  p->sigma.assign(sigma, sigma + size_t(ns) * dim);
   int st = precision == PII_PREC_FP32 ? upload_tables<float>(p) : upload_tables<double>(p);
   if (st != PII_OK) {
     free_plan(p);
@@ -256,7 +280,7 @@ static int create(pii_plan** out, int n, int nr, int ns, const double* r, const 
       (s2 = alloc(p, (void**)&p->d0, size_t(batch_max) * N * 8)) != PII_OK ||
       (s2 = alloc(p, (void**)&p->v1dev, size_t(n) * 8)) != PII_OK ||
       (s2 = alloc(p, (void**)&p->mom, size_t(batch_max) * 5 * 8)) != PII_OK ||
-      (s2 = alloc(p, (void**)&p->flag, sizeof(int))) != PII_OK) {
+      (s2 = alloc(p, (void**)&p->flag, 16)) != PII_OK) {  // guard flag + sweep error word
     free_plan(p);
     return s2;
   }
@@ -264,7 +288,7 @@ static int create(pii_plan** out, int n, int nr, int ns, const double* r, const 
     free_plan(p);
     return s2;
   }
-  if (n == 32 && precision == PII_PREC_FP32) {
+  if (n == 32 && precision == PII_PREC_FP32 && dim == 3) {
     if ((s2 = gain_cluster_prepare(p)) != PII_OK || (s2 = gain_parity_prepare(p)) != PII_OK) {
       free_plan(p);
       return s2;
@@ -286,9 +310,18 @@ const char* pii_version(void) { return "pii_gb300 0.1 (sm_103a)"; }
 int pii_plan_create(pii_plan** out, int n, int n_r, int n_sigma, const double* r, const double* w_r,
                     const double* sigma, double w_sigma, double L, double R, double e, double e0,
                     double gamma, int precision, int64_t batch_max, int device) {
-  return pii::create(out, n, n_r, n_sigma, r, w_r, sigma, w_sigma, L, R, e, e0, gamma, precision, batch_max,
+  return pii::create(out, 3, n, n_r, n_sigma, r, w_r, sigma, w_sigma, L, R, e, e0, gamma, precision, batch_max,
                      device);
 }
+
+int pii_plan_create_nd(pii_plan** out, int dim, int n, int n_r, int n_sigma, const double* r, const double* w_r,
+                       const double* sigma, double w_sigma, double L, double R, double e, double e0, double gamma,
+                       int precision, int64_t batch_max, int device) {
+  return pii::create(out, dim, n, n_r, n_sigma, r, w_r, sigma, w_sigma, L, R, e, e0, gamma, precision,
+                     batch_max, device);
+}
+
+int pii_plan_dim(const pii_plan* plan) { return plan ? plan->dim : -1; }
 
 int pii_plan_destroy(pii_plan* plan) {
   if (!plan) {

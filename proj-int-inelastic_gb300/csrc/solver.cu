@@ -160,7 +160,7 @@ int pii_step_splitting(pii_plan* plan, int integrator, double* f, int64_t nx, do
   if (dx > 0) PII_TRY(pii::check_bcs(bc_lower, bc_upper));
   PII_TRY(pii::upload_v1(plan, v1, s));
   const double delta = v1[1] - v1[0];
-  plan->delta3 = delta * delta * delta;
+  plan->delta3 = plan->dim == 3 ? delta * delta * delta : delta * delta;  // velocity cell volume
   pii::StepCtx c{plan, f, nx, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, s};
   if (!use_graph || s == nullptr || plan->prof) return pii::splitting_body(c, integrator, dt, penalty, e, tau);
   pii::GraphKey key{integrator, f, nx, dt, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, 0,

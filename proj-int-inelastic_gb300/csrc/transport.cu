@@ -9,6 +9,8 @@
 //   * k_moments   : per-cell FP64 sums of f, f v, f |v|^2 / 2
 // The state f and every increment are FP64 in every precision mode.
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 
 #include "pii_internal.cuh"
 
@@ -102,18 +104,19 @@ __global__ void __launch_bounds__(256) k_massfix(double* q, int64_t N) {
   for (int64_t i = threadIdx.x; i < N; i += blockDim.x) qc[i] -= m;
 }
 
-__global__ void __launch_bounds__(256) k_moments(const double* f, double* out, const double* v, int n,
+// per-cell sums of f, f v1, f v2, f v3 (0 in 2D), f |v|^2 / 2, times dv
+__global__ void __launch_bounds__(256) k_moments(const double* f, double* out, const double* v, int n, int dim,
                                                   double dv) {
   __shared__ double sh[8];
-  const int64_t N = int64_t(n) * n * n;
+  const int64_t N = dim == 3 ? int64_t(n) * n * n : int64_t(n) * n;
+  const int64_t slab = N / n;  // points per first-axis index
   const double* fc = f + int64_t(blockIdx.x) * N;
   double m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0;
   for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
-    const int a = int(i / (int64_t(n) * n));
-    const int b = int((i / n) % n);
-    const int c = int(i % n);
+    const int a = int(i / slab);
+    const int b = dim == 3 ? int((i / n) % n) : int(i % n);
     const double x = fc[i];
-    const double va = v[a], vb = v[b], vc = v[c];
+    const double va = v[a], vb = v[b], vc = dim == 3 ? v[i % n] : 0.0;
     m0 += x;
     m1 += x * va;
     m2 += x * vb;
@@ -128,29 +131,74 @@ __global__ void __launch_bounds__(256) k_moments(const double* f, double* out, c
   }
 }
 
-// CONSP_M update: f += c Q + c2 (M[rho, u1, T_new] - M[rho, u1, T]) per cell, moments from mom
+// CONSP_M update: f += c Q + c2 (M[rho, u1, T_new] - M[rho, u1, T]) per cell,
+// moments from mom.  dim = 2 is the reference's form (src/boltzmann.py:9-13,96-118,
+// T = E / rho - |u|^2 / 2 of src/state.py:45-52); dim = 3 its 3D generalisation.
 __global__ void __launch_bounds__(256) k_consp_m(double* f, const double* q, const double* mom, const double* v, int n,
-                                                  int64_t count, double c, double c2, double dt, double kn, double e,
-                                                  double tau) {
+                                                  int dim, int64_t count, double c, double c2, double dt, double kn,
+                                                  double e, double tau) {
   const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (gid >= count) return;
-  const int64_t N = int64_t(n) * n * n;
+  const int64_t N = dim == 3 ? int64_t(n) * n * n : int64_t(n) * n;
   const int64_t cell = gid / N;
   const int64_t j = gid - cell * N;
   const double* m = mom + cell * 5;
   const double rho = m[0];
   const double u = m[1] / rho;
   const double ux = m[1] / rho, uy = m[2] / rho, uz = m[3] / rho;
-  const double T = (2.0 / 3.0) * (m[4] / rho - 0.5 * (ux * ux + uy * uy + uz * uz));
+  const double T = (2.0 / dim) * (m[4] / rho - 0.5 * (ux * ux + uy * uy + uz * uz));
   const double ee = 1.0 - e * e;
   const double Tinf = 8.0 * tau / ee;
   const double Tn = (T - Tinf) * exp(-ee / kn / 4.0 * rho * dt) + Tinf;
-  const double v1 = v[j / (int64_t(n) * n)], v2 = v[(j / n) % n], v3 = v[j % n];
+  const int64_t slab = N / n;
+  const double v1 = v[j / slab], v2 = dim == 3 ? v[(j / n) % n] : v[j % n], v3 = dim == 3 ? v[j % n] : 0.0;
   const double d2 = (v1 - u) * (v1 - u) + v2 * v2 + v3 * v3;
   const double pi = 3.141592653589793238462643383279502884;
-  const double Mn = rho / pow(2.0 * pi * Tn, 1.5) * exp(-d2 / (2.0 * Tn));
-  const double Mo = rho / pow(2.0 * pi * T, 1.5) * exp(-d2 / (2.0 * T));
+  const double Mn = dim == 3 ? rho / pow(2.0 * pi * Tn, 1.5) * exp(-d2 / (2.0 * Tn))
+                             : rho / (2.0 * pi * Tn) * exp(-d2 / (2.0 * Tn));
+  const double Mo = dim == 3 ? rho / pow(2.0 * pi * T, 1.5) * exp(-d2 / (2.0 * T))
+                             : rho / (2.0 * pi * T) * exp(-d2 / (2.0 * T));
   f[gid] += c * q[gid] + c2 * (Mn - Mo);
+}
+
+// One Gauss-Seidel upwind sweep of BoltzmannFastSweep.step (src/iter_solver.py:38-62)
+// for every velocity point j: v1 > 0 runs i = 1 .. nx-2 left to right,
+//   f[i] = (nu g[i] + (v1/dx) f[i-1]) / (nu rho[i] + v1/dx),
+// v1 < 0 runs i = nx-2 .. 1 right to left with f[i+1] and the signs flipped;
+// cells 0 and nx-1 and v1 = 0 points stay.  rho[i] = mom[5 i] (old f), g = the
+// collision term of the old f.  max |f_new - f_old| is folded into *errbits
+// (the bits of a non-negative double order like the value).
+__global__ void __launch_bounds__(256) k_sweep(double* f, const double* g, const double* mom, const double* v1,
+                                                int64_t nx, int64_t N, int64_t slab, double dx, double nu,
+                                                unsigned long long* errbits) {
+  const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  double err = 0.0;
+  if (j < N && nx > 2) {
+    const double v = v1[j / slab];
+    const double vdx = v / dx;
+    if (v > 0.0) {
+      double prev = f[j];
+      for (int64_t i = 1; i < nx - 1; ++i) {
+        const double old = f[i * N + j];
+        const double nw = (nu * g[i * N + j] + vdx * prev) / (nu * mom[i * 5] + vdx);
+        f[i * N + j] = nw;
+        err = fmax(err, fabs(nw - old));
+        prev = nw;
+      }
+    } else if (v < 0.0) {
+      double prev = f[(nx - 1) * N + j];
+      for (int64_t i = nx - 2; i >= 1; --i) {
+        const double old = f[i * N + j];
+        const double nw = (nu * g[i * N + j] - vdx * prev) / (nu * mom[i * 5] - vdx);
+        f[i * N + j] = nw;
+        err = fmax(err, fabs(nw - old));
+        prev = nw;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_down_sync(0xffffffffu, err, o));
+  if ((threadIdx.x & 31) == 0 && err > 0.0) atomicMax(errbits, static_cast<unsigned long long>(__double_as_longlong(err)));
 }
 
 __global__ void __launch_bounds__(256) k_nonfinite(const double* f, int64_t count, int* flag) {
@@ -166,13 +214,13 @@ int consp_m_impl(pii_plan* p, double* f, const double* q, int64_t cells, double 
   const int64_t count = cells * p->N;
   {
     StageTimer st(p, ST_AXPY, s);
-    k_moments<<<unsigned(cells), 256, 0, s>>>(f, p->mom, p->v1dev, p->n, p->delta3);
+    k_moments<<<unsigned(cells), 256, 0, s>>>(f, p->mom, p->v1dev, p->n, p->dim, p->delta3);
   }
   PII_CHECK_LAUNCH();
   {
     StageTimer st(p, ST_AXPY, s);
-    k_consp_m<<<unsigned((count + 255) / 256), 256, 0, s>>>(f, q, p->mom, p->v1dev, p->n, count, c, c2, dt, kn, e,
-                                                            tau);
+    k_consp_m<<<unsigned((count + 255) / 256), 256, 0, s>>>(f, q, p->mom, p->v1dev, p->n, p->dim, count, c, c2, dt,
+                                                            kn, e, tau);
   }
   PII_CHECK_LAUNCH();
   return PII_OK;
@@ -187,7 +235,7 @@ int transport_impl(pii_plan* p, const double* f, const double* q, double* df, in
   a.v1 = p->v1dev;
   a.nx = nx;
   a.N = p->N;
-  a.N2 = int64_t(p->n) * p->n;
+  a.N2 = p->N / p->n;  // points per first-axis velocity index
   a.dt = dt;
   a.kn = kn;
   a.transport = dx > 0.0 ? 1 : 0;
@@ -270,7 +318,8 @@ int pii_moments(pii_plan* plan, const double* f, double* out, int64_t cells, con
   cudaStream_t s = (cudaStream_t)stream;
   PII_CUDA(cudaSetDevice(plan->device));
   PII_TRY(pii::upload_v1(plan, v, s));
-  pii::k_moments<<<unsigned(cells), 256, 0, s>>>(f, out, plan->v1dev, plan->n, delta * delta * delta);
+  pii::k_moments<<<unsigned(cells), 256, 0, s>>>(f, out, plan->v1dev, plan->n, plan->dim,
+                                                  plan->dim == 3 ? delta * delta * delta : delta * delta);
   PII_CHECK_LAUNCH();
   return PII_OK;
 }
@@ -284,7 +333,8 @@ int pii_state_check(pii_plan* plan, const double* f, double* out, int64_t cells,
   cudaStream_t s = (cudaStream_t)stream;
   PII_CUDA(cudaSetDevice(plan->device));
   PII_TRY(pii::upload_v1(plan, v, s));
-  pii::k_moments<<<unsigned(cells), 256, 0, s>>>(f, out, plan->v1dev, plan->n, delta * delta * delta);
+  pii::k_moments<<<unsigned(cells), 256, 0, s>>>(f, out, plan->v1dev, plan->n, plan->dim,
+                                                  plan->dim == 3 ? delta * delta * delta : delta * delta);
   PII_CHECK_LAUNCH();
   PII_CUDA(cudaMemsetAsync(plan->flag, 0, sizeof(int), s));
   const int64_t count = cells * plan->N;
@@ -298,6 +348,39 @@ int pii_state_check(pii_plan* plan, const double* f, double* out, int64_t cells,
     pii::set_error("pii_state_check: f holds NaN or Inf values");
     return PII_ERR_NONFINITE;
   }
+  return PII_OK;
+}
+
+int pii_fast_sweep(pii_plan* plan, double* f, const double* q, int64_t nx, double dx, double kn, const double* v1,
+                   double* err, void* stream) {
+  if (!plan || !f || !q || !v1 || !err || nx <= 0 || !(dx > 0) || !(kn > 0)) {
+    pii::set_error("pii_fast_sweep: invalid arguments");
+    return PII_ERR_ARG;
+  }
+  if (nx > plan->batch_max) {
+    pii::set_error("pii_fast_sweep: nx beyond batch_max");
+    return PII_ERR_SIZE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  PII_CUDA(cudaSetDevice(plan->device));
+  PII_TRY(pii::upload_v1(plan, v1, s));
+  const double delta = v1[1] - v1[0];
+  const double dv = plan->dim == 3 ? delta * delta * delta : delta * delta;
+  pii::k_moments<<<unsigned(nx), 256, 0, s>>>(f, plan->mom, plan->v1dev, plan->n, plan->dim, dv);
+  PII_CHECK_LAUNCH();
+  // the plan's 16-byte flag block: int guard flag at 0, the sweep's error word at 8
+  auto* word = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(plan->flag) + 8);
+  PII_CUDA(cudaMemsetAsync(word, 0, sizeof(unsigned long long), s));
+  const double pi = 3.141592653589793238462643383279502884;
+  const double nu = 1.0 / std::sqrt(pi / 2.0) / kn;  // (src/iter_solver.py:46)
+  const int64_t N = plan->N;
+  pii::k_sweep<<<unsigned((N + 255) / 256), 256, 0, s>>>(f, q, plan->mom, plan->v1dev, nx, N, N / plan->n, dx, nu,
+                                                           word);
+  PII_CHECK_LAUNCH();
+  unsigned long long h = 0;
+  PII_CUDA(cudaMemcpyAsync(&h, word, sizeof(h), cudaMemcpyDeviceToHost, s));
+  PII_CUDA(cudaStreamSynchronize(s));
+  std::memcpy(err, &h, sizeof(double));
   return PII_OK;
 }
 

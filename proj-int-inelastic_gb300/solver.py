@@ -6,10 +6,12 @@
   ``inner_steps``, ``inner_dt``, ``bc_lower`` / ``bc_upper`` / ``all_bcs``,
   ``step``, ``df``, ``df_advection``, ``evolve_to_time``).
 * ``State`` / ``Solution`` hold f as a torch CUDA FP64 tensor of shape
-  (n_x, n, n, n) (or (n, n, n) for a space-homogeneous problem), with FP64
-  3D-velocity moments ``rho``, ``u``, ``T`` (src/state.py, src/solution.py).
+  (n_x, n, n, n) or (n_x, n, n) (3D or 2D velocity; no n_x for a
+  space-homogeneous problem), with FP64 moments ``rho``, ``u``, ``T``
+  (src/state.py, src/solution.py).
 * ``IterativeBoltzmannSolver`` keeps ``solve`` / ``step``
-  (src/iter_solver.py:9-35).
+  (src/iter_solver.py:9-35); ``BoltzmannFastSweep`` is its Gauss-Seidel
+  upwind sweep (src/iter_solver.py:38-62) on the GPU.
 
 With the GB300 ``FSInelasticVHSCollision`` as the collision operator, a whole
 macro-step (all inner steps, transport, FP64 extrapolations) runs as one
@@ -54,8 +56,12 @@ class State:
         return np.array([lo + (i + 0.5) * d for i in range(n)])
 
     @property
+    def dim_v(self):
+        return len(self.num_cells) - self.num_dim_x
+
+    @property
     def v(self):
-        """Velocity centres (same on the three velocity axes)."""
+        """Velocity centres (same on every velocity axis)."""
         return self.centers(self.num_dim_x)
 
     @property
@@ -67,23 +73,20 @@ class State:
         return self.delta[self.num_dim_x]
 
     def moments(self):
-        """FP64 (rho, u[3], T) per cell from ``pii_moments`` (3D-velocity form of
-        State.rho / u / T, src/state.py:31-52)."""
+        """FP64 (rho, u[dim], T) per cell from ``pii_moments``: State.rho / u / T
+        (src/state.py:31-52; T = E / rho - |u|^2 / 2 in 2D, (2/3)(E / rho -
+        |u|^2 / 2) in 3D)."""
         f = self.f
+        d = self.dim_v
         n = f.shape[-1]
-        cells = f.numel() // (n**3)
+        cells = f.numel() // (n**d)
         out = torch.empty((cells, 5), dtype=torch.float64, device=f.device)
-        plan = _moment_plan(n, f.device.index or 0)
+        plan = _moment_plan(n, f.device.index or 0, d, cells)
         v = np.ascontiguousarray(self.v, np.float64)
         st = plan._lib.pii_moments(plan.handle, f.contiguous().data_ptr(), out.data_ptr(), cells, _lib.dptr(v),
                                    float(self.dv), torch.cuda.current_stream().cuda_stream)
         _lib.check(st, "pii_moments")
-        m = out.cpu().numpy()
-        rho = m[:, 0]
-        u = m[:, 1:4] / rho[:, None]
-        T = (2.0 / 3.0) * (m[:, 4] / rho - 0.5 * (u**2).sum(-1))
-        shape = f.shape[:-3]
-        return rho.reshape(shape), u.reshape(shape + (3,)), T.reshape(shape)
+        return _split_moments(out.cpu().numpy(), d, f.shape[:-d])
 
     @property
     def rho(self):
@@ -98,17 +101,28 @@ class State:
         return self.moments()[2]
 
 
+def _split_moments(m, d, shape):
+    """(rho, u, T) from the per-cell sums [rho, m1, m2, m3, E] of pii_moments."""
+    rho = m[:, 0]
+    u = m[:, 1 : 1 + d] / rho[:, None]
+    T = (2.0 / d) * (m[:, 4] / rho - 0.5 * (u**2).sum(-1))
+    return rho.reshape(shape), u.reshape(tuple(shape) + (d,)), T.reshape(shape)
+
+
 _MPLANS = {}
 
 
-def _moment_plan(n, device):
-    """A minimal plan used only for its moment / velocity buffers."""
-    key = (n, device)
+def _moment_plan(n, device, dim=3, cells=1):
+    """A minimal plan used only for its moment / velocity / transport buffers."""
+    key = (n, device, dim)
+    if key in _MPLANS and _MPLANS[key].batch_max < cells:
+        _MPLANS.pop(key).close()
     if key not in _MPLANS:
         from .collision import Plan
 
         class _Mesh:
             nv = n
+            ndim = dim
             L = 1.0
             R = 1.0
 
@@ -118,9 +132,10 @@ def _moment_plan(n, device):
 
             @staticmethod
             def circ_or_sphr_quad():
-                return np.array([[0.0, 0.0, 1.0]]), 4 * math.pi
+                return (np.array([[0.0, 0.0, 1.0]]), 4 * math.pi) if dim == 3 else (np.array([[1.0, 0.0]]),
+                                                                                     2 * math.pi)
 
-        _MPLANS[key] = Plan(_Mesh, 1.0, 1.0, 0.0, _lib.PREC_FP64, 1, device)
+        _MPLANS[key] = Plan(_Mesh, 1.0, 1.0, 0.0, _lib.PREC_FP64, max(1, int(cells)), device)
     return _MPLANS[key]
 
 
@@ -132,8 +147,8 @@ class Solution:
     def __init__(self, config, device=0):
         get = (lambda k: config[k]) if isinstance(config, dict) else (lambda k: getattr(config, k))
         dim_x, dim_v = int(get("dim_x")), int(get("dim_v"))
-        if dim_v != 3:
-            raise NotImplementedError("the GB300 solver implements 3D velocity only")
+        if dim_v not in (2, 3):
+            raise ValueError("Dimension must be 2 or 3.")
         lower, upper, nn = [], [], []
         if dim_x:
             lower += [float(get("xmin"))] * dim_x
@@ -158,7 +173,7 @@ class Solution:
         return self.state.f
 
     def __getattr__(self, key):
-        if key in ("rho", "u", "T", "num_cells", "lower", "upper", "delta", "num_dim_x", "v"):
+        if key in ("rho", "u", "T", "num_cells", "lower", "upper", "delta", "num_dim_x", "v", "dim_v"):
             return getattr(self.state, key)
         raise AttributeError(key)
 
@@ -253,7 +268,7 @@ class BoltzmannSolver(Solver):
         """(nx, dx, v1, bc_lo, bc_hi); dx = 0 disables transport."""
         f = state.f
         n = f.shape[-1]
-        cells = f.numel() // n**3
+        cells = f.numel() // n**state.dim_v
         return cells, 0.0, np.ascontiguousarray(state.v, np.float64), _lib.BC_EXTRAP, _lib.BC_EXTRAP
 
 
@@ -304,9 +319,10 @@ class BoltzmannSolver(Solver):
         (relative) since the first check.  Returns (rho, u, T) per cell."""
         f = state.f
         n = f.shape[-1]
-        cells = f.numel() // n**3
+        d = state.dim_v
+        cells = f.numel() // n**d
         out = torch.empty((cells, 5), dtype=torch.float64, device=f.device)
-        plan = _moment_plan(n, f.device.index or 0)
+        plan = _moment_plan(n, f.device.index or 0, d, cells)
         v = np.ascontiguousarray(state.v, np.float64)
         st = plan._lib.pii_state_check(plan.handle, f.contiguous().data_ptr(), out.data_ptr(), cells, _lib.dptr(v),
                                        float(state.dv), torch.cuda.current_stream(f.device).cuda_stream)
@@ -317,10 +333,7 @@ class BoltzmannSolver(Solver):
             self._mass0 = mass
         elif self.mass_drift_tol is not None and abs(mass - self._mass0) > self.mass_drift_tol * abs(self._mass0):
             raise RuntimeError(f"total mass drifted from {self._mass0:.12g} to {mass:.12g}")
-        rho = m[:, 0]
-        u = m[:, 1:4] / rho[:, None]
-        T = (2.0 / 3.0) * (m[:, 4] / rho - 0.5 * (u**2).sum(-1))
-        return rho, u, T
+        return _split_moments(m, d, (cells,))
 
     def _fused_splitting(self, state, ti):
         f = state.f
@@ -454,34 +467,11 @@ class BoltzmannSolver1D(BoltzmannSolver):
         f = state.f.contiguous()
         nx, dx, v1, lo, hi = self._transport_args(state)
         out = torch.empty_like(f)
-        plan = _moment_plan(f.shape[-1], f.device.index or 0)
-        if plan.batch_max < nx:
-            _MPLANS.pop((f.shape[-1], f.device.index or 0)).close()
-            plan = _grow_mplan(f.shape[-1], f.device.index or 0, nx)
+        plan = _moment_plan(f.shape[-1], f.device.index or 0, state.dim_v, nx)
         st = plan._lib.pii_transport_df(plan.handle, f.data_ptr(), out.data_ptr(), nx, float(dt), dx, _lib.dptr(v1),
                                         lo, hi, torch.cuda.current_stream().cuda_stream)
         _lib.check(st, "pii_transport_df")
         return out
-
-
-def _grow_mplan(n, device, cells):
-    from .collision import Plan
-
-    class _Mesh:
-        nv = n
-        L = 1.0
-        R = 1.0
-
-        @staticmethod
-        def rquad():
-            return np.array([0.5]), np.array([1.0])
-
-        @staticmethod
-        def circ_or_sphr_quad():
-            return np.array([[0.0, 0.0, 1.0]]), 4 * math.pi
-
-    _MPLANS[(n, device)] = Plan(_Mesh, 1.0, 1.0, 0.0, _lib.PREC_FP64, cells, device)
-    return _MPLANS[(n, device)]
 
 
 class IterativeBoltzmannSolver:
@@ -517,3 +507,30 @@ class IterativeBoltzmannSolver:
 
     def step(self, solution):
         raise NotImplementedError("No stepping routine has been defined!")
+
+
+class BoltzmannFastSweep(IterativeBoltzmannSolver):
+    """``BoltzmannFastSweep`` (src/iter_solver.py:38-62): one ``step(state)`` =
+    the collision term and densities of the current state, then a Gauss-Seidel
+    upwind sweep in x (v1 > 0 left to right, v1 < 0 right to left, interior
+    cells) in FP64 on the GPU (``pii_fast_sweep``); returns max |f_new - f_old|.
+    The reference writes it for 2D velocity; 3D states sweep the same way over
+    (v2, v3)."""
+
+    def step(self, state):
+        f = state.f
+        if not (f.is_cuda and f.dtype == torch.float64 and f.is_contiguous()):
+            raise ValueError("state.f must be a contiguous CUDA float64 tensor")
+        q = self.collision(f)
+        if not isinstance(q, torch.Tensor):
+            q = torch.as_tensor(q, device=f.device)
+        q = q.to(torch.float64).contiguous()
+        nx = f.shape[0]
+        plan = _moment_plan(f.shape[-1], f.device.index or 0, state.dim_v, nx)
+        v1 = np.ascontiguousarray(state.v, np.float64)
+        err = _lib.ctypes.c_double()
+        st = plan._lib.pii_fast_sweep(plan.handle, f.data_ptr(), q.data_ptr(), nx, float(state.delta[0]),
+                                      float(self.kn), _lib.dptr(v1), _lib.ctypes.byref(err),
+                                      torch.cuda.current_stream(f.device).cuda_stream)
+        _lib.check(st, "pii_fast_sweep")
+        return err.value

@@ -93,7 +93,7 @@ def test_config_errors():
     with pytest.raises(ValueError):
         pkg.SpectralMesh(cfg)
     cfg["collision-model"]["dim"] = 2
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(KeyError):  # 2D needs config["circle-quad-rule"] (src/collision/spectral_mesh.py:52)
         pkg.SpectralMesh(cfg)
     cfg = op_config(16, L8_S, 8, 12, 0.9, 0.9, 1.0)
     sm = pkg.SpectralMesh(cfg)
@@ -124,3 +124,20 @@ def test_solver_host_logic():
     with pytest.raises(Exception, match="does not divide"):
         s._is_set_up = True
         s.evolve_to_time(_Sol(), 1.0)
+
+
+def test_mesh_2d_matches_oracle():
+    """2D-velocity mesh: circle quadrature and radial nodes as the reference's
+    SpectralMesh (src/collision/spectral_mesh.py:51-56,94-97)."""
+    import proj_int_inelastic_gb300 as pkg
+    from oracle import fs_inelastic as fo
+
+    cfg = {"velocity-mesh": {"nv": 32, "s": L8_S, "nr": 16}, "circle-quad-rule": {"nphi": 16},
+           "collision-model": {"dim": 2, "type": "vhs", "e": 0.8, "gamma": 0.0}}
+    sm = pkg.SpectralMesh(cfg)
+    m = fo.Mesh(32, L8_S, 16, dim=2, nphi=16)
+    sig, w = sm.circ_or_sphr_quad()
+    assert sm.ndim == 2 and sm.ncirc_or_nsphr == 16 and sig.shape == (16, 2)
+    assert np.array_equal(sig, m.sigma) and w == m.wsigma
+    assert np.array_equal(sm.rquad()[0], m.r) and np.array_equal(sm.v_center, m.v)
+    assert len(sm.v_centers) == 2 and sm.v_centers[0].shape == (32, 32)
