@@ -97,10 +97,12 @@ int64_t pii_plan_workspace_bytes(const pii_plan* plan);
 
 /*
  * Kernel choice for the gain term of n = 32 FP32 plans (tuning knob, no
- * reference counterpart): 2 = the fused a-parity kernel with its accumulator in
- * tensor memory (the default where it exists), 1 = the fused 2-CTA-cluster
- * kernel, 0 = the column / plane pass pipeline used for every other size and
- * for FP64.  All compute the same operator.
+ * reference counterpart): 3 = the fused a-parity kernel on antipodal direction
+ * pairs (sigma, -sigma packed into one real-phase pass) plus the exact
+ * Nyquist-plane correction (the default where the design is antipodally
+ * symmetric), 2 = the fused a-parity kernel with its accumulator in tensor
+ * memory, 1 = the fused 2-CTA-cluster kernel, 0 = the column / plane pass
+ * pipeline used for every other size and for FP64.  All compute the same operator.
  */
 int pii_plan_set_gain_path(pii_plan* plan, int path);
 
@@ -244,9 +246,9 @@ int pii_collide_noalloc(const double* f, double* q, int64_t cells, int n, int n_
  * pii_plan_profile_read fills ms[PII_NSTAGES] (summed device time) and
  * launches[PII_NSTAGES] after synchronising, and resets the counters.
  */
-#define PII_NSTAGES 13
+#define PII_NSTAGES 14
 /* stage order: fwd_plane, col_fwd, col_pstart, pair_plane, col_pend, reduce,
- * col_iprep, finish, df, axpy, massfix, gain_cluster, gain_parity */
+ * col_iprep, finish, df, axpy, massfix, gain_cluster, gain_parity, nyq_corr */
 int64_t pii_kernel_launches(void);
 int pii_plan_profile(pii_plan* plan, int enable);
 int pii_plan_profile_read(pii_plan* plan, double* ms, int64_t* launches);

@@ -66,9 +66,9 @@ SIGNATURES = {
     "pii_plan_profile_read": (_c_int, [_vp, _pdbl, ctypes.POINTER(ctypes.c_int64)]),
 }
 
-NSTAGES = 13
+NSTAGES = 14
 STAGES = ["fwd_plane", "col_fwd", "col_pstart", "pair_plane", "col_pend", "reduce", "col_iprep", "finish", "df",
-          "axpy", "massfix", "gain_cluster", "gain_parity"]
+          "axpy", "massfix", "gain_cluster", "gain_parity", "nyq_corr"]
 
 _lib = None
 

@@ -160,7 +160,7 @@ def _precision_of(config, precision):
     raise ValueError(f"precision must be 'mixed'/'fp32' or 'double'/'fp64', got {precision!r}")
 
 
-GAIN_PATHS = {"pipeline": 0, "cluster": 1, "parity": 2}
+GAIN_PATHS = {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3}
 
 
 class Plan:

@@ -25,8 +25,13 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
   const int64_t N = p->N;
   PII_TRY(K::fwd(p, f, 0, cells, s));
   if constexpr (std::is_same<T, float>::value && NV == 32) {
-    if (p->gain_path == 1 || p->gain_path == 2) {
-      PII_TRY(p->gain_path == 1 ? gain_cluster_run(p, cells, s) : gain_parity_run(p, cells, s));
+    if (p->gain_path >= 1 && p->gain_path <= 3) {
+      if (p->gain_path == 1) {
+        PII_TRY(gain_cluster_run(p, cells, s));
+      } else {
+        PII_TRY(gain_parity_run(p, cells, s, p->gain_path == 3));
+        if (p->gain_path == 3) PII_TRY(nyq_corr_run(p, cells, s));
+      }
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
   }
@@ -132,9 +137,11 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
   };
   std::vector<Cand> cands;
   const bool cluster_ok = plan->gc_clusters > 0;
-  if (cluster_ok)
-    for (int path : {1, 2})
-      for (int items : {2, 4, 6, 8}) cands.push_back({path, items, plan->chunk_points});
+  if (cluster_ok) {
+    for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points});
+    cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points});  // even split: no item knob
+    if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points});
+  }
   for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
     cands.push_back({0, plan->gc_items_per_cluster, pts});
   const int saved_path = plan->gain_path;
@@ -211,8 +218,12 @@ extern "C" int pii_plan_set_tuning(pii_plan* plan, int gain_path, int items_per_
 }
 
 extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
-  if (!plan || path < 0 || path > 2) {
-    pii::set_error("pii_plan_set_gain_path: path must be 0 (pipeline), 1 (cluster) or 2 (a-parity)");
+  if (!plan || path < 0 || path > 3) {
+    pii::set_error("pii_plan_set_gain_path: path must be 0 (pipeline), 1 (cluster), 2 (a-parity) or 3 (packed)");
+    return PII_ERR_ARG;
+  }
+  if (path == 3 && plan->ap_count == 0) {
+    pii::set_error("pii_plan_set_gain_path: the packed kernel needs an antipodally symmetric design");
     return PII_ERR_ARG;
   }
   if (path != 0 && (plan->gc_clusters <= 0 || plan->gp_ctas <= 0)) {

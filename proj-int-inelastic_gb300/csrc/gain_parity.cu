@@ -28,6 +28,7 @@
 #include <algorithm>
 
 #include "gain_common.cuh"
+#include "tmem.cuh"
 
 namespace pii {
 
@@ -42,48 +43,6 @@ constexpr size_t FS_OFF = size_t(PLANES) * N2 * sizeof(float2);
 constexpr size_t SMEM = FS_OFF + size_t(PLANES) * 32 * FPITCH * sizeof(float) + 16;
 }  // namespace gpar
 
-// ---- tensor-memory access (PTX tcgen05, CTA group 1)
-__device__ __forceinline__ void tm_alloc(uint32_t* slot, uint32_t ncols) {
-  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(slot));
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(a), "r"(ncols)
-               : "memory");
-}
-__device__ __forceinline__ void tm_relinquish() {
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tm_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tm_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tm_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// 16 consecutive 32-bit columns of this thread's lane
-__device__ __forceinline__ void tm_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
-// completes the loads above; the registers are tied to it so that no use is
-// scheduled before the wait
-__device__ __forceinline__ void tm_wait_ld(uint32_t (&r)[16]) {
-  asm volatile("tcgen05.wait::ld.sync.aligned;"
-               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
-                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
-                 "+r"(r[15]));
-}
-__device__ __forceinline__ void tm_st16(uint32_t taddr, const uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-      "%14, %15, %16};" ::"r"(taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]));
-}
-__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;"); }
-
 struct GainParityArgs {
   const float2* fhat;    // [cells][N3] spectra of f
   const float* fT;       // [cells][N3] f in FP32
@@ -93,6 +52,8 @@ struct GainParityArgs {
   const float2* gpar;    // [Q][2][32]
   const float* gsx;      // [n_r][513][20]
   int ns, Q;
+  int QP;                // passes per (cell, parity): Q, or the antipodal pairs when packed
+  const int* reps;       // [QP] pair index of each packed pass (packed mode)
   int64_t cells;
   float2* hpart;      // [CTAs + 2 cells][32][HSLOTS]
   const int4* ucols;  // [THREADS] (column, column, first slot, 1 if two self-conjugate columns)
@@ -201,6 +162,171 @@ __device__ __forceinline__ void par_stage_c(const float2* W, int j, const float2
   });
 }
 
+// ---------------------------------------------------------------------------
+// Packed (antipodal) mode.  The designs are symmetric: pair q = (r, -sigma_p)
+// has E_q = conj E_p and gain_q = conj gain_p.  With E+ = (E(k) + conj E(-k))/2
+// (the Hermitian part of the phase; it differs from E only where a component of
+// k is the Nyquist index 16), the real fields Re A_p = IFFT3(f^ E+_p) and
+// Re A_q pack into one complex pipeline whose input is f^ t with the REAL
+//   t(k) = Re E+_p(k) + Im E+_p(k)        (E+_p + i E+_q = (1 + i) t),
+// and whose output F gives the pairs' Hermitian gain contributions with the
+// REAL coefficient 2 s(k), s = Re g+_p - Im g+_p, g+ = (g(k) + conj g(-k))/2.
+// The remaining parts of the two pairs (E- = E - E+, g- = g - g+), which live on
+// the Nyquist planes only, are added by the Nyquist correction kernel.
+// Per column the separable factors give, for k_a != 16,
+//   t(k_a, j) = e_a.x (c.x + c.y) + e_a.y (c.x - c.y),  c = (e_bc(j) + e~_bc(j)) / 2,
+//   s(k_a, j) = g_a.x (d.x - d.y) - g_a.y (d.x + d.y),  d = (g_bc(j) + g~_bc(j)) / 2,
+// where ~ conjugates the factor of a Nyquist component; k_a = 16 takes the
+// two-term form directly.
+__device__ __forceinline__ float2 cconj(float2 v) { return make_float2(v.x, -v.y); }
+
+struct PackCol {
+  float cp, cm, t16;  // t(k_a, j) = e_a.x cp + e_a.y cm (k_a != 16); t(16, j) = t16
+};
+__device__ __forceinline__ PackCol pack_col_consts(const float2* ep, int jb, int jc) {
+  using namespace gc;
+  const float2 eb = ep[32 + jb], ec = ep[64 + jc];
+  const float2 ebc = cmul(eb, ec);
+  const float2 ebct = cmul(jb == 16 ? cconj(eb) : eb, jc == 16 ? cconj(ec) : ec);
+  const float2 c = make_float2(0.5f * (ebc.x + ebct.x), 0.5f * (ebc.y + ebct.y));
+  const float2 e16 = ep[16];
+  const float2 u = cmul(e16, ebc), v = cmul(cconj(e16), ebct);
+  PackCol r;
+  r.cp = c.x + c.y;
+  r.cm = c.x - c.y;
+  r.t16 = 0.5f * (u.x + v.x + u.y + v.y);
+  return r;
+}
+__device__ __forceinline__ float pack_t(float2 ea, const PackCol& c) { return fmaf(ea.y, c.cm, ea.x * c.cp); }
+
+// stage A (packed) for the column pair (j, -j), as par_stage_a_pair with the real phase t
+template <int PAR>
+__device__ __forceinline__ void pack_stage_a_pair(float2* W, const float2* fh, const float2* ep, int j) {
+  using namespace gc;
+  const int jb = j >> 5, jc = j & 31;
+  const int nb = (32 - jb) & 31, nc = (32 - jc) & 31;
+  const PackCol c0 = pack_col_consts(ep, jb, jc), c1 = pack_col_consts(ep, nb, nc);
+  const float4* e4 = reinterpret_cast<const float4*>(ep);
+  auto ea = [&](int k) {
+    const float4 v = e4[k >> 1];
+    return (k & 1) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
+  };
+  constexpr float sg = PAR ? -1.f : 1.f;
+  float2 u0[16], u1[16];
+  static_for<0, 16>([&](auto ki) {
+    constexpr int k = decltype(ki)::value;
+    constexpr int k1 = (16 - k) & 15;
+    const float2 lo = fh[k * N2 + j], hi = fh[(k + 16) * N2 + j];
+    const float tl = pack_t(ea(k), c0);
+    const float th = k == 0 ? c0.t16 : pack_t(ea(k + 16), c0);
+    const float2 y0 = make_float2(lo.x * tl + sg * hi.x * th, lo.y * tl + sg * hi.y * th);
+    u0[k] = twiddle<PAR * k, 32, +1>(y0);
+    const float ta = pack_t(ea(k1), c1);
+    const float tb = k1 == 0 ? c1.t16 : pack_t(ea(k1 + 16), c1);
+    // column -j: Y[k1] = conj F[-k1] t, Y[k1 + 16] = conj F[-k1 - 16] t (indices mod 32)
+    const float2 A = k == 0 ? cconj(lo) : cconj(hi), B = k == 0 ? cconj(hi) : cconj(lo);
+    const float2 y1 = make_float2(A.x * ta + sg * B.x * tb, A.y * ta + sg * B.y * tb);
+    u1[k1] = twiddle<PAR * k1, 32, +1>(y1);
+  });
+  fft_line<16, +1>(u0);
+  fft_line<16, +1>(u1);
+  static_for<0, 16>([&](auto mi) {
+    constexpr int m = decltype(mi)::value;
+    W[widx(m, jb, jc)] = u0[pos(16, m)];
+    W[widx(m, nb, nc)] = u1[pos(16, m)];
+  });
+}
+
+// stage A (packed) for one column j from its own values
+template <int PAR>
+__device__ __forceinline__ void pack_stage_a_col(float2* W, const float2* fh, const float2* ep, int j) {
+  using namespace gc;
+  const int jb = j >> 5, jc = j & 31;
+  const PackCol c0 = pack_col_consts(ep, jb, jc);
+  constexpr float sg = PAR ? -1.f : 1.f;
+  float2 u[16];
+  static_for<0, 16>([&](auto ki) {
+    constexpr int k = decltype(ki)::value;
+    const float2 lo = fh[k * N2 + j], hi = fh[(k + 16) * N2 + j];
+    const float tl = pack_t(ep[k], c0);
+    const float th = k == 0 ? c0.t16 : pack_t(ep[k + 16], c0);
+    u[k] = twiddle<PAR * k, 32, +1>(make_float2(lo.x * tl + sg * hi.x * th, lo.y * tl + sg * hi.y * th));
+  });
+  fft_line<16, +1>(u);
+  static_for<0, 16>([&](auto mi) {
+    constexpr int m = decltype(mi)::value;
+    W[widx(m, jb, jc)] = u[pos(16, m)];
+  });
+}
+
+// stage C (packed): X(k) = s(k) F(k) with F(k) = W^{PAR k} Z[k mod 16]
+template <int PAR, int PASS>
+__device__ __forceinline__ void pack_stage_c(const float2* W, int j, const float2* gp, const float* gsr,
+                                             uint32_t treg) {
+  using namespace gc;
+  const int jb = j >> 5, jc = j & 31;
+  uint32_t r[16];
+  tm_ld16(treg, r);  // chunk 0 of the accumulator, in flight during the transform
+  float2 z[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) z[m] = W[widx(m, jb, jc)];
+  fft_line<16, -1>(z);
+  float2 zw[16];
+  static_for<0, 16>([&](auto ki) {
+    constexpr int k = decltype(ki)::value;
+    zw[k] = twiddle<PAR * k, 32, -1>(z[pos(16, k)]);
+  });
+  const int kb = kval(jb, 32), kc = kval(jc, 32);
+  const float4* grow = reinterpret_cast<const float4*>(gsr + (kb * kb + kc * kc) * 20);
+  float g[20];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const float4 v = grow[i];
+    g[4 * i] = v.x;
+    g[4 * i + 1] = v.y;
+    g[4 * i + 2] = v.z;
+    g[4 * i + 3] = v.w;
+  }
+  // d = (g_bc + g~_bc) / 2; s(k_a) = g_a.x dp - g_a.y dm (k_a != 16), s16 at k_a = 16
+  const float2 gb = gp[32 + jb], gc2 = gp[64 + jc];
+  const float2 gbc = cmul(gb, gc2);
+  const float2 gbct = cmul(jb == 16 ? cconj(gb) : gb, jc == 16 ? cconj(gc2) : gc2);
+  const float2 d = make_float2(0.5f * (gbc.x + gbct.x), 0.5f * (gbc.y + gbct.y));
+  const float dp = d.x - d.y, dm = d.x + d.y;
+  float s16;
+  {
+    const float2 g16 = gp[16];
+    const float2 u = cmul(g16, gbc), v = cmul(cconj(g16), gbct);
+    s16 = 0.5f * ((u.x + v.x) - (u.y + v.y));
+  }
+  const float4* g4 = reinterpret_cast<const float4*>(gp);
+  static_for<0, 4>([&](auto ci) {
+    constexpr int c = decltype(ci)::value;
+    if constexpr (c > 0) tm_ld16(treg + 16 * c, r);
+    tm_wait_ld(r);
+    static_for<0, 8>([&](auto ii) {
+      constexpr int i = decltype(ii)::value;
+      constexpr int k = 8 * c + i;
+      constexpr int src = PASS == 0 ? k : ((32 - k) & 31);
+      constexpr int q = kval(src, 32) < 0 ? -kval(src, 32) : kval(src, 32);
+      float sv;
+      if constexpr (src == 16) {
+        sv = s16;
+      } else {
+        const float4 w4 = g4[src >> 1];
+        const float2 ga = (src & 1) ? make_float2(w4.z, w4.w) : make_float2(w4.x, w4.y);
+        sv = fmaf(-ga.y, dm, ga.x * dp);
+      }
+      const float cf = g[q] * sv;
+      const float2 F = src < 16 ? zw[src] : (PAR ? make_float2(-zw[src - 16].x, -zw[src - 16].y) : zw[src - 16]);
+      r[2 * i] = __float_as_uint(fmaf(cf, F.x, __uint_as_float(r[2 * i])));
+      r[2 * i + 1] = __float_as_uint(fmaf(PASS == 0 ? cf : -cf, F.y, __uint_as_float(r[2 * i + 1])));
+    });
+    tm_st16(treg + 16 * c, r);
+  });
+}
+
+template <bool PACK>
 __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a) {
   using namespace gpar;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -223,16 +349,16 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
   // the contiguous range [T b / G, T (b + 1) / G) of the T = 2 cells Q units,
   // split into segments of constant (cell, parity); segment (b, cp) writes
   // Hermitian slot set b + cp.
-  const int64_t total = a.cells * 2 * a.Q;
+  const int64_t total = a.cells * 2 * a.QP;
   const int64_t w0 = total * blockIdx.x / gridDim.x, w1 = total * (blockIdx.x + 1) / gridDim.x;
 
   for (int64_t w = w0; w < w1;) {
-    const int64_t cp = w / a.Q;
+    const int64_t cp = w / a.QP;
     const int par = int(cp & 1);
     const int64_t cell = cp >> 1;
-    const int p0 = int(w - cp * a.Q);
-    const int p1 = int(min(int64_t(a.Q), w1 - cp * a.Q));
-    w = cp * a.Q + p1;
+    const int p0 = int(w - cp * a.QP);
+    const int p1 = int(min(int64_t(a.QP), w1 - cp * a.QP));
+    w = cp * a.QP + p1;
     {
       uint32_t zr[16];
 #pragma unroll
@@ -255,7 +381,8 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       }
     }
 
-    for (int p = p0; p < p1; ++p) {
+    for (int ip = p0; ip < p1; ++ip) {
+      const int p = PACK ? a.reps[ip] : ip;
       // (per-pair pointers are formed inside each stage so that none stays
       // live across the register-heavy plane pass)
       // ---- A: the thread's two columns (those it also takes in stage C)
@@ -264,17 +391,31 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
         const float2* epp = a.epar + (int64_t(p) * 2 + par) * 32;
         const int4 uc = a.ucols[t];
         if (warp < 15) {  // column pairs {j, -j}: rows 1..15 and 31..17
-          if (par == 0)
-            par_stage_a_pair<0>(W, fh, ep, epp, uc.x);
-          else
-            par_stage_a_pair<1>(W, fh, ep, epp, uc.x);
+          if constexpr (PACK) {
+            if (par == 0)
+              pack_stage_a_pair<0>(W, fh, ep, uc.x);
+            else
+              pack_stage_a_pair<1>(W, fh, ep, uc.x);
+          } else {
+            if (par == 0)
+              par_stage_a_pair<0>(W, fh, ep, epp, uc.x);
+            else
+              par_stage_a_pair<1>(W, fh, ep, epp, uc.x);
+          }
         } else {  // rows 0 and 16 (with the self-conjugate columns): each column from its own values
 #pragma unroll 1
           for (int h = 0; h < 2; ++h) {
-            if (par == 0)
-              par_stage_a_col<0>(W, fh, ep, epp, h ? uc.y : uc.x);
-            else
-              par_stage_a_col<1>(W, fh, ep, epp, h ? uc.y : uc.x);
+            if constexpr (PACK) {
+              if (par == 0)
+                pack_stage_a_col<0>(W, fh, ep, h ? uc.y : uc.x);
+              else
+                pack_stage_a_col<1>(W, fh, ep, h ? uc.y : uc.x);
+            } else {
+              if (par == 0)
+                par_stage_a_col<0>(W, fh, ep, epp, h ? uc.y : uc.x);
+              else
+                par_stage_a_col<1>(W, fh, ep, epp, h ? uc.y : uc.x);
+            }
           }
         }
       }
@@ -289,18 +430,30 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
         const float* gsr = a.gsx + int64_t(p / a.ns) * (513 * 20);
         const int4 uc = a.ucols[t];
         tm_wait_st();
-        par_stage_c<0>(W, uc.x, gp, gpp, gsr, treg0);
-        par_stage_c<1>(W, uc.y, gp, gpp, gsr, treg0 + 64);
+        if constexpr (PACK) {
+          if (par == 0) {
+            pack_stage_c<0, 0>(W, uc.x, gp, gsr, treg0);
+            pack_stage_c<0, 1>(W, uc.y, gp, gsr, treg0 + 64);
+          } else {
+            pack_stage_c<1, 0>(W, uc.x, gp, gsr, treg0);
+            pack_stage_c<1, 1>(W, uc.y, gp, gsr, treg0 + 64);
+          }
+        } else {
+          par_stage_c<0>(W, uc.x, gp, gpp, gsr, treg0);
+          par_stage_c<1>(W, uc.y, gp, gpp, gsr, treg0 + 64);
+        }
       }
       __syncthreads();  // the next pair's stage A overwrites the planes
     }
-    // ---- write the work item's Hermitian slots (x 1/2).  Every thread of a
+    // ---- write the work item's Hermitian slots (x 1/2; packed: x 1, its
+    // coefficient is 2 s).  Every thread of a
     // warp issues the same TMEM loads (they are warp-collective); values are
     // parked in the thread's own entries S[k][t] of the (now free) plane buffer.
     tm_wait_st();
     const int4 uc = a.ucols[t];
     float2* out = a.hpart + (int64_t(blockIdx.x) + cp) * 32 * HSLOTS;
     float2* S = W;
+    constexpr float sc = PACK ? 1.f : 0.5f;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       uint32_t r[16];
@@ -315,7 +468,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
 #pragma unroll 4
       for (int k = 0; k < 32; ++k) {
         const float2 h = S[k * THREADS + t], g = S[((32 - k) & 31) * THREADS + t];
-        out[k * HSLOTS + uc.z + s] = make_float2(0.5f * (h.x + g.x), 0.5f * (h.y - g.y));
+        out[k * HSLOTS + uc.z + s] = make_float2(sc * (h.x + g.x), sc * (h.y - g.y));
       }
     };
     if (uc.w) self_conj(0);
@@ -331,7 +484,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
         const float2 v = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
         if (uc.w == 0) {  // column pair: H(j, k) = region0(k) + region1(k)
           const float2 h = S[k * THREADS + t];
-          out[k * HSLOTS + uc.z] = make_float2(0.5f * (h.x + v.x), 0.5f * (h.y + v.y));
+          out[k * HSLOTS + uc.z] = make_float2(sc * (h.x + v.x), sc * (h.y + v.y));
         } else {
           S[k * THREADS + t] = v;
         }
@@ -388,9 +541,10 @@ int gain_parity_prepare(pii_plan* p) {
     set_error("gain_parity_prepare: parity tables or column map missing");
     return PII_ERR_ARG;
   }
-  PII_CUDA(cudaFuncSetAttribute(k_gain_parity, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM)));
+  PII_CUDA(cudaFuncSetAttribute(k_gain_parity<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM)));
+  PII_CUDA(cudaFuncSetAttribute(k_gain_parity<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM)));
   int per_sm = 0, sms = 0;
-  PII_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gain_parity, THREADS, SMEM));
+  PII_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gain_parity<true>, THREADS, SMEM));
   PII_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
   if (per_sm != 1) {
     // every CTA takes all 512 TMEM columns: exactly one may be resident per SM
@@ -404,13 +558,51 @@ int gain_parity_prepare(pii_plan* p) {
   PII_CUDA(cudaMalloc(&p->gp_hpart, bytes));
   p->bytes += int64_t(bytes);
   p->gp_max_items = max_items;
+  // antipodal pairs of the design (the symmetric designs list every point and
+  // its negative): one representative per pair and radial node
+  const int ns = p->ns;
+  std::vector<int> mate(ns, -1);
+  bool sym = ns % 2 == 0;
+  for (int i = 0; i < ns && sym; ++i) {
+    for (int j = 0; j < ns; ++j) {
+      double d = 0;
+      for (int k = 0; k < 3; ++k) d = std::max(d, std::fabs(p->sigma[3 * i + k] + p->sigma[3 * j + k]));
+      if (d < 1e-12) {
+        mate[i] = j;
+        break;
+      }
+    }
+    sym = mate[i] >= 0 && mate[i] != i;
+  }
+  if (sym) {
+    std::vector<int> reps;
+    for (int ir = 0; ir < p->nr; ++ir)
+      for (int i = 0; i < ns; ++i)
+        if (i < mate[i]) reps.push_back(ir * ns + i);
+    if (int(reps.size()) * 2 == p->Q) {
+      PII_CUDA(cudaMalloc(&p->ap_reps, reps.size() * sizeof(int)));
+      PII_CUDA(cudaMemcpy(p->ap_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
+      p->bytes += int64_t(reps.size() * sizeof(int));
+      p->ap_count = int(reps.size());
+      // Nyquist-correction accumulators: cells x ceil(2 SMs / cells) <= 2 SMs + cells CTAs
+      const size_t nq = (size_t(2 * sms) + size_t(p->batch_max)) * 3 * N2 * sizeof(float2);
+      PII_CUDA(cudaMalloc(&p->nq_part, nq));
+      p->bytes += int64_t(nq);
+      PII_TRY(nyq_corr_prepare(p));
+    }
+  }
   return PII_OK;
 }
 
-int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s) {
+int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s, bool packed) {
   using namespace gpar;
-  // one CTA per SM, each with an equal share of the (cell, parity, pair) work
-  const int nct = int(std::min<int64_t>(p->gp_ctas, cells * 2 * p->Q));
+  if (packed && p->ap_count == 0) {
+    set_error("gain_parity_run: the packed kernel needs an antipodally symmetric design");
+    return PII_ERR_ARG;
+  }
+  const int QP = packed ? p->ap_count : p->Q;
+  // one CTA per SM, each with an equal share of the (cell, parity, pass) work
+  const int nct = int(std::min<int64_t>(p->gp_ctas, cells * 2 * QP));
   if (nct + 2 * cells > p->gp_max_items) {
     set_error("gain_parity_run: %lld cells beyond the plan's capacity", (long long)cells);
     return PII_ERR_SIZE;
@@ -425,19 +617,24 @@ int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.gsx = static_cast<const float*>(p->tab.gsx);
   a.ns = p->ns;
   a.Q = p->Q;
+  a.QP = QP;
+  a.reps = packed ? p->ap_reps : nullptr;
   a.cells = cells;
   a.hpart = static_cast<float2*>(p->gp_hpart);
   a.ucols = static_cast<const int4*>(p->gc_maps);
   {
     StageTimer st(p, ST_GAIN_PARITY, s);
-    k_gain_parity<<<unsigned(nct), THREADS, SMEM, s>>>(a);
+    if (packed)
+      k_gain_parity<true><<<unsigned(nct), THREADS, SMEM, s>>>(a);
+    else
+      k_gain_parity<false><<<unsigned(nct), THREADS, SMEM, s>>>(a);
   }
   PII_CHECK_LAUNCH();
   {
     StageTimer st(p, ST_REDUCE, s);
     k_herm_expand_par<<<unsigned((cells * N3 + 255) / 256), 256, 0, s>>>(
         static_cast<float2*>(p->G), a.hpart,
-        reinterpret_cast<const int2*>(static_cast<const char*>(p->gc_maps) + THREADS * sizeof(int4)), cells, p->Q,
+        reinterpret_cast<const int2*>(static_cast<const char*>(p->gc_maps) + THREADS * sizeof(int4)), cells, QP,
         nct);
   }
   PII_CHECK_LAUNCH();

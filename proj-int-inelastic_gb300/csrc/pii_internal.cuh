@@ -20,7 +20,7 @@ extern std::atomic<int64_t> g_launches;
 
 enum Stage {
   ST_FWD_PLANE = 0, ST_COL_FWD, ST_COL_PSTART, ST_PAIR_PLANE, ST_COL_PEND, ST_REDUCE,
-  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_GAIN_PARITY, ST_COUNT
+  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_GAIN_PARITY, ST_NYQ, ST_COUNT
 };
 
 #define PII_CUDA(call)                                                                    \
@@ -128,7 +128,8 @@ struct pii_plan {
   int* flag = nullptr;      // 16 device bytes: pii_state_check flag (0), pii_fast_sweep error word (8)
   double delta3 = 0;        // velocity cell volume of the last splitting step
   // gain kernel for n = 32, FP32: 0 = column/plane pipeline, 1 = fused
-  // 2-CTA-cluster kernel, 2 = fused a-parity kernel (tensor-memory accumulator)
+  // 2-CTA-cluster kernel, 2 = fused a-parity kernel (tensor-memory accumulator),
+  // 3 = a-parity kernel on antipodal pairs + Nyquist correction
   int gain_path = 0;
   // tunables (pii_plan_autotune): work items per resident cluster, and the
   // points per chunk of the pipeline path (cells per chunk = this / n^3)
@@ -141,6 +142,9 @@ struct pii_plan {
   int gp_ctas = 0;           // resident CTAs of the a-parity kernel
   int64_t gp_max_items = 0;
   void* gp_hpart = nullptr;  // its per-item Hermitian slots
+  int* ap_reps = nullptr;    // device: representative pair of each antipodal pair (0 if the design is not symmetric)
+  int ap_count = 0;
+  void* nq_part = nullptr;   // Nyquist-correction accumulators [<= 2 SMs + batch_max CTAs][3][1024]
   int64_t bytes = 0;
   std::map<pii::GraphKey, pii::GraphEntry> graphs;
   // per-stage CUDA-event profiling (pii_plan_profile)
@@ -177,7 +181,10 @@ int collide2d_f32(pii_plan* p, const double* f, double* q, int64_t cells, int wi
 int collide2d_f64(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb, cudaStream_t s);
 // gain_parity.cu
 int gain_parity_prepare(pii_plan* p);
-int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s);
+int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s, bool packed);
+// nyq_corr.cu
+int nyq_corr_prepare(pii_plan* p);
+int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // transport.cu
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
                    double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);

@@ -210,7 +210,7 @@ static void free_plan(pii_plan* p) {
   }
   void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
-                  p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->mom,       p->flag};
+                  p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -293,7 +293,7 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
       free_plan(p);
       return s2;
     }
-    p->gain_path = 2;
+    p->gain_path = p->ap_count > 0 ? 3 : 2;
   }
   *out = p;
   return PII_OK;

@@ -123,7 +123,7 @@ def test_full_size_properties_c2():
     assert float((q7[0] - q[7]).abs().max() / q[7].abs().max()) < 1e-6
 
 
-@pytest.mark.parametrize("path", ["cluster", "parity"])
+@pytest.mark.parametrize("path", ["cluster", "parity", "packed"])
 @pytest.mark.parametrize("cells", [1, 3, 128])
 def test_fused_kernel_matches_pipeline_and_fp64(cells, path):
     """n = 32 mixed precision: the fused gain kernels (2-CTA cluster, a-parity)
@@ -147,7 +147,7 @@ def test_fused_kernel_matches_pipeline_and_fp64(cells, path):
             assert rel_linf(qc[c].cpu().numpy(), qp[c].cpu().numpy()) < 1e-5, (wl, c)
 
 
-@pytest.mark.parametrize("path", ["cluster", "parity"])
+@pytest.mark.parametrize("path", ["cluster", "parity", "packed"])
 def test_fused_kernel_rough_input(path):
     """Uniform random f (spectrum up to the Nyquist planes, where exp_rs f^ is
     not Hermitian): fused kernels against the FP64 path, with and without loss,
@@ -172,7 +172,7 @@ def test_autotuner_keeps_results():
     sm = pkg.SpectralMesh(cfg)
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=8)
     best, choice = col.plan.autotune(8)
-    assert best > 0 and choice["gain_path"] in ("parity", "cluster", "pipeline")
+    assert best > 0 and choice["gain_path"] in ("packed", "parity", "cluster", "pipeline")
     assert choice["items_per_cluster"] in (2, 4, 6, 8)
     v = sm.v_center
     f = torch.as_tensor(np.stack([maxwellian(v, 1.0, (0.3 * c, 0, 0), 1.0) for c in range(8)]), device="cuda:0")
