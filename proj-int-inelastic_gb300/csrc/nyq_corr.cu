@@ -19,9 +19,9 @@
 //   R_c = (-1)^a sum_c (-1)^c P_a(b,c) f + (-1)^b sum_c (-1)^c P_b(a,c) f + P_c F_c,
 // with F_a = sum_a f etc.  A CTA owns one cell and a range of antipodal pairs,
 // two at a time: build f^ t- on the three sets, six 2D inverse transforms, the
-// reductions with f held in registers (three thread layouts: (b,c), (a,c),
-// (a,b) columns), six 2D forward transforms, then C(k) into a per-CTA
-// accumulator.  k_nyq_add sums the CTAs' accumulators into G.
+// reductions with f resident in shared memory (three thread layouts: (b,c),
+// (a,c), (a,b) columns), six 2D forward transforms, then C(k) into per-thread
+// accumulators.  k_nyq_add sums the CTAs' accumulators into G.
 #include <algorithm>
 
 #include "fft_reg.cuh"
@@ -30,12 +30,21 @@
 namespace pii {
 
 namespace nq {
-constexpr int NV = 32, N2 = 1024, N3 = 32768;
+constexpr int N2 = 1024, N3 = 32768;
 constexpr int THREADS = 512;
-constexpr int PB = 2;  // antipodal pairs per batch
-// shared memory: Fh[3][N2] + P[PB][3][N2] + R[PB][3][N2] + Acc[3][N2], all float2
-constexpr size_t SMEM = size_t(3 + 6 * PB + 3) * N2 * sizeof(float2);
-__device__ __forceinline__ int sw(int r, int c) { return r * 32 + (c ^ r); }  // swizzled plane element
+constexpr int PB = 2;        // antipodal pairs per batch
+constexpr int PL = 32 * 33;  // plane footprint: rows padded to 33 (row and column access conflict-free)
+// shared memory: f of the cell [a][b][c ^ b] (float), f^ on the three Nyquist
+// planes [3][N2] (float2), P[PB][3] planes (float2), the batch's phase / gain
+// rows [PB][2][96] and their row factors [PB][2][6 x 32] (float2); the
+// correction accumulator lives in registers (each thread owns the same points
+// in every batch)
+constexpr size_t OFF_P = size_t(N3) * sizeof(float) + size_t(3 * N2) * sizeof(float2);
+constexpr size_t SMEM = OFF_P + size_t(3 * PB) * PL * sizeof(float2) + size_t(PB) * 2 * 96 * sizeof(float2) +
+                        size_t(PB) * 2 * 6 * 32 * sizeof(float2);
+constexpr int PTS = 3 * N2 / THREADS;  // Nyquist points per thread
+__device__ __forceinline__ int sw(int r, int c) { return r * 33 + c; }
+__device__ __forceinline__ int fidx(int a, int b, int c) { return a * N2 + b * 32 + (c ^ b); }
 }  // namespace nq
 
 struct NyqArgs {
@@ -53,26 +62,58 @@ struct NyqArgs {
 
 __device__ __forceinline__ float2 nq_conj(float2 v) { return make_float2(v.x, -v.y); }
 
-// one warp transforms one swizzled 32 x 32 plane in place: rows then columns
-template <int DIR>
-__device__ __forceinline__ void plane_fft2(float2* P, int lane) {
-  using namespace nq;
+// 2D transform of padded 32 x 32 planes in place, two warps per plane: lane =
+// line, warp parity = parity of the outputs the warp produces (decimation in
+// frequency: even outputs are the 16-point transform of x_j + x_{j+16}, odd
+// ones of (x_j - x_{j+16}) w^j).  Every thread of the CTA calls it: its
+// barriers are unconditional; only warps with a plane compute.
+template <int DIR, int PAR>
+__device__ __forceinline__ void split_half(const float2* L, int stride, float2 (&y)[16]) {
   float2 x[32];
 #pragma unroll
-  for (int c = 0; c < 32; ++c) x[c] = P[sw(lane, c)];
-  fft_line<32, DIR>(x);
-  static_for<0, 32>([&](auto ci) {
-    constexpr int c = decltype(ci)::value;
-    P[sw(lane, c)] = x[pos(32, c)];
+  for (int j = 0; j < 32; ++j) x[j] = L[j * stride];
+  static_for<0, 16>([&](auto ji) {
+    constexpr int j = decltype(ji)::value;
+    y[j] = PAR == 0 ? cadd(x[j], x[j + 16]) : twiddle<j, 32, DIR>(csub(x[j], x[j + 16]));
   });
-  __syncwarp();
-#pragma unroll
-  for (int r = 0; r < 32; ++r) x[r] = P[sw(r, lane)];
-  fft_line<32, DIR>(x);
-  static_for<0, 32>([&](auto ri) {
-    constexpr int r = decltype(ri)::value;
-    P[sw(r, lane)] = x[pos(32, r)];
+  fft_line<16, DIR>(y);
+}
+
+template <int PAR>
+__device__ __forceinline__ void split_store(float2* L, int stride, const float2 (&y)[16]) {
+  static_for<0, 16>([&](auto mi) {
+    constexpr int m = decltype(mi)::value;
+    L[(2 * m + PAR) * stride] = y[pos(16, m)];
   });
+}
+
+template <int DIR>
+__device__ __forceinline__ void planes_fft2(float2* base, int nplanes, int warp, int lane) {
+  using namespace nq;
+  const int plane = warp >> 1, par = warp & 1;
+  const bool active = plane < nplanes;
+  float2* P = base + (active ? plane : 0) * PL;
+  float2 y[16];
+#pragma unroll 1
+  for (int pass = 0; pass < 2; ++pass) {
+    // pass 0: line = row `lane` (elements along the row); pass 1: column `lane`
+    float2* L = pass == 0 ? P + lane * 33 : P + lane;
+    const int stride = pass == 0 ? 1 : 33;
+    if (active) {
+      if (par == 0)
+        split_half<DIR, 0>(L, stride, y);
+      else
+        split_half<DIR, 1>(L, stride, y);
+    }
+    __syncthreads();  // both halves of every line have been read
+    if (active) {
+      if (par == 0)
+        split_store<0>(L, stride, y);
+      else
+        split_store<1>(L, stride, y);
+    }
+    __syncthreads();
+  }
 }
 
 // (E(k) - E~(k)) / 2 and (g(k) - g~(k)) / 2 for k = (ka, kb, kc): ~ conjugates
@@ -81,6 +122,43 @@ __device__ __forceinline__ float2 minus_part(const float2* rows, int ka, int kb,
   const float2 xa = rows[ka], xb = rows[32 + kb], xc = rows[64 + kc];
   const float2 p = cmul(cmul(xa, xb), xc);
   const float2 q = cmul(cmul(ka == 16 ? nq_conj(xa) : xa, kb == 16 ? nq_conj(xb) : xb), kc == 16 ? nq_conj(xc) : xc);
+  return make_float2(0.5f * (p.x - q.x), 0.5f * (p.y - q.y));
+}
+
+// Row factors of (X(k) - X~(k)) / 2 on the three planes for one table X (the
+// per-axis rows xa, xb, xc; ~ conjugates the factor of a Nyquist component):
+//   plane 0, k = (16, r, c): (A0[r] xc(c) - A1[r] xc~(c)) / 2, A0 = xa(16) xb(r), A1 = conj xa(16) xb~(r)
+//   plane 1, k = (r, 16, c): (B0[r] xc(c) - B1[r] xc~(c)) / 2, B0 = xa(r) xb(16), B1 = xa~(r) conj xb(16)
+//   plane 2, k = (r, c, 16): (xa(r) C0[c] - xa~(r) C1[c]) / 2, C0 = xb(c) xc(16), C1 = xb~(c) conj xc(16)
+// fac = [A0, A1, B0, B1, C0, C1] x 32
+__device__ __forceinline__ void row_factors(const float2* rows, float2* fac, int i) {
+  const int which = i >> 5, r = i & 31;
+  const float2* xa = rows;
+  const float2* xb = rows + 32;
+  const float2* xc = rows + 64;
+  auto tl = [](float2 v, int k) { return k == 16 ? nq_conj(v) : v; };
+  float2 v;
+  switch (which) {
+    case 0: v = cmul(xa[16], xb[r]); break;
+    case 1: v = cmul(nq_conj(xa[16]), tl(xb[r], r)); break;
+    case 2: v = cmul(xa[r], xb[16]); break;
+    case 3: v = cmul(tl(xa[r], r), nq_conj(xb[16])); break;
+    case 4: v = cmul(xb[r], xc[16]); break;
+    default: v = cmul(tl(xb[r], r), nq_conj(xc[16])); break;
+  }
+  fac[i] = v;
+}
+__device__ __forceinline__ float2 minus_from(const float2* rows, const float2* fac, int plane, int r, int c) {
+  float2 p, q;
+  if (plane == 2) {
+    const float2 x = rows[r];
+    p = cmul(x, fac[128 + c]);
+    q = cmul(r == 16 ? nq_conj(x) : x, fac[160 + c]);
+  } else {
+    const float2 x = rows[64 + c];
+    p = cmul(fac[64 * plane + r], x);
+    q = cmul(fac[64 * plane + 32 + r], c == 16 ? nq_conj(x) : x);
+  }
   return make_float2(0.5f * (p.x - q.x), 0.5f * (p.y - q.y));
 }
 
@@ -105,10 +183,11 @@ __device__ __forceinline__ bool nyq_point(int i, int& plane, int& r, int& c, int
 __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
   using namespace nq;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* Fh = reinterpret_cast<float2*>(smem_raw);  // [3][N2] f^ on the planes, swizzled
-  float2* P = Fh + 3 * N2;                           // [PB][3][N2]
-  float2* R = P + PB * 3 * N2;                       // [PB][3][N2]
-  float2* Acc = R + PB * 3 * N2;                     // [3][N2]
+  float* fS = reinterpret_cast<float*>(smem_raw);  // f(a, b, c) at fidx(a, b, c)
+  float2* Fh = reinterpret_cast<float2*>(fS + N3);  // [3][N2]: f^(16,r,c), f^(r,16,c), f^(r,c,16)
+  float2* P = reinterpret_cast<float2*>(smem_raw + OFF_P);  // [PB][3] planes: P, then R, then U
+  float2* Rows = P + PB * 3 * PL;                            // [PB][2][96]: phase rows, gain rows
+  float2* Fac = Rows + PB * 2 * 96;                          // [PB][2][6 x 32] row factors
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int64_t cell = blockIdx.x / a.blocks;
   const int blk = int(blockIdx.x - cell * a.blocks);
@@ -117,150 +196,142 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
   const float2* fh = a.fhat + cell * N3;
   const float* fr = a.fT + cell * N3;
 
+  for (int i = t; i < N3; i += THREADS) fS[fidx(i >> 10, (i >> 5) & 31, i & 31)] = fr[i];
   for (int i = t; i < 3 * N2; i += THREADS) {
     const int plane = i >> 10, r = (i >> 5) & 31, c = i & 31;
-    const int e = plane == 0 ? (16 * N2 + r * 32 + c) : plane == 1 ? (r * N2 + 16 * 32 + c) : (r * N2 + c * 32 + 16);
-    Fh[plane * N2 + sw(r, c)] = fh[e];
-    Acc[plane * N2 + sw(r, c)] = make_float2(0.f, 0.f);
+    Fh[i] = fh[plane == 0 ? (16 * N2 + r * 32 + c) : plane == 1 ? (r * N2 + 16 * 32 + c) : (r * N2 + c * 32 + 16)];
   }
+  float2 acc[PTS];
+#pragma unroll
+  for (int k = 0; k < PTS; ++k) acc[k] = make_float2(0.f, 0.f);
   __syncthreads();
 
   for (int ib = i0; ib < i1; ib += PB) {
     const int nb = min(PB, i1 - ib);
+    for (int i = t; i < PB * 2 * 96; i += THREADS) {
+      const int sidx = i / 192, w = (i / 96) & 1, e = i % 96;
+      Rows[i] = sidx < nb ? (w == 0 ? a.ephase : a.gphase)[int64_t(a.reps[ib + sidx]) * 96 + e] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int i = t; i < PB * 2 * 192; i += THREADS) row_factors(Rows + (i / 192) * 96, Fac + (i / 192) * 192, i % 192);
+    __syncthreads();
     // ---- 1. f^ t- on the three point sets (0 elsewhere on the planes)
-    for (int i = t; i < PB * 3 * N2; i += THREADS) {
+#pragma unroll 4
+    for (int it = 0; it < PB * 3 * N2 / THREADS; ++it) {  // fixed trip count: loads of several points in flight
+      const int i = t + it * THREADS;
       const int s = i / (3 * N2);
       const int ii = i - s * 3 * N2;
       int plane, r, c, ka, kb, kc;
       const bool on = nyq_point(ii, plane, r, c, ka, kb, kc) && s < nb;
       float2 y = make_float2(0.f, 0.f);
       if (on) {
-        const int p = a.reps[ib + s];
-        const float2 em = minus_part(a.ephase + int64_t(p) * 96, ka, kb, kc);
+        const float2 em = minus_from(Rows + s * 192, Fac + s * 384, plane, r, c);
         const float tm = em.x + em.y;
-        const float2 fv = Fh[plane * N2 + sw(r, c)];
+        const float2 fv = Fh[ii];
         y = make_float2(fv.x * tm, fv.y * tm);
       }
-      P[(s * 3 + plane) * N2 + sw(r, c)] = y;
+      P[(s * 3 + plane) * PL + sw(r, c)] = y;
     }
     __syncthreads();
-    // ---- 2. P = unnormalised 2D inverse transforms (one warp per plane)
-    if (warp < PB * 3) plane_fft2<+1>(P + warp * N2, lane);
-    __syncthreads();
-    // ---- 3. reductions R_a, R_b, R_c; thread layouts: rows w and w + 16, lane = column
-#pragma unroll 1
+    // ---- 2. P = unnormalised 2D inverse transforms (two warps per plane)
+    planes_fft2<+1>(P, 3 * nb, warp, lane);
+    // ---- 3. reductions R_a (lay 0), R_b (1), R_c (2) for both pairs of the
+    // batch; outputs (row w and w + 16, column lane) of the layout's plane;
+    // results stay in registers until every layout has read the P planes
+    float2 Rr[3][2][PB];
+#pragma unroll
     for (int lay = 0; lay < 3; ++lay) {
-      // f along the summed axis for the thread's two outputs
-      float f0[32], f1[32];
-      if (lay == 0) {  // outputs (b, c) = (w, lane), (w + 16, lane): f(., b, c)
+      const int o0 = warp, o1 = warp + 16;
+      float2 sh[2][PB], un[2][PB];
 #pragma unroll
-        for (int x = 0; x < 32; ++x) {
-          f0[x] = fr[x * N2 + warp * 32 + lane];
-          f1[x] = fr[x * N2 + (warp + 16) * 32 + lane];
-        }
-      } else if (lay == 1) {  // outputs (a, c): f(a, ., c)
-#pragma unroll
-        for (int x = 0; x < 32; ++x) {
-          f0[x] = fr[warp * N2 + x * 32 + lane];
-          f1[x] = fr[(warp + 16) * N2 + x * 32 + lane];
-        }
-      } else {  // outputs (a, b) = (w, lane), (w + 16, lane): f(a, b, .)
-        const float4* q0 = reinterpret_cast<const float4*>(fr + warp * N2 + lane * 32);
-        const float4* q1 = reinterpret_cast<const float4*>(fr + (warp + 16) * N2 + lane * 32);
-#pragma unroll
-        for (int x = 0; x < 8; ++x) {
-          const float4 v0 = q0[x], v1 = q1[x];
-          f0[4 * x] = v0.x, f0[4 * x + 1] = v0.y, f0[4 * x + 2] = v0.z, f0[4 * x + 3] = v0.w;
-          f1[4 * x] = v1.x, f1[4 * x + 1] = v1.y, f1[4 * x + 2] = v1.z, f1[4 * x + 3] = v1.w;
-        }
-      }
-      float F0 = 0.f, F1 = 0.f;
-#pragma unroll
+      for (int s = 0; s < PB; ++s) sh[0][s] = sh[1][s] = un[0][s] = un[1][s] = make_float2(0.f, 0.f);
+      float F0 = 0.f, F1 = 0.f;  // sums of f along the axis (the own-plane term)
+#pragma unroll 8
       for (int x = 0; x < 32; ++x) {
-        F0 += f0[x];
-        F1 += f1[x];
-      }
-      for (int s = 0; s < nb; ++s) {
-        const float2* Pa = P + (s * 3 + 0) * N2;
-        const float2* Pb = P + (s * 3 + 1) * N2;
-        const float2* Pc = P + (s * 3 + 2) * N2;
-        // "shared" plane value (same for both outputs) and the two "uniform" ones
-        float2 sh0 = make_float2(0.f, 0.f), sh1 = sh0, un0 = sh0, un1 = sh0;
+        // f along the summed axis for the two outputs, signed by (-1)^x
+        float g0, g1;
+        if (lay == 0) {  // outputs (b, c): f(x, b, c)
+          g0 = fS[fidx(x, o0, lane)], g1 = fS[fidx(x, o1, lane)];
+        } else if (lay == 1) {  // outputs (a, c): f(a, x, c)
+          g0 = fS[fidx(o0, x, lane)], g1 = fS[fidx(o1, x, lane)];
+        } else {  // outputs (a, b): f(a, b, x)
+          g0 = fS[fidx(o0, lane, x)], g1 = fS[fidx(o1, lane, x)];
+        }
+        F0 += g0, F1 += g1;
+        if (x & 1) g0 = -g0, g1 = -g1;
 #pragma unroll
-        for (int x = 0; x < 32; ++x) {
+        for (int s = 0; s < PB; ++s) {
+          const float2* Pa = P + (s * 3 + 0) * PL;
+          const float2* Pb = P + (s * 3 + 1) * PL;
+          const float2* Pc = P + (s * 3 + 2) * PL;
+          // "shared" plane value (both outputs) and the two "uniform" ones
           float2 ps, pu0, pu1;
           if (lay == 0) {  // sum over a: P_b(a, c) shared, P_c(a, b) uniform
-            ps = Pb[sw(x, lane)];
-            pu0 = Pc[sw(x, warp)];
-            pu1 = Pc[sw(x, warp + 16)];
+            ps = Pb[sw(x, lane)], pu0 = Pc[sw(x, o0)], pu1 = Pc[sw(x, o1)];
           } else if (lay == 1) {  // sum over b: P_a(b, c) shared, P_c(a, b) uniform
-            ps = Pa[sw(x, lane)];
-            pu0 = Pc[sw(warp, x)];
-            pu1 = Pc[sw(warp + 16, x)];
+            ps = Pa[sw(x, lane)], pu0 = Pc[sw(o0, x)], pu1 = Pc[sw(o1, x)];
           } else {  // sum over c: P_a(b, c) shared (b = lane), P_b(a, c) uniform
-            ps = Pa[sw(lane, x)];
-            pu0 = Pb[sw(warp, x)];
-            pu1 = Pb[sw(warp + 16, x)];
+            ps = Pa[sw(lane, x)], pu0 = Pb[sw(o0, x)], pu1 = Pb[sw(o1, x)];
           }
-          const float g0 = (x & 1) ? -f0[x] : f0[x], g1 = (x & 1) ? -f1[x] : f1[x];
-          sh0.x = fmaf(ps.x, g0, sh0.x), sh0.y = fmaf(ps.y, g0, sh0.y);
-          sh1.x = fmaf(ps.x, g1, sh1.x), sh1.y = fmaf(ps.y, g1, sh1.y);
-          un0.x = fmaf(pu0.x, g0, un0.x), un0.y = fmaf(pu0.y, g0, un0.y);
-          un1.x = fmaf(pu1.x, g1, un1.x), un1.y = fmaf(pu1.y, g1, un1.y);
+          sh[0][s].x = fmaf(ps.x, g0, sh[0][s].x), sh[0][s].y = fmaf(ps.y, g0, sh[0][s].y);
+          sh[1][s].x = fmaf(ps.x, g1, sh[1][s].x), sh[1][s].y = fmaf(ps.y, g1, sh[1][s].y);
+          un[0][s].x = fmaf(pu0.x, g0, un[0][s].x), un[0][s].y = fmaf(pu0.y, g0, un[0][s].y);
+          un[1][s].x = fmaf(pu1.x, g1, un[1][s].x), un[1][s].y = fmaf(pu1.y, g1, un[1][s].y);
         }
-        // combine with the own-plane term and the signs of the output indices
-        float2 r0, r1;
-        const int o0 = warp, o1 = warp + 16;  // first output index of each row
-        const float so0 = (o0 & 1) ? -1.f : 1.f, so1 = (o1 & 1) ? -1.f : 1.f;
-        const float sl = (lane & 1) ? -1.f : 1.f;
-        if (lay == 0) {  // R_a(b,c) = P_a F_a + (-1)^b sh + (-1)^c un
-          const float2 p0 = Pa[sw(o0, lane)], p1 = Pa[sw(o1, lane)];
-          r0 = make_float2(p0.x * F0 + so0 * sh0.x + sl * un0.x, p0.y * F0 + so0 * sh0.y + sl * un0.y);
-          r1 = make_float2(p1.x * F1 + so1 * sh1.x + sl * un1.x, p1.y * F1 + so1 * sh1.y + sl * un1.y);
-        } else if (lay == 1) {  // R_b(a,c) = (-1)^a sh + P_b F_b + (-1)^c un
-          const float2 p0 = Pb[sw(o0, lane)], p1 = Pb[sw(o1, lane)];
-          r0 = make_float2(so0 * sh0.x + p0.x * F0 + sl * un0.x, so0 * sh0.y + p0.y * F0 + sl * un0.y);
-          r1 = make_float2(so1 * sh1.x + p1.x * F1 + sl * un1.x, so1 * sh1.y + p1.y * F1 + sl * un1.y);
-        } else {  // R_c(a,b) = (-1)^a sh + (-1)^b un + P_c F_c
-          const float2 p0 = Pc[sw(o0, lane)], p1 = Pc[sw(o1, lane)];
-          r0 = make_float2(so0 * sh0.x + sl * un0.x + p0.x * F0, so0 * sh0.y + sl * un0.y + p0.y * F0);
-          r1 = make_float2(so1 * sh1.x + sl * un1.x + p1.x * F1, so1 * sh1.y + sl * un1.y + p1.y * F1);
-        }
-        R[(s * 3 + lay) * N2 + sw(o0, lane)] = r0;
-        R[(s * 3 + lay) * N2 + sw(o1, lane)] = r1;
+      }
+      // own-plane term and the signs of the output indices
+      const float so0 = (o0 & 1) ? -1.f : 1.f, so1 = (o1 & 1) ? -1.f : 1.f;
+      const float sl = (lane & 1) ? -1.f : 1.f;
+#pragma unroll
+      for (int s = 0; s < PB; ++s) {
+        const float2 p0 = P[(s * 3 + lay) * PL + sw(o0, lane)], p1 = P[(s * 3 + lay) * PL + sw(o1, lane)];
+        // R_a = P_a F_a + (-1)^b sh + (-1)^c un;  R_b = (-1)^a sh + P_b F_b + (-1)^c un;
+        // R_c = (-1)^a sh + (-1)^b un + P_c F_c  (sh / un as assigned above)
+        const float a0 = sl, b0 = so0, b1 = so1;
+        Rr[lay][0][s] = make_float2(p0.x * F0 + b0 * sh[0][s].x + a0 * un[0][s].x,
+                                    p0.y * F0 + b0 * sh[0][s].y + a0 * un[0][s].y);
+        Rr[lay][1][s] = make_float2(p1.x * F1 + b1 * sh[1][s].x + a0 * un[1][s].x,
+                                    p1.y * F1 + b1 * sh[1][s].y + a0 * un[1][s].y);
       }
     }
+    __syncthreads();  // every layout has read P
+#pragma unroll
+    for (int lay = 0; lay < 3; ++lay)
+#pragma unroll
+      for (int s = 0; s < PB; ++s) {
+        P[(s * 3 + lay) * PL + sw(warp, lane)] = Rr[lay][0][s];
+        P[(s * 3 + lay) * PL + sw(warp + 16, lane)] = Rr[lay][1][s];
+      }
     __syncthreads();
     // ---- 4. U = unnormalised 2D forward transforms of R
-    if (warp < PB * 3) plane_fft2<-1>(R + warp * N2, lane);
-    __syncthreads();
-    // ---- 5. C(k) = (w.x - w.y) U(k) - (w.x + w.y) conj U(-k), w = g-_p(k), into Acc
-    for (int i = t; i < 3 * N2; i += THREADS) {
+    planes_fft2<-1>(P, 3 * nb, warp, lane);
+    // ---- 5. C(k) = (w.x - w.y) U(k) - (w.x + w.y) conj U(-k), w = g-_p(k), accumulated
+#pragma unroll
+    for (int it = 0; it < PTS; ++it) {
+      const int i = t + it * THREADS;
       int plane, r, c, ka, kb, kc;
       if (!nyq_point(i, plane, r, c, ka, kb, kc)) continue;
       const int nr = (32 - r) & 31, nc = (32 - c) & 31;
       const int kk = kval(ka, 32) * kval(ka, 32) + kval(kb, 32) * kval(kb, 32) + kval(kc, 32) * kval(kc, 32);
-      float2 acc = Acc[plane * N2 + sw(r, c)];
-      for (int s = 0; s < nb; ++s) {
+#pragma unroll
+      for (int s = 0; s < PB; ++s) {
+        if (s >= nb) break;
         const int p = a.reps[ib + s];
         const float gsv = a.gsinc[int64_t(p / a.ns) * (a.M + 1) + kk];
-        const float2 gm = minus_part(a.gphase + int64_t(p) * 96, ka, kb, kc);
+        const float2 gm = minus_from(Rows + s * 192 + 96, Fac + s * 384 + 192, plane, r, c);
         const float wx = gsv * gm.x, wy = gsv * gm.y;
-        const float2 u = R[(s * 3 + plane) * N2 + sw(r, c)];
-        const float2 um = R[(s * 3 + plane) * N2 + sw(nr, nc)];
+        const float2 u = P[(s * 3 + plane) * PL + sw(r, c)];
+        const float2 um = P[(s * 3 + plane) * PL + sw(nr, nc)];
         const float cp = wx - wy, cm = wx + wy;
-        acc.x += cp * u.x - cm * um.x;
-        acc.y += cp * u.y + cm * um.y;
+        acc[it].x += cp * u.x - cm * um.x;
+        acc[it].y += cp * u.y + cm * um.y;
       }
-      Acc[plane * N2 + sw(r, c)] = acc;
     }
     __syncthreads();
   }
   float2* out = a.part + (cell * a.blocks + blk) * 3 * N2;
-  for (int i = t; i < 3 * N2; i += THREADS) {
-    const int plane = i >> 10, r = (i >> 5) & 31, c = i & 31;
-    out[i] = Acc[plane * N2 + sw(r, c)];
-  }
+#pragma unroll
+  for (int it = 0; it < PTS; ++it) out[t + it * THREADS] = acc[it];
 }
 
 // G[cell][k] += sum over the cell's CTAs of the correction at the Nyquist points
@@ -307,8 +378,8 @@ int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.cells = cells;
   int sms = 0;
   PII_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
-  a.blocks = int(std::max<int64_t>(1, std::min<int64_t>(16, (2 * int64_t(sms) + cells - 1) / cells)));
-  a.blocks = std::min(a.blocks, std::max(1, a.QP / PB));
+  // about 8 waves of CTAs (one per SM), at least one batch each
+  a.blocks = int(std::max<int64_t>(1, std::min<int64_t>(std::max(1, a.QP / PB), (8 * int64_t(sms) + cells - 1) / cells)));
   a.part = static_cast<float2*>(p->nq_part);
   {
     StageTimer st(p, ST_NYQ, s);
