@@ -471,6 +471,9 @@ def main():
     for v in stages.values():
         v["share"] = v["ms"] / tot if tot else None
     dom = max(stages, key=lambda k: stages[k]["ms"])
+    # the packed gain path is two kernels (the a-parity pass over antipodal
+    # pairs and its Nyquist correction): the gain term's time is their sum
+    gain_ms = stages[dom]["ms"] + (stages["nyq_corr"]["ms"] if dom == "gain_parity" and "nyq_corr" in stages else 0.0)
     # algorithmic FLOPs: one 1D pass over a grid = 5 N log2(n); items = (cell, pair)
     N = NV**3
     items_per_collide = NX * NR * NS
@@ -495,9 +498,13 @@ def main():
             "launches_per_step": stages[dom]["launches"], "avg_launch_ms": stages[dom]["ms"] / stages[dom]["launches"]}
     if flops_total:
         per_launch = flops_total / stages[dom]["launches"]
-        roof["achieved"] = per_launch / (roof["avg_launch_ms"] / 1e3) / 1e12
+        roof["achieved"] = per_launch / (gain_ms / stages[dom]["launches"] / 1e3) / 1e12
         roof["frac"] = roof["achieved"] / fp32_peak
         roof["algorithmic_flops_per_launch"] = per_launch
+        if gain_ms != stages[dom]["ms"]:
+            roof["timed_kernels"] = "gain_parity + nyq_corr (the gain term)"
+            roof["note"] = ("algorithmic FLOPs of the direct method (2 * 5 N log2 N + 16 N per (cell, pair)); the "
+                            "packed path evaluates antipodal pairs together and performs about half of them")
     else:
         roof["achieved"] = roof["frac"] = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
