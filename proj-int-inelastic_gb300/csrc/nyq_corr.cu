@@ -378,8 +378,9 @@ int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.cells = cells;
   int sms = 0;
   PII_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
-  // about 8 waves of CTAs (one per SM), at least one batch each
-  a.blocks = int(std::max<int64_t>(1, std::min<int64_t>(std::max(1, a.QP / PB), (8 * int64_t(sms) + cells - 1) / cells)));
+  // about 8 waves of CTAs (one per SM), each with at least 16 antipodal pairs
+  // so that loading the cell's f into shared memory stays a small share
+  a.blocks = int(std::max<int64_t>(1, std::min<int64_t>(std::max(1, a.QP / 16), (8 * int64_t(sms) + cells - 1) / cells)));
   a.part = static_cast<float2*>(p->nq_part);
   {
     StageTimer st(p, ST_NYQ, s);
