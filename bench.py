@@ -511,9 +511,10 @@ def main():
     roof["traffic"] = None
     if os.path.exists(tfile):
         tr = json.load(open(tfile))
-        if dom in tr:
-            roof["traffic"] = tr[dom].get("dram_bytes_per_launch")
-            roof["traffic_source"] = tr[dom].get("source")
+        tkey = "gain_packed" if gain_ms != stages[dom]["ms"] else dom  # packed: both kernels of the gain term
+        if tkey in tr:
+            roof["traffic"] = tr[tkey].get("dram_bytes_per_launch")
+            roof["traffic_source"] = tr[tkey].get("source")
     # whole-step FLOP rate (algorithmic F per cell-eval, survey formula) for context
     F_cell = (2 * NR * NS + NR + 2) * 5 * N * math.log2(N) + 16 * NR * NS * N
     roof["step_algorithmic_tflops"] = F_cell * value / world / 1e12
