@@ -110,13 +110,26 @@ int pii_plan_set_gain_path(pii_plan* plan, int path);
  * Autotuner (no reference counterpart): times, for `cells` cells, every
  * candidate of the plan's kernel choices -- gain path (a-parity / cluster /
  * pipeline), work items per resident cluster or CTA (2, 4, 6, 8), pipeline
- * chunk size (64K to
- * 512K velocity points) -- on scratch inputs it allocates and frees itself,
+ * chunk size (64K to 512K velocity points), column-transform path (n = 64
+ * FP32: CUDA-core FFT or tensor-core DFT) -- on scratch inputs it allocates and frees itself,
  * keeps the fastest and drops captured step graphs.  best_ms (may be NULL)
  * receives the best time of one Q evaluation.  Synchronises the stream.
  * pii_plan_get_tuning reads the current choices.
  */
 int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stream);
+
+/*
+ * First-axis column transforms of the n = 64 FP32 pipeline (no reference
+ * counterpart; the reference calls FFTW / cuFFT for the whole 3D transform,
+ * src/collision/inelastic_collisions.py:212-214): 0 = in-register CUDA-core
+ * FFT, 1 = dense 64-point DFT on the tensor cores (tcgen05.mma, split-BF16
+ * operands hi + lo, FP32 accumulation in tensor memory).  Path 1 exists for
+ * n = 64, FP32, 3D plans only; the autotuner times both.  get: `stalled`
+ * (may be NULL) receives 1 if a tensor-core CTA ever gave up waiting for its
+ * MMAs (results of that call are incomplete); reading it synchronises.
+ */
+int pii_plan_set_dft_path(pii_plan* plan, int path);
+int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stalled);
 int pii_plan_get_tuning(const pii_plan* plan, int* gain_path, int* items_per_cluster, int64_t* chunk_points);
 /* Restores choices read by pii_plan_get_tuning (e.g. saved from an earlier
  * autotune); drops captured step graphs.  items_per_cluster in [1, 64]. */

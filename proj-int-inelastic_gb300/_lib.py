@@ -47,6 +47,8 @@ SIGNATURES = {
     "pii_plan_autotune": (_c_int, [_vp, _c_i64, _pdbl, _vp]),
     "pii_plan_get_tuning": (_c_int, [_vp, _pint, _pint, ctypes.POINTER(ctypes.c_int64)]),
     "pii_plan_set_tuning": (_c_int, [_vp, _c_int, _c_int, _c_i64]),
+    "pii_plan_set_dft_path": (_c_int, [_vp, _c_int]),
+    "pii_plan_get_dft_path": (_c_int, [_vp, _pint, _pint]),
     "pii_collide": (_c_int, [_vp, _vp, _vp, _c_i64, _c_int, _c_dbl, _c_int, _vp]),
     "pii_transport_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _vp]),
     "pii_boltzmann_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _c_dbl, _c_int,

@@ -161,6 +161,8 @@ def _precision_of(config, precision):
 
 
 GAIN_PATHS = {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3}
+# first-axis column transforms of the n = 64 FP32 pipeline
+DFT_PATHS = {"fft": 0, "tensor": 1}
 
 
 class Plan:
@@ -198,18 +200,37 @@ class Plan:
                                                torch.cuda.current_stream().cuda_stream), "pii_plan_autotune")
         return best.value, self.tuning
 
-    def set_tuning(self, gain_path, items_per_cluster, chunk_points, **_):
-        """Restore choices (as returned by :attr:`tuning`), ``pii_plan_set_tuning``."""
+    def set_tuning(self, gain_path, items_per_cluster, chunk_points, dft_path=None, **_):
+        """Restore choices (as returned by :attr:`tuning`), ``pii_plan_set_tuning``
+        (and ``pii_plan_set_dft_path`` when `dft_path` is given)."""
         _lib.check(self._lib.pii_plan_set_tuning(self.handle, GAIN_PATHS[gain_path], int(items_per_cluster),
                                                  int(chunk_points)), "pii_plan_set_tuning")
+        if dft_path is not None:
+            self.set_dft_path(dft_path)
+
+    def set_dft_path(self, dft_path):
+        """'fft' (CUDA-core FFT) or 'tensor' (tensor-core split-BF16 DFT; n = 64
+        FP32 plans) for the first-axis column transforms, ``pii_plan_set_dft_path``."""
+        _lib.check(self._lib.pii_plan_set_dft_path(self.handle, DFT_PATHS[dft_path]), "pii_plan_set_dft_path")
+
+    @property
+    def dft_stalled(self):
+        """True if a tensor-core DFT CTA ever gave up waiting for its MMAs
+        (``pii_plan_get_dft_path``; synchronises)."""
+        path, stalled = _lib.ctypes.c_int(), _lib.ctypes.c_int()
+        _lib.check(self._lib.pii_plan_get_dft_path(self.handle, _lib.ctypes.byref(path), _lib.ctypes.byref(stalled)),
+                   "pii_plan_get_dft_path")
+        return bool(stalled.value)
 
     @property
     def tuning(self):
         path, items, pts = _lib.ctypes.c_int(), _lib.ctypes.c_int(), _lib.ctypes.c_int64()
         _lib.check(self._lib.pii_plan_get_tuning(self.handle, _lib.ctypes.byref(path), _lib.ctypes.byref(items),
                                                  _lib.ctypes.byref(pts)), "pii_plan_get_tuning")
+        dft = _lib.ctypes.c_int()
+        _lib.check(self._lib.pii_plan_get_dft_path(self.handle, _lib.ctypes.byref(dft), None), "pii_plan_get_dft_path")
         return {"gain_path": {v: k for k, v in GAIN_PATHS.items()}[path.value], "items_per_cluster": items.value,
-                "chunk_points": pts.value}
+                "chunk_points": pts.value, "dft_path": {v: k for k, v in DFT_PATHS.items()}[dft.value]}
 
     @property
     def workspace_bytes(self):

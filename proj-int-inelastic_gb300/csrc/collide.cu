@@ -134,26 +134,30 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
   struct Cand {
     int path, items;
     int64_t points;
+    int dft;
   };
   std::vector<Cand> cands;
   const bool cluster_ok = plan->gc_clusters > 0;
   if (cluster_ok) {
-    for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points});
-    cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points});  // even split: no item knob
-    if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points});
+    for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points, 0});
+    cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points, 0});  // even split: no item knob
+    if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points, 0});
   }
-  for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
-    cands.push_back({0, plan->gc_items_per_cluster, pts});
+  for (int dft = 0; dft <= (plan->dft_img ? 1 : 0); ++dft)
+    for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
+      cands.push_back({0, plan->gc_items_per_cluster, pts, dft});
   const int saved_path = plan->gain_path;
   const int saved_items = plan->gc_items_per_cluster;
   const int64_t saved_points = plan->chunk_points;
+  const int saved_dft = plan->dft_path;
   float best = 1e30f;
-  Cand pick{saved_path, saved_items, saved_points};
+  Cand pick{saved_path, saved_items, saved_points, saved_dft};
   int st = PII_OK;
   for (const Cand& c : cands) {
     plan->gain_path = c.path;
     plan->gc_items_per_cluster = c.items;
     plan->chunk_points = c.points;
+    plan->dft_path = c.dft;
     st = collide_impl(plan, f, q, cells, 1, 0.0, 0, s);  // warm-up
     if (st != PII_OK) break;
     cudaEventRecord(e0, s);
@@ -179,6 +183,7 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
   plan->gain_path = st == PII_OK ? pick.path : saved_path;
   plan->gc_items_per_cluster = st == PII_OK ? pick.items : saved_items;
   plan->chunk_points = st == PII_OK ? pick.points : saved_points;
+  plan->dft_path = st == PII_OK ? pick.dft : saved_dft;
   for (auto& kv : plan->graphs) {  // captured graphs baked the old choices in
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
@@ -231,6 +236,40 @@ extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
     return PII_ERR_ARG;
   }
   plan->gain_path = path;
+  return PII_OK;
+}
+
+extern "C" int pii_plan_set_dft_path(pii_plan* plan, int path) {
+  if (!plan || path < 0 || path > 1) {
+    pii::set_error("pii_plan_set_dft_path: path must be 0 (CUDA-core FFT) or 1 (tensor-core split-BF16 DFT)");
+    return PII_ERR_ARG;
+  }
+  if (path == 1 && !plan->dft_img) {
+    pii::set_error("pii_plan_set_dft_path: the tensor-core DFT exists for n = 64, FP32, 3D plans only");
+    return PII_ERR_ARG;
+  }
+  plan->dft_path = path;
+  for (auto& kv : plan->graphs) {  // captured graphs baked the old choice in
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+  }
+  plan->graphs.clear();
+  return PII_OK;
+}
+
+extern "C" int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stalled) {
+  if (!plan || !path) {
+    pii::set_error("pii_plan_get_dft_path: NULL argument");
+    return PII_ERR_ARG;
+  }
+  *path = plan->dft_path;
+  if (stalled) {
+    *stalled = 0;
+    if (plan->dft_err) {
+      PII_CUDA(cudaSetDevice(plan->device));
+      PII_CUDA(cudaMemcpy(stalled, plan->dft_err, sizeof(int), cudaMemcpyDeviceToHost));
+    }
+  }
   return PII_OK;
 }
 

@@ -21,6 +21,7 @@
 // with q = Re(Y1) - f Re(Y2)              (k_col<IPREP> + k_finish).
 // Intermediates of a chunk of items live in one buffer sized to stay L2-resident.
 #pragma once
+#include <type_traits>
 #include "fft_reg.cuh"
 #include "pii_internal.cuh"
 
@@ -34,8 +35,6 @@ struct Geo {
   static constexpr int THREADS = PPB * NV;
   static constexpr int LD = NV + 1;  // padded row stride (complex elements)
 };
-
-enum ColMode { COL_FWD = 0, COL_PSTART = 1, COL_PEND = 2, COL_IPREP = 3 };
 
 struct ColArgs {
   const void* src;     // input grid(s)
@@ -417,11 +416,15 @@ int CollideKernels<T, NV>::pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t
   a.p0 = p0;
   a.np = np;
   const unsigned colblocks = unsigned((items * N2 + 127) / 128);
-  {
+  bool tc = false;
+  if constexpr (std::is_same<T, float>::value && NV == 64) tc = p->dft_path == 1;
+  if (tc) {
+    PII_TRY(col_tc_run(p, COL_PSTART, items, c0, p0, np, s));
+  } else {
     StageTimer st(p, ST_COL_PSTART, s);
     k_col<T, NV, COL_PSTART><<<colblocks, 128, 0, s>>>(a);
+    PII_CHECK_LAUNCH();
   }
-  PII_CHECK_LAUNCH();
   const int64_t nplanes = items * NV;
   {
     StageTimer st(p, ST_PAIR_PLANE, s);
@@ -429,11 +432,13 @@ int CollideKernels<T, NV>::pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t
         reinterpret_cast<V*>(p->buf), reinterpret_cast<const T*>(p->fT), c0, np, nplanes);
   }
   PII_CHECK_LAUNCH();
-  {
+  if (tc) {
+    PII_TRY(col_tc_run(p, COL_PEND, items, c0, p0, np, s));
+  } else {
     StageTimer st(p, ST_COL_PEND, s);
     k_col<T, NV, COL_PEND><<<colblocks, 128, 0, s>>>(a);
+    PII_CHECK_LAUNCH();
   }
-  PII_CHECK_LAUNCH();
   {
     StageTimer st(p, ST_REDUCE, s);
     k_reduce<T><<<unsigned((cells * N3 + 255) / 256), 256, 0, s>>>(

@@ -18,6 +18,9 @@ void set_error(const char* fmt, ...);
 // kernels enqueued by the library (eager launches + kernel nodes of graph replays)
 extern std::atomic<int64_t> g_launches;
 
+// modes of the first-axis column pass (collide_kernels.cuh, col_tc.cu)
+enum ColMode { COL_FWD = 0, COL_PSTART = 1, COL_PEND = 2, COL_IPREP = 3 };
+
 enum Stage {
   ST_FWD_PLANE = 0, ST_COL_FWD, ST_COL_PSTART, ST_PAIR_PLANE, ST_COL_PEND, ST_REDUCE,
   ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_GAIN_PARITY, ST_NYQ, ST_COUNT
@@ -145,6 +148,15 @@ struct pii_plan {
   int* ap_reps = nullptr;    // device: representative pair of each antipodal pair (0 if the design is not symmetric)
   int ap_count = 0;
   void* nq_part = nullptr;   // Nyquist-correction accumulators [<= 2 SMs + batch_max CTAs][3][1024]
+  // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core
+  // FFT (k_col), 1 = tensor-core split-BF16 DFT (k_col_tc)
+  int dft_path = 0;
+  void* dft_img = nullptr;  // DFT matrix images (A_hi | A_lo) for DIR = +1 and -1
+  int* dft_err = nullptr;   // device word: 1 if a k_col_tc CTA gave up waiting for its MMAs
+  int dft_ctas = 0;         // resident CTAs of k_col_tc (one per SM)
+  // TMA tensor maps (CUtensorMap, 128 bytes each) of f^ and of the chunk buffer
+  // as 2D FP32 arrays [rows of 64 (a) per grid][8192 floats per row]
+  alignas(128) unsigned char dft_tmap[2][128] = {};
   int64_t bytes = 0;
   std::map<pii::GraphKey, pii::GraphEntry> graphs;
   // per-stage CUDA-event profiling (pii_plan_profile)
@@ -185,6 +197,9 @@ int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s, bool packed);
 // nyq_corr.cu
 int nyq_corr_prepare(pii_plan* p);
 int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s);
+// col_tc.cu: tensor-core first-axis DFT of the n = 64 FP32 pipeline
+int col_tc_prepare(pii_plan* p);
+int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int64_t np, cudaStream_t s);
 // transport.cu
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
                    double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);

@@ -210,7 +210,8 @@ static void free_plan(pii_plan* p) {
   }
   void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
-                  p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag};
+                  p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag,
+                  p->dft_img,    p->dft_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -294,6 +295,10 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
       return s2;
     }
     p->gain_path = p->ap_count > 0 ? 3 : 2;
+  }
+  if (n == 64 && precision == PII_PREC_FP32 && dim == 3 && (s2 = col_tc_prepare(p)) != PII_OK) {
+    free_plan(p);
+    return s2;
   }
   *out = p;
   return PII_OK;

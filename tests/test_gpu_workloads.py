@@ -123,3 +123,47 @@ def test_large_grid_n64_full_quadrature():
     qd = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=2).collide(f, with_loss=True)
     for c in range(2):
         assert rel_linf(qm[c].cpu().numpy(), qd[c].cpu().numpy()) < 1e-5, c
+
+
+def test_large_grid_n64_tensor_core_dft():
+    """The first-axis column transforms of the n = 64 pipeline on the tensor
+    cores (split-BF16 DFT, FP32 accumulation) against the FP64 path, next to
+    the CUDA-core FFT path; the full 48 x 70 quadrature on two cells."""
+    pkg = _pkg()
+    s = 20.0 / (3.0 + math.sqrt(2.0))  # L = 10
+    cfg = op_config(64, s, 48, 70, 0.7, 0.7, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    rng = np.random.default_rng(11)
+    f = np.stack([_mixture(sm.v_center, rng, 3, 3.0, (0.5, 3.0)) for _ in range(2)])
+    f = torch.as_tensor(f, device="cuda:0")
+    qd = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=2).collide(f, with_loss=True)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=2)
+    col.plan.set_dft_path("fft")
+    qf = col.collide(f, with_loss=True)
+    col.plan.set_dft_path("tensor")
+    assert col.plan.tuning["dft_path"] == "tensor"
+    qt = col.collide(f, with_loss=True)
+    assert not col.plan.dft_stalled
+    for c in range(2):
+        et = rel_linf(qt[c].cpu().numpy(), qd[c].cpu().numpy())
+        ef = rel_linf(qf[c].cpu().numpy(), qd[c].cpu().numpy())
+        print(f"n=64 cell {c}: rel Linf vs FP64: tensor-core DFT {et:.3e}, CUDA-core FFT {ef:.3e}")
+        assert et < 1e-5, c
+    # mass defect of Q relative to the mass of f: no worse than the FFT path's
+    dv = sm.delta**3
+    mass = f.sum(dim=(1, 2, 3)) * dv
+    mt = float((qt.sum(dim=(1, 2, 3)) * dv / mass).abs().max())
+    mf = float((qf.sum(dim=(1, 2, 3)) * dv / mass).abs().max())
+    print(f"n=64 mass defect: tensor-core {mt:.3e}, CUDA-core {mf:.3e}")
+    assert mt < max(1e-6, 2 * mf)
+
+
+def test_tensor_core_dft_path_rules():
+    """The tensor-core DFT exists for n = 64 FP32 3D plans only; other plans
+    refuse it with ValueError."""
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 8, 12, 0.9, 0.9, 1.0)
+    col = pkg.FSInelasticVHSCollision(cfg, pkg.SpectralMesh(cfg), precision="mixed", batch_max=1)
+    with pytest.raises(ValueError):
+        col.plan.set_dft_path("tensor")
+    assert col.plan.tuning["dft_path"] == "fft"
