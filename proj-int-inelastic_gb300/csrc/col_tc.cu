@@ -28,7 +28,8 @@
 //   warps 8-15  epilogue: tcgen05.ld of the accumulator (lane = column n,
 //               TMEM column = output o: whole complex outputs per thread),
 //               arrive on tempty, store Y[k][j] coalesced along j (PEND: times
-//               the pair's gain, :213-214, from rows staged in shared memory).
+//               the pair's gain, :213-214, from its radial sinc row and phase
+//               rows, bulk-copied by the TMA thread into gain buffer i % 2).
 // Tensor memory: X buffers at columns [0, 256), accumulators at [256, 512).
 // The F image (F_hi | F_lo, 64 KB, laid out on the host) is bulk-copied once
 // per CTA.  Every mbarrier wait is bounded; a role that gives up raises a
@@ -63,10 +64,11 @@ constexpr int OFF_F = 0;                    // F_hi, F_lo
 constexpr int OFF_R = 2 * OPB;              // raw tiles 0, 1, then the two phase rows
 constexpr int OFF_P = OFF_R + 2 * RAW;
 constexpr int GS_MAX = 3 * 32 * 32 + 1;     // gsinc row: |k|^2 <= 3 (n / 2)^2
-constexpr int GROW = GS_MAX + 1 + 2 * 3 * NV;  // one pair's gain rows: gsinc row, then the 3 x 64 phases (floats)
+constexpr int GS_PAD = (GS_MAX + 3) / 4 * 4;   // row pitch of the padded copy (16-byte rows)
+constexpr int GROW = GS_PAD + 2 * 3 * NV;   // one pair's gain rows: gsinc row, then the 3 x 64 phases (floats)
 constexpr int OFF_G = OFF_P + 2 * PROW;     // gain rows of the epilogue's two accumulators
 constexpr int OFF_BAR = OFF_G + 2 * GROW * 4;
-constexpr int NBAR = 13;                    // rfull[2] rempty[2] xfull[2] xempty[2] tfull[2] tempty[2] fbar
+constexpr int NBAR = 17;  // rfull[2] rempty[2] xfull[2] xempty[2] tfull[2] tempty[2] fbar gfull[2] gempty[2]
 constexpr int SMEM = OFF_BAR + NBAR * 8 + 16;
 constexpr uint32_t TMEM_COLS = 512;         // X buffers [0, 256), accumulators [256, 512)
 constexpr uint32_t WAIT_LIMIT = 1u << 22;   // mbarrier polls before a role gives up
@@ -79,8 +81,8 @@ struct ColTcArgs {
   const uint4* fimg;    // DFT matrix image of the direction (F_hi | F_lo)
   const float2* ephase;  // [Q][3][64]
   const float2* gphase;  // [Q][3][64]
-  const float* gsinc;    // [n_r][M + 1]
-  int M1, ns;
+  const float* gsinc;    // [n_r][GS_PAD]: the radial sinc rows, padded to 16-byte rows
+  int ns;
   int64_t items, c0, p0, np;
   int* err;             // set to 1 if a role gave up waiting
 };
@@ -97,21 +99,6 @@ __device__ __forceinline__ bool mbar_wait_role(uint64_t* mbar, uint32_t parity, 
   return false;
 }
 
-// true in every thread of the named barrier `ID` (COUNT threads) if `pred` holds in any of them
-template <int ID, int COUNT>
-__device__ __forceinline__ bool bar_any(bool pred) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.or.pred q, %2, %3, p;\n\t"
-      "selp.u32 %0, 1, 0, q;\n\t}\n"
-      : "=r"(r)
-      : "r"(uint32_t(pred)), "n"(ID), "n"(COUNT)
-      : "memory");
-  return r != 0;
-}
-
 template <int MODE>
 __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constant__ CUtensorMap tmap, ColTcArgs a) {
   using namespace ctc;
@@ -124,6 +111,8 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
   uint64_t* tfull = bars + 8;
   uint64_t* tempty = bars + 10;
   uint64_t* fbar = bars + 12;
+  uint64_t* gfull = bars + 13;
+  uint64_t* gempty = bars + 15;
   volatile int* abort = reinterpret_cast<volatile int*>(bars + NBAR);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + NBAR) + 1;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -140,6 +129,8 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       mbar_init(xempty + b, 1);
       mbar_init(tfull + b, 1);
       mbar_init(tempty + b, EPILOGUE);
+      mbar_init(gfull + b, 1);
+      mbar_init(gempty + b, EPILOGUE);
     }
     mbar_init(fbar, 1);
     *abort = 0;
@@ -205,7 +196,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
     // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) + lane (column n) and
     // accumulator columns [64 h', 64 h' + 64) (outputs k = 32 h' .. 32 h' + 31)
     const int ew = warp - CONVERTERS / 32, qd = ew & 3, hh = ew >> 2;
-    const int n = 32 * qd + lane, te = t - CONVERTERS;
+    const int n = 32 * qd + lane;
     int i = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int d = i & 1;
@@ -213,22 +204,12 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       const int j = int(tile - item * TILES_PER_ITEM) * TN + n;
       float2* out = a.dst + item * N3 + j;
       // PEND: gain(k, j) = g_a[k] g_b[jb] g_c[jc] * gsinc[r][k_b^2 + k_c^2 + k_a^2], from
-      // the pair's rows staged in shared memory (L1 is mostly carved out for the operands)
-      float* gsS = reinterpret_cast<float*>(sm + OFF_G) + d * GROW;
-      const float2* gpS = reinterpret_cast<const float2*>(gsS + GS_MAX + 1);
-      if constexpr (MODE == COL_PEND) {
-        const int64_t ci = item / a.np;
-        const int64_t pair = a.p0 + (item - ci * a.np);
-        const float* gs = a.gsinc + int64_t(pair / a.ns) * a.M1;
-        const float* gp = reinterpret_cast<const float*>(a.gphase + pair * 3 * NV);
-        for (int e = te; e < a.M1; e += EPILOGUE) gsS[e] = gs[e];
-        for (int e = te; e < 2 * 3 * NV; e += EPILOGUE) gsS[GS_MAX + 1 + e] = gp[e];
-        // the rows are complete; the previous use of this buffer (two tiles ago)
-        // ended before every epilogue thread reached this tile
-        asm volatile("bar.sync 1, %0;" ::"n"(EPILOGUE) : "memory");
-      }
-      // leave together: the staging barrier above must never wait for a thread that left
-      if (bar_any<1, EPILOGUE>(!mbar_wait_role(tfull + d, uint32_t(i >> 1) & 1u, abort))) break;
+      // the pair's rows in gain buffer d
+      const float* gsS = reinterpret_cast<const float*>(sm + OFF_G) + d * GROW;
+      const float2* gpS = reinterpret_cast<const float2*>(gsS + GS_PAD);
+      const uint32_t u = uint32_t(i >> 1) & 1u;
+      if (!mbar_wait_role(tfull + d, u, abort)) break;
+      if (MODE == COL_PEND && !mbar_wait_role(gfull + d, u, abort)) break;
       tm_fence_after();
       const uint32_t ta = tmem + (uint32_t(32 * qd) << 16) + uint32_t(256 + 128 * d + 64 * hh);
       float2 gbc = make_float2(1.f, 0.f);
@@ -258,6 +239,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       // the accumulator has been read: the issuer may overwrite it
       tm_fence_before();
       mbar_arrive(tempty + d);
+      if constexpr (MODE == COL_PEND) mbar_arrive(gempty + d);  // and the gain rows
     }
   } else if (warp == ISSUER_WARP) {
     if (lane == 0) {
@@ -304,6 +286,14 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       mbar_arrive_tx(rfull + b, RAW + (MODE == COL_PSTART ? PROW : 0));
       tma_load_2d(sm + OFF_R + b * RAW, &tmap, 2 * j0, y, rfull + b);
       if constexpr (MODE == COL_PSTART) bulk_g2s(sm + OFF_P + b * PROW, a.ephase + pair * 3 * NV, PROW, rfull + b);
+      if constexpr (MODE == COL_PEND) {
+        // the pair's gain rows into gain buffer b once the epilogue of tile i - 2 is done with it
+        if (!mbar_wait_role(gempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
+        unsigned char* g = sm + OFF_G + b * GROW * 4;
+        mbar_arrive_tx(gfull + b, GS_PAD * 4 + PROW);
+        bulk_g2s(g, a.gsinc + int64_t(pair / a.ns) * GS_PAD, GS_PAD * 4, gfull + b);
+        bulk_g2s(g + GS_PAD * 4, a.gphase + pair * 3 * NV, PROW, gfull + b);
+      }
     }
   }
   __syncthreads();
@@ -408,6 +398,13 @@ int col_tc_prepare(pii_plan* p) {
     PII_CUDA(cudaMemset(p->dft_err, 0, sizeof(int)));
     p->bytes += int64_t(img.size() * 2 + sizeof(int));
   }
+  if (!p->dft_gs) {  // the radial sinc rows with a 16-byte row pitch (bulk-copy sources)
+    PII_CUDA(cudaMalloc(&p->dft_gs, size_t(p->nr) * GS_PAD * sizeof(float)));
+    PII_CUDA(cudaMemset(p->dft_gs, 0, size_t(p->nr) * GS_PAD * sizeof(float)));
+    PII_CUDA(cudaMemcpy2D(p->dft_gs, GS_PAD * sizeof(float), p->tab.gsinc, size_t(p->tab.M + 1) * sizeof(float),
+                          size_t(p->tab.M + 1) * sizeof(float), size_t(p->nr), cudaMemcpyDeviceToDevice));
+    p->bytes += int64_t(p->nr) * GS_PAD * sizeof(float);
+  }
   PII_CUDA(cudaDeviceGetAttribute(&p->dft_ctas, cudaDevAttrMultiProcessorCount, p->device));
   return PII_OK;
 }
@@ -424,8 +421,7 @@ int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int
   a.fimg = reinterpret_cast<const uint4*>(static_cast<const char*>(p->dft_img) + (mode == COL_PSTART ? 0 : 2 * OPB));
   a.ephase = static_cast<const float2*>(p->tab.ephase);
   a.gphase = static_cast<const float2*>(p->tab.gphase);
-  a.gsinc = static_cast<const float*>(p->tab.gsinc);
-  a.M1 = p->tab.M + 1;
+  a.gsinc = static_cast<const float*>(p->dft_gs);
   a.ns = p->ns;
   a.items = items;
   a.c0 = c0;
