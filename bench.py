@@ -225,6 +225,23 @@ def measure_n64(pkg, device, cells=256, cells_fp64=2):
     out = {"config": f"n_v={N64}^3 on [-10,10]^3, {NR64} GL radial x {NS64}-point symmetric design, "
                      f"hard spheres, e=e0={E64}, 3-Maxwellian mixtures", "cells": cells,
            "mixed": mixed, "unit": UNIT, "tuning": col.plan.tuning}
+    # the two first-axis column paths side by side (32 cells each): in-register
+    # CUDA-core FFT and the tensor-core split-BF16 DFT
+    tuned = col.plan.tuning
+    paths, q_path = {}, {}
+    nc = min(cells, 32)
+    for path in ("fft", "tensor"):
+        col.plan.set_dft_path(path)
+        col.collide(f[:nc], with_loss=True)
+        torch.cuda.synchronize()
+        a.record()
+        col.collide(f[:nc], with_loss=True)
+        b.record()
+        torch.cuda.synchronize()
+        paths[path] = nc / (a.elapsed_time(b) / 1e3)
+        q_path[path] = col.collide(f[:cells_fp64], with_loss=True).clone()
+    out["dft_paths"] = {"cells": nc, "unit": UNIT, **paths, "tensor_core_stalled": col.plan.dft_stalled}
+    col.plan.set_dft_path(tuned["dft_path"])
     try:
         op = TorchFP64Operator(sm, device, e=E64, gamma=1.0)
         fc = f[:cells_fp64].to(torch.complex128)
@@ -238,6 +255,9 @@ def measure_n64(pkg, device, cells=256, cells_fp64=2):
         out["speedup_vs_fp64_gpu"] = mixed / out["fp64_torch"]
         errs = [float((q[c] - q64[c]).abs().max() / q64[c].abs().max()) for c in range(cells_fp64)]
         out["rel_linf_err_vs_fp64"] = max(errs)
+        for path, qp in q_path.items():
+            out["dft_paths"][f"rel_linf_err_{path}"] = max(
+                float((qp[c] - q64[c]).abs().max() / q64[c].abs().max()) for c in range(cells_fp64))
         del op
     except Exception as ex:  # noqa: BLE001
         out["fp64_torch_error"] = str(ex)[:200]

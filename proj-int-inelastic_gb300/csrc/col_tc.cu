@@ -5,14 +5,19 @@
 // One item (cell, pair) is a 64 x 4096 complex array X[a][j] (j = (b, c)); its
 // transform along a, Y[k][j] = sum_a W^{k a} X[a][j] with W = exp(DIR 2 pi i / 64)
 // (DIR = +1 for the inverse transform of the first stage, -1 for the forward
-// transform of the last), is, per tile of 128 columns, the real GEMM
-//   D[n][o] = sum_kappa X[n][kappa] F[o][kappa],   n < 128 columns,
-// kappa = a (Re X) or 64 + a (Im X), o = 2 k (Re Y[k]) or 2 k + 1 (Im Y[k]),
-//   F[2k][a] = C, F[2k][64+a] = -S, F[2k+1][a] = S, F[2k+1][64+a] = C,   C + i S = W^{k a}.
-// Both operands are split into BF16 pairs, x = x_hi + x_lo (x_hi = bf16(x),
+// transform of the last), is split once by decimation in frequency,
+//   Y[2 k'] = sum_{a' < 32} S[a'] W^{2 k' a'},   Y[2 k' + 1] = sum_{a' < 32} D[a'] W^{(2 k' + 1) a'},
+//   S = X[a'] + X[a' + 32],  D = X[a'] - X[a' + 32],
+// and each half is, per tile of 128 columns, the real GEMM (g = even, odd)
+//   D_g[n][o] = sum_kappa Z_g[n][kappa] F_g[o][kappa],   n < 128 columns,
+// kappa = a' (Re Z) or 32 + a' (Im Z), o = 2 k' (Re) or 2 k' + 1 (Im), Z = S or D,
+//   F_g[2k'][a'] = C, F_g[2k'][32+a'] = -S, F_g[2k'+1][a'] = S, F_g[2k'+1][32+a'] = C,
+//   C + i S = W^{2 k' a'} (even) or W^{(2 k' + 1) a'} (odd)
+// (K = 64, N = 64: half the products of the dense 64-point DFT).  Both
+// operands are split into BF16 pairs, x = x_hi + x_lo (x_hi = bf16(x),
 // x_lo = bf16(x - x_hi): 16 significant bits), and the product is formed as
-// X_hi F_hi + X_lo F_hi + X_hi F_lo with FP32 accumulation (the dropped
-// X_lo F_lo and the residual of the split are ~2^-17 of each term).
+// Z_hi F_hi + Z_lo F_hi + Z_hi F_lo with FP32 accumulation (the dropped
+// Z_lo F_lo and the residual of the split are ~2^-17 of each term).
 //
 // Kernel: persistent, one CTA per SM, warp-specialised, every stage double-buffered:
 //   warp 17     TMA: one 2D tensor-map load of the tile (64 rows a x 128
@@ -20,19 +25,23 @@
 //               copy of the pair's phase rows, src/collision/inelastic_collisions.py:212;
 //               PEND: the plane-pass output in the chunk buffer);
 //   warps 0-7   converters: lane = column n; multiply by the phase (PSTART),
-//               split to BF16 hi / lo and tcgen05.st the operand X into tensor
-//               memory (X buffer i % 2: row n = TMEM lane n, K pairs per column);
-//   warp 16     issuer (one thread): 3 x 8 tcgen05.mma (M = N = 128, K = 16,
-//               A = X from tensor memory, B = F from shared memory) into
-//               accumulator i % 2, then commits to xempty (X buffer free) and tfull;
+//               form S and D, split to BF16 hi / lo and tcgen05.st the operands
+//               into tensor memory (buffer i % 2: row n = TMEM lane n, K pairs
+//               per column);
+//   warp 16     issuer (one thread): 2 x 3 x 4 tcgen05.mma (M = 128, N = 64,
+//               K = 16, A = Z_g from tensor memory, B = F_g from shared memory)
+//               into accumulator i % 2 (D_even | D_odd), then commits to xempty
+//               (operand buffer free) and tfull;
 //   warps 8-15  epilogue: tcgen05.ld of the accumulator (lane = column n,
 //               TMEM column = output o: whole complex outputs per thread),
 //               arrive on tempty, store Y[k][j] coalesced along j (PEND: times
-//               the pair's gain, :213-214, from its radial sinc row and phase
-//               rows, bulk-copied by the TMA thread into gain buffer i % 2).
-// Tensor memory: X buffers at columns [0, 256), accumulators at [256, 512).
-// The F image (F_hi | F_lo, 64 KB, laid out on the host) is bulk-copied once
-// per CTA.  Every mbarrier wait is bounded; a role that gives up raises a
+//               the pair's gain, :213-214: its phase rows and the slices
+//               gsinc[r][|k_b|^2 + |k_c|^2 + |k_a|^2] of the tile's two k_b,
+//               bulk-copied by the TMA thread into gain buffer i % 2).
+// Tensor memory: operand buffers at columns [0, 256) (per buffer: S_hi, D_hi,
+// S_lo, D_lo, 32 columns each), accumulators at [256, 512).  The F images
+// (F_even hi / lo, F_odd hi / lo, 32 KB, laid out on the host) are
+// bulk-copied once per CTA.  Every mbarrier wait is bounded; a role that gives up raises a
 // shared abort flag that ends the other roles' waits, and the device error
 // word is set.  Replaces k_col<float, 64, PSTART / PEND>.
 #include <cuda.h>
@@ -56,16 +65,19 @@ constexpr int ISSUER_WARP = (CONVERTERS + EPILOGUE) / 32, TMA_WARP = ISSUER_WARP
 constexpr int THREADS = CONVERTERS + EPILOGUE + 64;
 constexpr int TN = 128;                     // columns per tile (MMA M)
 constexpr int TILES_PER_ITEM = N2 / TN;     // 32
-constexpr uint32_t SBO = 2048, LBO = 128;   // K = 128 bf16 per row: 16 core matrices of 128 B
-constexpr int OPB = 128 * 128 * 2;          // bytes of one 128 x 128 BF16 operand
+constexpr uint32_t SBO = 1024, LBO = 128;   // K = 64 bf16 per row: 8 core matrices of 128 B
+constexpr int FOP = 64 * 64 * 2;            // bytes of one 64 x 64 BF16 matrix F_g (hi or lo)
+constexpr int FIMG = 4 * FOP;               // F_even hi, F_even lo, F_odd hi, F_odd lo
 constexpr int RAW = NV * TN * 8;            // one raw tile: 64 rows of 128 complex columns
 constexpr int PROW = 3 * NV * 8;            // one pair's phase rows (3 x 64 complex)
 constexpr int OFF_F = 0;                    // F_hi, F_lo
-constexpr int OFF_R = 2 * OPB;              // raw tiles 0, 1, then the two phase rows
+constexpr int OFF_R = FIMG;                 // raw tiles 0, 1, then the two phase rows
 constexpr int OFF_P = OFF_R + 2 * RAW;
-constexpr int GS_MAX = 3 * 32 * 32 + 1;     // gsinc row: |k|^2 <= 3 (n / 2)^2
-constexpr int GS_PAD = (GS_MAX + 3) / 4 * 4;   // row pitch of the padded copy (16-byte rows)
-constexpr int GROW = GS_PAD + 2 * 3 * NV;   // one pair's gain rows: gsinc row, then the 3 x 64 phases (floats)
+// radial sinc factor of the gain by |k| components: slice [|k_c| < 36 (33 used)][|k_a| pitch 33]
+// per (r, |k_b|); odd pitch: lanes with distinct |k_c| read distinct banks
+constexpr int KS = NV / 2 + 1, KC_ROWS = 36, KA_PITCH = 33;
+constexpr int SLICE = KC_ROWS * KA_PITCH;   // floats (a multiple of 4: 16-byte bulk copies)
+constexpr int GROW = 2 * SLICE + 2 * 3 * NV;  // two slices (the tile's two k_b), then the 3 x 64 phases (floats)
 constexpr int OFF_G = OFF_P + 2 * PROW;     // gain rows of the epilogue's two accumulators
 constexpr int OFF_BAR = OFF_G + 2 * GROW * 4;
 constexpr int NBAR = 17;  // rfull[2] rempty[2] xfull[2] xempty[2] tfull[2] tempty[2] fbar gfull[2] gempty[2]
@@ -78,10 +90,10 @@ static_assert(SMEM <= 232448, "shared memory per CTA");
 struct ColTcArgs {
   const float2* src;    // PSTART: f^ [cells][N3]; PEND: the chunk buffer (in place)
   float2* dst;          // the chunk buffer [items][N3]
-  const uint4* fimg;    // DFT matrix image of the direction (F_hi | F_lo)
+  const uint4* fimg;    // DFT matrix images of the direction (F_even hi, lo, F_odd hi, lo)
   const float2* ephase;  // [Q][3][64]
   const float2* gphase;  // [Q][3][64]
-  const float* gsinc;    // [n_r][GS_PAD]: the radial sinc rows, padded to 16-byte rows
+  const float* gsk;      // [n_r][|k_b| < 33][SLICE]: gsinc[r][k_b^2 + k_c^2 + k_a^2]
   int ns;
   int64_t items, c0, p0, np;
   int* err;             // set to 1 if a role gave up waiting
@@ -158,33 +170,45 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       }
       if (!mbar_wait_role(xempty + b, u ^ 1u, abort)) break;
       tm_fence_after();
-      // X buffer b: hi at columns 128 b + [0, 64), lo at 128 b + [64, 128); K index
-      // kappa = a (re) -> column kappa / 2, 64 + a (im) -> column 32 + a / 2.
-      // Two halves of 16 a: 8 K pairs of real parts and 8 of imaginary parts, hi and lo.
+      // operand buffer b (columns 128 b + ...): S_hi [0, 32), D_hi [32, 64), S_lo [64, 96),
+      // D_lo [96, 128); K index kappa = a' (re) -> column a' / 2, 32 + a' (im) -> 16 + a' / 2.
+      // This thread: a' in [16 h, 16 h + 16), in two quarters of 8 (4 K pairs each).
       const uint32_t tx = tmem + (uint32_t(32 * qd) << 16) + uint32_t(128 * b);
 #pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        uint32_t w[4][8];  // re hi, re lo, im hi, im lo
+      for (int s4 = 0; s4 < 2; ++s4) {
+        uint32_t w[8][4];  // [S re hi, S re lo, S im hi, S im lo, D re hi, D re lo, D im hi, D im lo][pair]
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int a0 = 32 * h + 16 * s + 2 * q;
-          float2 v0 = raw[a0 * TN + n], v1 = raw[(a0 + 1) * TN + n];
+        for (int q = 0; q < 4; ++q) {
+          const int a0 = 16 * h + 8 * s4 + 2 * q;
+          float2 x0 = raw[a0 * TN + n], x1 = raw[(a0 + 1) * TN + n];
+          float2 y0 = raw[(a0 + 32) * TN + n], y1 = raw[(a0 + 33) * TN + n];
           if constexpr (MODE == COL_PSTART) {
-            v0 = cmul(v0, cmul(ep[a0], ebc));
-            v1 = cmul(v1, cmul(ep[a0 + 1], ebc));
+            x0 = cmul(x0, cmul(ep[a0], ebc));
+            x1 = cmul(x1, cmul(ep[a0 + 1], ebc));
+            y0 = cmul(y0, cmul(ep[a0 + 32], ebc));
+            y1 = cmul(y1, cmul(ep[a0 + 33], ebc));
           }
-          const __nv_bfloat162 rh = __floats2bfloat162_rn(v0.x, v1.x), ih = __floats2bfloat162_rn(v0.y, v1.y);
-          const float2 rhf = __bfloat1622float2(rh), ihf = __bfloat1622float2(ih);
-          w[0][q] = bf2_bits(rh);
-          w[1][q] = bf2_bits(__floats2bfloat162_rn(v0.x - rhf.x, v1.x - rhf.y));
-          w[2][q] = bf2_bits(ih);
-          w[3][q] = bf2_bits(__floats2bfloat162_rn(v0.y - ihf.x, v1.y - ihf.y));
+          const float2 v[2][2] = {{cadd(x0, y0), cadd(x1, y1)}, {csub(x0, y0), csub(x1, y1)}};
+#pragma unroll
+          for (int g = 0; g < 2; ++g) {
+            const __nv_bfloat162 rh = __floats2bfloat162_rn(v[g][0].x, v[g][1].x);
+            const __nv_bfloat162 ih = __floats2bfloat162_rn(v[g][0].y, v[g][1].y);
+            const float2 rhf = __bfloat1622float2(rh), ihf = __bfloat1622float2(ih);
+            w[4 * g + 0][q] = bf2_bits(rh);
+            w[4 * g + 1][q] = bf2_bits(__floats2bfloat162_rn(v[g][0].x - rhf.x, v[g][1].x - rhf.y));
+            w[4 * g + 2][q] = bf2_bits(ih);
+            w[4 * g + 3][q] = bf2_bits(__floats2bfloat162_rn(v[g][0].y - ihf.x, v[g][1].y - ihf.y));
+          }
         }
-        const uint32_t c = uint32_t(16 * h + 8 * s);
-        tm_st8(tx + c, w[0]);
-        tm_st8(tx + 64 + c, w[1]);
-        tm_st8(tx + 32 + c, w[2]);
-        tm_st8(tx + 96 + c, w[3]);
+        const uint32_t c = uint32_t(8 * h + 4 * s4);  // column of the first K pair (re)
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          const uint32_t base = tx + uint32_t(32 * g);
+          tm_st4(base + c, w[4 * g + 0]);            // re hi
+          tm_st4(base + 64 + c, w[4 * g + 1]);       // re lo
+          tm_st4(base + 16 + c, w[4 * g + 2]);       // im hi
+          tm_st4(base + 64 + 16 + c, w[4 * g + 3]);  // im lo
+        }
       }
       // the raw tile has been read
       mbar_arrive(rempty + b);
@@ -194,7 +218,8 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
     }
   } else if (warp < (CONVERTERS + EPILOGUE) / 32) {
     // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) + lane (column n) and
-    // accumulator columns [64 h', 64 h' + 64) (outputs k = 32 h' .. 32 h' + 31)
+    // accumulator columns [64 h', 64 h' + 64): D_even (h' = 0, outputs k = 2 k')
+    // or D_odd (h' = 1, k = 2 k' + 1), k' < 32
     const int ew = warp - CONVERTERS / 32, qd = ew & 3, hh = ew >> 2;
     const int n = 32 * qd + lane;
     int i = 0;
@@ -205,20 +230,20 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       float2* out = a.dst + item * N3 + j;
       // PEND: gain(k, j) = g_a[k] g_b[jb] g_c[jc] * gsinc[r][k_b^2 + k_c^2 + k_a^2], from
       // the pair's rows in gain buffer d
-      const float* gsS = reinterpret_cast<const float*>(sm + OFF_G) + d * GROW;
-      const float2* gpS = reinterpret_cast<const float2*>(gsS + GS_PAD);
+      const float* gsl = reinterpret_cast<const float*>(sm + OFF_G) + d * GROW;
+      const float2* gpS = reinterpret_cast<const float2*>(gsl + 2 * SLICE);
       const uint32_t u = uint32_t(i >> 1) & 1u;
       if (!mbar_wait_role(tfull + d, u, abort)) break;
       if (MODE == COL_PEND && !mbar_wait_role(gfull + d, u, abort)) break;
       tm_fence_after();
       const uint32_t ta = tmem + (uint32_t(32 * qd) << 16) + uint32_t(256 + 128 * d + 64 * hh);
       float2 gbc = make_float2(1.f, 0.f);
-      int mbc = 0;
+      const float* grow = gsl;
       if constexpr (MODE == COL_PEND) {
         const int jb = j >> 6, jc = j & 63;
         gbc = cmul(gpS[NV + jb], gpS[2 * NV + jc]);
-        const int kb = kval(jb, NV), kc = kval(jc, NV);
-        mbc = kb * kb + kc * kc;
+        const int kc = kval(jc, NV);
+        grow = gsl + (n >> 6) * SLICE + (kc < 0 ? -kc : kc) * KA_PITCH;  // slice of this column's k_b, row |k_c|
       }
 #pragma unroll 1
       for (int c = 0; c < 4; ++c) {
@@ -227,11 +252,11 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         tm_wait_ld(r);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const int k = 32 * hh + 8 * c + q;
+          const int k = 2 * (8 * c + q) + hh;
           float2 y = make_float2(__uint_as_float(r[2 * q]), __uint_as_float(r[2 * q + 1]));
           if constexpr (MODE == COL_PEND) {
             const int ka = kval(k, NV);
-            y = cmul(y, cscale(cmul(gpS[k], gbc), gsS[mbc + ka * ka]));
+            y = cmul(y, cscale(cmul(gpS[k], gbc), grow[ka < 0 ? -ka : ka]));
           }
           out[int64_t(k) * N2] = y;
         }
@@ -245,7 +270,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
     if (lane == 0) {
       // ---- issuer
       const uint32_t sf = smem_u32(sm + OFF_F);
-      constexpr uint32_t idesc = umma_idesc_bf16(TN, 128);
+      constexpr uint32_t idesc = umma_idesc_bf16(TN, 64);
       bool go = mbar_wait_role(fbar, 0, abort);
       int i = 0;
       for (int64_t tile = blockIdx.x; go && tile < ntiles; tile += gridDim.x, ++i) {
@@ -256,12 +281,17 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         tm_fence_after();
         const uint32_t tx = tmem + uint32_t(128 * b), td = tmem + uint32_t(256 + 128 * b);
 #pragma unroll
-        for (int s = 0; s < 8; ++s) {
-          const uint32_t ko = 256u * s;  // two core matrices of F along K per step
-          const uint64_t fhi = umma_sdesc(sf + ko, LBO, SBO), flo = umma_sdesc(sf + OPB + ko, LBO, SBO);
-          umma_bf16_ts(td, tx + uint32_t(8 * s), fhi, idesc, s > 0 ? 1u : 0u);  // X_hi F_hi
-          umma_bf16_ts(td, tx + uint32_t(64 + 8 * s), fhi, idesc, 1u);          // X_lo F_hi
-          umma_bf16_ts(td, tx + uint32_t(8 * s), flo, idesc, 1u);               // X_hi F_lo
+        for (int g = 0; g < 2; ++g) {  // even outputs from S, odd outputs from D
+          const uint32_t zhi = tx + uint32_t(32 * g), zlo = zhi + 64, dg = td + uint32_t(64 * g);
+          const uint32_t fh = sf + uint32_t(2 * g * FOP), fl = fh + uint32_t(FOP);
+#pragma unroll
+          for (int st = 0; st < 4; ++st) {
+            const uint32_t ko = 256u * st;  // two core matrices of F_g along K per step
+            const uint64_t fhi = umma_sdesc(fh + ko, LBO, SBO), flo = umma_sdesc(fl + ko, LBO, SBO);
+            umma_bf16_ts(dg, zhi + uint32_t(8 * st), fhi, idesc, st > 0 ? 1u : 0u);  // Z_hi F_hi
+            umma_bf16_ts(dg, zlo + uint32_t(8 * st), fhi, idesc, 1u);                // Z_lo F_hi
+            umma_bf16_ts(dg, zhi + uint32_t(8 * st), flo, idesc, 1u);                // Z_hi F_lo
+          }
         }
         umma_commit(xempty + b);
         umma_commit(tfull + b);
@@ -269,10 +299,10 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
     }
   } else if (warp == TMA_WARP && lane == 0) {
     // ---- TMA: the F image, then each tile's rows (and the pair's phase rows)
-    mbar_arrive_tx(fbar, 2 * OPB);
+    mbar_arrive_tx(fbar, FIMG);
 #pragma unroll 1
     for (int c = 0; c < 4; ++c)
-      bulk_g2s(sm + OFF_F + c * (OPB / 2), reinterpret_cast<const char*>(a.fimg) + c * (OPB / 2), OPB / 2, fbar);
+      bulk_g2s(sm + OFF_F + c * FOP, reinterpret_cast<const char*>(a.fimg) + c * FOP, FOP, fbar);
     int i = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = i & 1;
@@ -290,9 +320,13 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         // the pair's gain rows into gain buffer b once the epilogue of tile i - 2 is done with it
         if (!mbar_wait_role(gempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
         unsigned char* g = sm + OFF_G + b * GROW * 4;
-        mbar_arrive_tx(gfull + b, GS_PAD * 4 + PROW);
-        bulk_g2s(g, a.gsinc + int64_t(pair / a.ns) * GS_PAD, GS_PAD * 4, gfull + b);
-        bulk_g2s(g + GS_PAD * 4, a.gphase + pair * 3 * NV, PROW, gfull + b);
+        mbar_arrive_tx(gfull + b, 2 * SLICE * 4 + PROW);
+        const float* gr = a.gsk + int64_t(pair / a.ns) * KS * SLICE;
+        for (int h = 0; h < 2; ++h) {  // columns j0 .. j0 + 127 span k_b rows j0 / 64 and j0 / 64 + 1
+          const int kb = kval(j0 / NV + h, NV);
+          bulk_g2s(g + h * SLICE * 4, gr + (kb < 0 ? -kb : kb) * SLICE, SLICE * 4, gfull + b);
+        }
+        bulk_g2s(g + 2 * SLICE * 4, a.gphase + pair * 3 * NV, PROW, gfull + b);
       }
     }
   }
@@ -324,26 +358,31 @@ static float host_bf16_f(uint16_t h) {
   return x;
 }
 
-// F_hi | F_lo images (rows o = 2 k + part, K index kappa) for DIR = +1 (index 0) and -1 (index 1)
+// F_even hi, lo, F_odd hi, lo images (rows o = 2 k' + part, K index kappa, K-major,
+// SBO / LBO as in the kernel) for DIR = +1 (index 0) and -1 (index 1)
 static void build_dft_images(std::vector<uint16_t>& img) {
   using namespace ctc;
-  img.assign(size_t(4) * OPB / 2, 0);
+  constexpr int E = FOP / 2;  // entries per matrix
+  img.assign(size_t(2) * 4 * E, 0);
   for (int d = 0; d < 2; ++d) {
     const int dir = d == 0 ? 1 : -1;
-    uint16_t* hi = img.data() + size_t(d) * OPB;  // OPB / 2 entries per operand, two operands
-    uint16_t* lo = hi + OPB / 2;
-    for (int o = 0; o < 128; ++o)
-      for (int kap = 0; kap < 128; ++kap) {
-        const int k = o >> 1, aa = kap & 63;
-        const CS w = cs_turn((long long)(k * aa) % NV, NV);
-        const double c = w.c, s = dir * w.s;
-        const double v = (o & 1) == 0 ? (kap < 64 ? c : -s) : (kap < 64 ? s : c);
-        const uint16_t h = host_bf16(float(v));
-        const uint16_t l = host_bf16(float(v - double(host_bf16_f(h))));
-        const uint32_t off = umma_kmajor_off(o, kap, SBO, LBO) / 2;
-        hi[off] = h;
-        lo[off] = l;
-      }
+    for (int g = 0; g < 2; ++g) {
+      uint16_t* hi = img.data() + size_t(d) * 4 * E + size_t(2 * g) * E;
+      uint16_t* lo = hi + E;
+      for (int o = 0; o < 64; ++o)
+        for (int kap = 0; kap < 64; ++kap) {
+          const int k = o >> 1, ap = kap & 31;
+          const long long m = (long long)(2 * k + g) * ap % NV;  // W^{(2 k' + g) a'}
+          const CS w = cs_turn(m, NV);
+          const double c = w.c, sn = dir * w.s;
+          const double v = (o & 1) == 0 ? (kap < 32 ? c : -sn) : (kap < 32 ? sn : c);
+          const uint16_t h = host_bf16(float(v));
+          const uint16_t l = host_bf16(float(v - double(host_bf16_f(h))));
+          const uint32_t off = umma_kmajor_off(o, kap, SBO, LBO) / 2;
+          hi[off] = h;
+          lo[off] = l;
+        }
+    }
   }
 }
 
@@ -398,12 +437,18 @@ int col_tc_prepare(pii_plan* p) {
     PII_CUDA(cudaMemset(p->dft_err, 0, sizeof(int)));
     p->bytes += int64_t(img.size() * 2 + sizeof(int));
   }
-  if (!p->dft_gs) {  // the radial sinc rows with a 16-byte row pitch (bulk-copy sources)
-    PII_CUDA(cudaMalloc(&p->dft_gs, size_t(p->nr) * GS_PAD * sizeof(float)));
-    PII_CUDA(cudaMemset(p->dft_gs, 0, size_t(p->nr) * GS_PAD * sizeof(float)));
-    PII_CUDA(cudaMemcpy2D(p->dft_gs, GS_PAD * sizeof(float), p->tab.gsinc, size_t(p->tab.M + 1) * sizeof(float),
-                          size_t(p->tab.M + 1) * sizeof(float), size_t(p->nr), cudaMemcpyDeviceToDevice));
-    p->bytes += int64_t(p->nr) * GS_PAD * sizeof(float);
+  if (!p->dft_gs) {  // gsinc[r][k_b^2 + k_c^2 + k_a^2] by (r, |k_b|, |k_c|, |k_a|) (bulk-copy sources)
+    const int M1 = p->tab.M + 1;
+    std::vector<float> gs(size_t(p->nr) * M1), gk(size_t(p->nr) * KS * SLICE, 0.f);
+    PII_CUDA(cudaMemcpy(gs.data(), p->tab.gsinc, gs.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int r = 0; r < p->nr; ++r)
+      for (int kb = 0; kb < KS; ++kb)
+        for (int kc = 0; kc < KS; ++kc)
+          for (int ka = 0; ka < KS; ++ka)
+            gk[(size_t(r) * KS + kb) * SLICE + kc * KA_PITCH + ka] = gs[size_t(r) * M1 + kb * kb + kc * kc + ka * ka];
+    PII_CUDA(cudaMalloc(&p->dft_gs, gk.size() * sizeof(float)));
+    PII_CUDA(cudaMemcpy(p->dft_gs, gk.data(), gk.size() * sizeof(float), cudaMemcpyHostToDevice));
+    p->bytes += int64_t(gk.size() * sizeof(float));
   }
   PII_CUDA(cudaDeviceGetAttribute(&p->dft_ctas, cudaDevAttrMultiProcessorCount, p->device));
   return PII_OK;
@@ -411,17 +456,17 @@ int col_tc_prepare(pii_plan* p) {
 
 int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int64_t np, cudaStream_t s) {
   using namespace ctc;
-  if (p->n != NV || p->tab.M + 1 > GS_MAX) {
+  if (p->n != NV || p->tab.M != 3 * (NV / 2) * (NV / 2)) {
     set_error("col_tc_run: plan is not an n = 64 3D plan");
     return PII_ERR_ARG;
   }
   ColTcArgs a{};
   a.src = static_cast<const float2*>(mode == COL_PSTART ? p->fhat : p->buf);
   a.dst = static_cast<float2*>(p->buf);
-  a.fimg = reinterpret_cast<const uint4*>(static_cast<const char*>(p->dft_img) + (mode == COL_PSTART ? 0 : 2 * OPB));
+  a.fimg = reinterpret_cast<const uint4*>(static_cast<const char*>(p->dft_img) + (mode == COL_PSTART ? 0 : FIMG));
   a.ephase = static_cast<const float2*>(p->tab.ephase);
   a.gphase = static_cast<const float2*>(p->tab.gphase);
-  a.gsinc = static_cast<const float*>(p->dft_gs);
+  a.gsk = static_cast<const float*>(p->dft_gs);
   a.ns = p->ns;
   a.items = items;
   a.c0 = c0;

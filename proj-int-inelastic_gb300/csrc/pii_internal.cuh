@@ -154,7 +154,7 @@ struct pii_plan {
   void* dft_img = nullptr;  // DFT matrix images (A_hi | A_lo) for DIR = +1 and -1
   int* dft_err = nullptr;   // device word: 1 if a k_col_tc CTA gave up waiting for its MMAs
   int dft_ctas = 0;         // resident CTAs of k_col_tc (one per SM)
-  void* dft_gs = nullptr;   // gsinc rows with a 16-byte row pitch (TMA sources)
+  void* dft_gs = nullptr;   // gsinc by (r, |k_b|, |k_c|, |k_a|) slices (TMA sources)
   // TMA tensor maps (CUtensorMap, 128 bytes each) of f^ and of the chunk buffer
   // as 2D FP32 arrays [rows of 64 (a) per grid][8192 floats per row]
   alignas(128) unsigned char dft_tmap[2][128] = {};
