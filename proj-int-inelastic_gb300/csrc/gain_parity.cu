@@ -259,9 +259,24 @@ __device__ __forceinline__ void pack_stage_a_col(float2* W, const float2* fh, co
   });
 }
 
-// stage C (packed): X(k) = s(k) F(k) with F(k) = W^{PAR k} Z[k mod 16]
+// the column's 17 sinc values |k_a| = 0..16 (of 20 padded) from its radial row of gsx
+__device__ __forceinline__ void load_gsx(const float* gsr, int j, float (&g)[20]) {
+  const int kb = kval(j >> 5, 32), kc = kval(j & 31, 32);
+  const float4* grow = reinterpret_cast<const float4*>(gsr + (kb * kb + kc * kc) * 20);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const float4 v = grow[i];
+    g[4 * i] = v.x;
+    g[4 * i + 1] = v.y;
+    g[4 * i + 2] = v.z;
+    g[4 * i + 3] = v.w;
+  }
+}
+
+// stage C (packed): X(k) = s(k) F(k) with F(k) = W^{PAR k} Z[k mod 16]; g = the
+// column's sinc values (load_gsx; the columns j and -j of a pair share them)
 template <int PAR, int PASS>
-__device__ __forceinline__ void pack_stage_c(const float2* W, int j, const float2* gp, const float* gsr,
+__device__ __forceinline__ void pack_stage_c(const float2* W, int j, const float2* gp, const float (&g)[20],
                                              uint32_t treg) {
   using namespace gc;
   const int jb = j >> 5, jc = j & 31;
@@ -276,17 +291,6 @@ __device__ __forceinline__ void pack_stage_c(const float2* W, int j, const float
     constexpr int k = decltype(ki)::value;
     zw[k] = twiddle<PAR * k, 32, -1>(z[pos(16, k)]);
   });
-  const int kb = kval(jb, 32), kc = kval(jc, 32);
-  const float4* grow = reinterpret_cast<const float4*>(gsr + (kb * kb + kc * kc) * 20);
-  float g[20];
-#pragma unroll
-  for (int i = 0; i < 5; ++i) {
-    const float4 v = grow[i];
-    g[4 * i] = v.x;
-    g[4 * i + 1] = v.y;
-    g[4 * i + 2] = v.z;
-    g[4 * i + 3] = v.w;
-  }
   // d = (g_bc + g~_bc) / 2; s(k_a) = g_a.x dp - g_a.y dm (k_a != 16), s16 at k_a = 16
   const float2 gb = gp[32 + jb], gc2 = gp[64 + jc];
   const float2 gbc = cmul(gb, gc2);
@@ -431,13 +435,19 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
         const int4 uc = a.ucols[t];
         tm_wait_st();
         if constexpr (PACK) {
-          if (par == 0) {
-            pack_stage_c<0, 0>(W, uc.x, gp, gsr, treg0);
-            pack_stage_c<0, 1>(W, uc.y, gp, gsr, treg0 + 64);
-          } else {
-            pack_stage_c<1, 0>(W, uc.x, gp, gsr, treg0);
-            pack_stage_c<1, 1>(W, uc.y, gp, gsr, treg0 + 64);
-          }
+          // |k_b|^2 + |k_c|^2 is the same for j and -j: one sinc row serves both
+          // columns of a pair; only the self-conjugate columns differ
+          float g[20];
+          load_gsx(gsr, uc.x, g);
+          if (par == 0)
+            pack_stage_c<0, 0>(W, uc.x, gp, g, treg0);
+          else
+            pack_stage_c<1, 0>(W, uc.x, gp, g, treg0);
+          if (uc.w) load_gsx(gsr, uc.y, g);
+          if (par == 0)
+            pack_stage_c<0, 1>(W, uc.y, gp, g, treg0 + 64);
+          else
+            pack_stage_c<1, 1>(W, uc.y, gp, g, treg0 + 64);
         } else {
           par_stage_c<0>(W, uc.x, gp, gpp, gsr, treg0);
           par_stage_c<1>(W, uc.y, gp, gpp, gsr, treg0 + 64);
