@@ -376,6 +376,27 @@ def ncu_case(cells):
     return 0
 
 
+def ncu_case64(cells, dft_path):
+    """Small profiling case at 64^3 (the 48 x 70 quadrature, 3-Maxwellian cells): one
+    mixed-precision Q(f,f) evaluation with the given first-axis column path."""
+    import torch
+
+    import proj_int_inelastic_gb300 as pkg
+
+    cfg = {"velocity-mesh": {"nv": N64, "s": S_L10, "nr": NR64},
+           "spherical-design-rule": {"ssrule": "womersley", "nsphr": NS64},
+           "collision-model": {"dim": 3, "type": "vhs", "e": E64, "e0": E64, "gamma": 1.0}}
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=cells)
+    col.plan.set_dft_path(dft_path)
+    f = torch.as_tensor(mixture_states(sm.v_center, cells, 64), device="cuda:0").contiguous()
+    q = col.collide(f, with_loss=True)
+    torch.cuda.synchronize()
+    print(json.dumps({"ncu_case64_cells": cells, "dft_path": dft_path, "q_abs_max": float(q.abs().max()),
+                      "stalled": col.plan.dft_stalled}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,11 +410,17 @@ def main():
     ap.add_argument("--no-n64", action="store_true", help="skip the 64^3 configuration measurement")
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: run 3 Q(f,f) evaluations on this many cells of the workload and exit")
+    ap.add_argument("--ncu-case64", type=int, default=0,
+                    help="profiling case: one 64^3 Q(f,f) evaluation on this many cells and exit")
+    ap.add_argument("--dft-path", default="tensor", choices=["tensor", "fft"],
+                    help="first-axis column path of the 64^3 profiling case")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.ncu_case:
         return ncu_case(args.ncu_case)
+    if args.ncu_case64:
+        return ncu_case64(args.ncu_case64, args.dft_path)
     args.warmup = max(3, args.warmup)
 
     import numpy as np
