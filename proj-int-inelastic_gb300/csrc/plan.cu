@@ -269,8 +269,12 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
   const size_t rs = precision == PII_PREC_FP32 ? 4 : 8;
   const size_t cs = 2 * rs;
   const size_t N = size_t(p->N);
-  // L2-resident chunk of (cell, pair) items: ~48 MB, at least 2 items
-  const size_t target = size_t(48) << 20;
+  // L2-resident chunk of (cell, pair) items: ~48 MB, at least 2 items; 76 MB
+  // (38 items) for the n = 64 FP32 plans, whose tensor-core column pass then
+  // gives each of 152 SMs 8 whole tiles per launch (measured: 48 MB -> 91.1,
+  // 80 MB -> 94.1, 96 MB -> 81.4 cell-evals/s; beyond ~80 MB the chunk no
+  // longer stays in the 126 MB L2 next to f^, f and G)
+  const size_t target = size_t(n == 64 && precision == PII_PREC_FP32 && dim == 3 ? 76 : 48) << 20;
   p->chunk_items = std::max<int64_t>(2, int64_t(target / (N * cs)));
   int s2 = PII_OK;
   if ((s2 = alloc(p, &p->fhat, size_t(batch_max) * N * cs)) != PII_OK ||
