@@ -53,6 +53,12 @@ def test_version_and_error_paths_without_gpu():
         pkg._lib.check(st, "pii_plan_create")
     assert lib.pii_plan_destroy(None) == pkg._lib.PII_ERR_ARG
     assert lib.pii_axpby(None, None, 1.0, 1.0, 4, None) == pkg._lib.PII_ERR_ARG
+    # tuning entry points validate before touching a plan
+    assert lib.pii_plan_set_dft_path(None, 1) == pkg._lib.PII_ERR_ARG
+    assert "path must be 0" in pkg._lib.last_error()
+    path, stalled = ctypes.c_int(-1), ctypes.c_int(-1)
+    assert lib.pii_plan_get_dft_path(None, ctypes.byref(path), ctypes.byref(stalled)) == pkg._lib.PII_ERR_ARG
+    assert lib.pii_plan_set_gain_path(None, 3) == pkg._lib.PII_ERR_ARG
 
 
 def test_spectral_mesh_matches_oracle():
@@ -141,3 +147,14 @@ def test_mesh_2d_matches_oracle():
     assert np.array_equal(sig, m.sigma) and w == m.wsigma
     assert np.array_equal(sm.rquad()[0], m.r) and np.array_equal(sm.v_center, m.v)
     assert len(sm.v_centers) == 2 and sm.v_centers[0].shape == (32, 32)
+
+
+def test_python_tuning_maps():
+    """The Python tuning names map onto the C ABI's path codes."""
+    import proj_int_inelastic_gb300 as pkg
+    from proj_int_inelastic_gb300 import collision
+
+    assert collision.GAIN_PATHS == {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3}
+    assert collision.DFT_PATHS == {"fft": 0, "tensor": 1}
+    assert set(pkg._lib.SIGNATURES) >= {"pii_plan_set_dft_path", "pii_plan_get_dft_path"}
+
