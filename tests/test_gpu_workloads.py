@@ -167,3 +167,27 @@ def test_tensor_core_dft_path_rules():
     with pytest.raises(ValueError):
         col.plan.set_dft_path("tensor")
     assert col.plan.tuning["dft_path"] == "fft"
+
+
+def test_tensor_core_dft_ragged_chunks():
+    """Tensor-core column passes on ragged chunks: 3 cells with 2 cells per
+    chunk (chunk_points = 2 x 64^3) and 24 pairs split 19 + 5, so items of one
+    launch span two cells and the last chunk holds one cell; against the
+    CUDA-core FFT columns and the FP64 path."""
+    pkg = _pkg()
+    s = 20.0 / (3.0 + math.sqrt(2.0))
+    cfg = op_config(64, s, 4, 6, 0.6, 0.8, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    rng = np.random.default_rng(3)
+    f = torch.as_tensor(np.stack([_mixture(sm.v_center, rng, 2, 2.0, (0.6, 2.0)) for _ in range(3)]),
+                        device="cuda:0")
+    qd = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=3).collide(f, with_loss=True)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=3)
+    out = {}
+    for path in ("fft", "tensor"):
+        col.plan.set_tuning("pipeline", 6, 2 * 64**3, dft_path=path)
+        out[path] = col.collide(f, with_loss=True)
+    assert not col.plan.dft_stalled
+    for c in range(3):
+        assert rel_linf(out["tensor"][c].cpu().numpy(), qd[c].cpu().numpy()) < 1e-5, c
+        assert rel_linf(out["tensor"][c].cpu().numpy(), out["fft"][c].cpu().numpy()) < 1e-5, c
