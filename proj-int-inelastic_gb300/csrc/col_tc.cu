@@ -14,40 +14,53 @@
 //   F_g[2k'][a'] = C, F_g[2k'][32+a'] = -S, F_g[2k'+1][a'] = S, F_g[2k'+1][32+a'] = C,
 //   C + i S = W^{2 k' a'} (even) or W^{(2 k' + 1) a'} (odd)
 // (K = 64, N = 64: half the products of the dense 64-point DFT).  Both
-// operands are split into BF16 pairs, x = x_hi + x_lo (x_hi = bf16(x),
-// x_lo = bf16(x - x_hi): 16 significant bits), and the product is formed as
+// operands are split into FP16 pairs, x = x_hi + x_lo (x_hi = fp16(x),
+// x_lo = fp16(x - x_hi): 22 significant bits), and the product is formed as
 // Z_hi F_hi + Z_lo F_hi + Z_hi F_lo with FP32 accumulation (the dropped
-// Z_lo F_lo and the residual of the split are ~2^-17 of each term).
+// Z_lo F_lo and the residual of the split are ~2^-22 of each term).  Each
+// column is first scaled by a power of two that brings a bound on its S and D
+// components (L1 norms of the inputs and phases, within ~3x of the largest)
+// into [1/2, 1) (FP16 range, and x_lo stays a normal number for the column's
+// large entries); the epilogue undoes it.  BF16 pairs (16 bits)
+// measured 1.3e-5 relative L-inf against FP64 on a peaked cell with a small
+// quadrature; FP16 pairs bring the path to the CUDA-core FFT's level.
 //
 // Kernel: persistent, one CTA per SM, warp-specialised, every stage double-buffered:
 //   warp 17     TMA: one 2D tensor-map load of the tile (64 rows a x 128
 //               columns, 64 KB) into raw buffer i % 2 (PSTART: f^, plus a bulk
 //               copy of the pair's phase rows, src/collision/inelastic_collisions.py:212;
 //               PEND: the plane-pass output in the chunk buffer);
-//   warps 0-7   converters: lane = column n; multiply by the phase (PSTART),
-//               form S and D, split to BF16 hi / lo and tcgen05.st the operands
-//               into tensor memory (buffer i % 2: row n = TMEM lane n, K pairs
-//               per column);
-//   warp 16     issuer (one thread): 2 x 3 x 4 tcgen05.mma (M = 128, N = 64,
-//               K = 16, A = Z_g from tensor memory, B = F_g from shared memory)
-//               into accumulator i % 2 (D_even | D_odd), then commits to xempty
+//   warps 0-7   converters: lane = column n, warps w and w + 4 take a' in
+//               [0, 16) and [16, 32); the two exchange their partial bounds
+//               (named barrier 1), multiply by the phase (PSTART), form S and
+//               D, scale, split to FP16 hi / lo, tcgen05.st the operands into
+//               tensor memory (buffer i % 2: row n = TMEM lane n, K pairs per
+//               column) and write the column's scale to scale buffer i % 4;
+//   warp 16     issuer (one thread): arrives on sready (the scales of the tile
+//               are visible), 2 x 3 x 4 tcgen05.mma (M = 128, N = 64, K = 16,
+//               A = Z_g from tensor memory, B = F_g from shared memory) into
+//               accumulator i % 2 (D_even | D_odd), then commits to xempty
 //               (operand buffer free) and tfull;
 //   warps 8-15  epilogue: tcgen05.ld of the accumulator (lane = column n,
 //               TMEM column = output o: whole complex outputs per thread),
-//               arrive on tempty, store Y[k][j] coalesced along j (PEND: times
+//               undo the column's scale, arrive on tempty, store Y[k][j]
+//               coalesced along j (PEND: times
 //               the pair's gain, :213-214: its phase rows and the slices
 //               gsinc[r][|k_b|^2 + |k_c|^2 + |k_a|^2] of the tile's two k_b,
 //               bulk-copied by the TMA thread into gain buffer i % 2).
 // Tensor memory: operand buffers at columns [0, 256) (per buffer: S_hi, D_hi,
 // S_lo, D_lo, 32 columns each), accumulators at [256, 512).  The F images
-// (F_even hi / lo, F_odd hi / lo, 32 KB, laid out on the host) are
-// bulk-copied once per CTA.  Every mbarrier wait is bounded; a role that gives up raises a
+// (F_even hi / lo, F_odd hi / lo in FP16, 32 KB, laid out on the host) are
+// bulk-copied once per CTA.  A scale buffer is rewritten four tiles later,
+// after the MMAs of tile i + 2 -- issued only once the epilogue of tile i has
+// released its accumulator, i.e. after it read the scales.  Every mbarrier wait is bounded; a role that gives up raises a
 // shared abort flag that ends the other roles' waits, and the device error
 // word is set.  Replaces k_col<float, 64, PSTART / PEND>.
 #include <cuda.h>
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -61,12 +74,15 @@ namespace pii {
 namespace ctc {
 constexpr int NV = 64, N2 = NV * NV, N3 = NV * N2;
 constexpr int CONVERTERS = 256, EPILOGUE = 256;
+// two more warps with one working lane each: the MMA issuer and the TMA thread
+// (in separate warps: a lane suspended in an mbarrier wait would hold up the
+// other's path; measured 20-25 % slower with the two roles in one warp)
 constexpr int ISSUER_WARP = (CONVERTERS + EPILOGUE) / 32, TMA_WARP = ISSUER_WARP + 1;
 constexpr int THREADS = CONVERTERS + EPILOGUE + 64;
 constexpr int TN = 128;                     // columns per tile (MMA M)
 constexpr int TILES_PER_ITEM = N2 / TN;     // 32
 constexpr uint32_t SBO = 1024, LBO = 128;   // K = 64 bf16 per row: 8 core matrices of 128 B
-constexpr int FOP = 64 * 64 * 2;            // bytes of one 64 x 64 BF16 matrix F_g (hi or lo)
+constexpr int FOP = 64 * 64 * 2;            // bytes of one 64 x 64 FP16 matrix F_g (hi or lo)
 constexpr int FIMG = 4 * FOP;               // F_even hi, F_even lo, F_odd hi, F_odd lo
 constexpr int RAW = NV * TN * 8;            // one raw tile: 64 rows of 128 complex columns
 constexpr int PROW = 3 * NV * 8;            // one pair's phase rows (3 x 64 complex)
@@ -79,8 +95,11 @@ constexpr int KS = NV / 2 + 1, KC_ROWS = 36, KA_PITCH = 33;
 constexpr int SLICE = KC_ROWS * KA_PITCH;   // floats (a multiple of 4: 16-byte bulk copies)
 constexpr int GROW = 2 * SLICE + 2 * 3 * NV;  // two slices (the tile's two k_b), then the 3 x 64 phases (floats)
 constexpr int OFF_G = OFF_P + 2 * PROW;     // gain rows of the epilogue's two accumulators
-constexpr int OFF_BAR = OFF_G + 2 * GROW * 4;
-constexpr int NBAR = 17;  // rfull[2] rempty[2] xfull[2] xempty[2] tfull[2] tempty[2] fbar gfull[2] gempty[2]
+constexpr int OFF_SC = OFF_G + 2 * GROW * 4;  // column scales [4 tiles][128 columns] (floats)
+constexpr int OFF_XB = OFF_SC + 4 * TN * 4;     // partial bounds [2 tiles][2 halves][128 columns]
+constexpr int OFF_BAR = OFF_XB + 2 * 2 * TN * 4;
+// rfull[2] rempty[2] xfull[2] xempty[2] tfull[2] tempty[2] fbar gfull[2] gempty[2] sready[2]
+constexpr int NBAR = 19;
 constexpr int SMEM = OFF_BAR + NBAR * 8 + 16;
 constexpr uint32_t TMEM_COLS = 512;         // X buffers [0, 256), accumulators [256, 512)
 constexpr uint32_t WAIT_LIMIT = 1u << 22;   // mbarrier polls before a role gives up
@@ -99,7 +118,15 @@ struct ColTcArgs {
   int* err;             // set to 1 if a role gave up waiting
 };
 
-__device__ __forceinline__ uint32_t bf2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
+__device__ __forceinline__ uint32_t h2_bits(__half2 v) { return *reinterpret_cast<uint32_t*>(&v); }
+
+// FP16 hi / lo words of the K pair (x0, x1) (x already scaled into [-1, 1))
+__device__ __forceinline__ void split_pair(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+  const __half2 h = __floats2half2_rn(x0, x1);
+  const float2 hf = __half22float2(h);
+  hi = h2_bits(h);
+  lo = h2_bits(__floats2half2_rn(x0 - hf.x, x1 - hf.y));
+}
 
 // bounded wait that also ends when another role has raised the abort flag
 __device__ __forceinline__ bool mbar_wait_role(uint64_t* mbar, uint32_t parity, volatile int* abort) {
@@ -109,6 +136,21 @@ __device__ __forceinline__ bool mbar_wait_role(uint64_t* mbar, uint32_t parity, 
   }
   *abort = 1;
   return false;
+}
+
+// true in every thread of the named barrier `ID` (COUNT threads) if `pred` holds in any of them
+template <int ID, int COUNT>
+__device__ __forceinline__ bool bar_any(bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"(uint32_t(pred)), "n"(ID), "n"(COUNT)
+      : "memory");
+  return r != 0;
 }
 
 template <int MODE>
@@ -125,6 +167,8 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
   uint64_t* fbar = bars + 12;
   uint64_t* gfull = bars + 13;
   uint64_t* gempty = bars + 15;
+  uint64_t* sready = bars + 17;
+  float* scl = reinterpret_cast<float*>(sm + OFF_SC);
   volatile int* abort = reinterpret_cast<volatile int*>(bars + NBAR);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + NBAR) + 1;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -143,6 +187,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       mbar_init(tempty + b, EPILOGUE);
       mbar_init(gfull + b, 1);
       mbar_init(gempty + b, EPILOGUE);
+      mbar_init(sready + b, 1);
     }
     mbar_init(fbar, 1);
     *abort = 0;
@@ -154,25 +199,50 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
   const int64_t ntiles = a.items * TILES_PER_ITEM;
 
   if (warp < CONVERTERS / 32) {
-    // ---- converters: warp w -> TMEM lanes 32 (w % 4) + lane (column n), a in [32 h, 32 h + 32)
+    // ---- converters: warp w -> TMEM lanes 32 (w % 4) + lane (column n), a' in [16 h, 16 h + 16)
     const int qd = warp & 3, h = warp >> 2, n = 32 * qd + lane;
+    float* xb = reinterpret_cast<float*>(sm + OFF_XB);
+    auto l1 = [](float2 v) { return fabsf(v.x) + fabsf(v.y); };
     int i = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = i & 1;
       const uint32_t u = uint32_t(i >> 1) & 1u;
-      if (!mbar_wait_role(rfull + b, u, abort)) break;
+      // the raw tile is in and operand buffer b is free (MMAs of tile i - 2 done)
+      const bool ok = mbar_wait_role(rfull + b, u, abort) && mbar_wait_role(xempty + b, u ^ 1u, abort);
       const float2* raw = reinterpret_cast<const float2*>(sm + OFF_R + b * RAW);
       const float2* ep = reinterpret_cast<const float2*>(sm + OFF_P + b * PROW);
       float2 ebc = make_float2(1.f, 0.f);
       if constexpr (MODE == COL_PSTART) {
         const int j = int(tile % TILES_PER_ITEM) * TN + n;
-        ebc = cmul(ep[NV + (j >> 6)], ep[2 * NV + (j & 63)]);
+        if (ok) ebc = cmul(ep[NV + (j >> 6)], ep[2 * NV + (j & 63)]);
       }
-      if (!mbar_wait_role(xempty + b, u ^ 1u, abort)) break;
+      if (ok) {
+        // pass 1: this half's bound on |x0 e0 +- x1 e1| (L1 norms, no products of complex numbers)
+        float mb = 0.f;
+#pragma unroll 8
+        for (int q = 0; q < 16; ++q) {
+          const int ap = 16 * h + q;
+          float t0 = l1(raw[ap * TN + n]), t1 = l1(raw[(ap + 32) * TN + n]);
+          if constexpr (MODE == COL_PSTART) {
+            t0 *= l1(ep[ap]);
+            t1 *= l1(ep[ap + 32]);
+          }
+          mb = fmaxf(mb, t0 + t1);
+        }
+        xb[((i & 1) * 2 + h) * TN + n] = mb;
+      }
+      // exchange with the other half of the column; every exit of this loop is
+      // voted here, so the barrier never waits for a converter that left
+      if (bar_any<1, CONVERTERS>(!ok)) break;
+      float mx = fmaxf(xb[((i & 1) * 2 + h) * TN + n], xb[((i & 1) * 2 + (h ^ 1)) * TN + n]);
+      if constexpr (MODE == COL_PSTART) mx *= l1(ebc);
+      // power of two bringing the bound into [1/2, 1): exponent arithmetic only
+      const int ex = mx > 0.f ? int((__float_as_uint(mx) >> 23) & 0xFF) - 126 : 0;
+      const float down = __uint_as_float(uint32_t(127 - ex) << 23), up = __uint_as_float(uint32_t(127 + ex) << 23);
       tm_fence_after();
-      // operand buffer b (columns 128 b + ...): S_hi [0, 32), D_hi [32, 64), S_lo [64, 96),
-      // D_lo [96, 128); K index kappa = a' (re) -> column a' / 2, 32 + a' (im) -> 16 + a' / 2.
-      // This thread: a' in [16 h, 16 h + 16), in two quarters of 8 (4 K pairs each).
+      // pass 2: operand buffer b (columns 128 b + ...): S_hi [0, 32), D_hi [32, 64),
+      // S_lo [64, 96), D_lo [96, 128); K index kappa = a' (re) -> column a' / 2,
+      // 32 + a' (im) -> 16 + a' / 2.  Two quarters of 8 a' (4 K pairs each).
       const uint32_t tx = tmem + (uint32_t(32 * qd) << 16) + uint32_t(128 * b);
 #pragma unroll
       for (int s4 = 0; s4 < 2; ++s4) {
@@ -191,13 +261,8 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
           const float2 v[2][2] = {{cadd(x0, y0), cadd(x1, y1)}, {csub(x0, y0), csub(x1, y1)}};
 #pragma unroll
           for (int g = 0; g < 2; ++g) {
-            const __nv_bfloat162 rh = __floats2bfloat162_rn(v[g][0].x, v[g][1].x);
-            const __nv_bfloat162 ih = __floats2bfloat162_rn(v[g][0].y, v[g][1].y);
-            const float2 rhf = __bfloat1622float2(rh), ihf = __bfloat1622float2(ih);
-            w[4 * g + 0][q] = bf2_bits(rh);
-            w[4 * g + 1][q] = bf2_bits(__floats2bfloat162_rn(v[g][0].x - rhf.x, v[g][1].x - rhf.y));
-            w[4 * g + 2][q] = bf2_bits(ih);
-            w[4 * g + 3][q] = bf2_bits(__floats2bfloat162_rn(v[g][0].y - ihf.x, v[g][1].y - ihf.y));
+            split_pair(v[g][0].x * down, v[g][1].x * down, w[4 * g + 0][q], w[4 * g + 1][q]);
+            split_pair(v[g][0].y * down, v[g][1].y * down, w[4 * g + 2][q], w[4 * g + 3][q]);
           }
         }
         const uint32_t c = uint32_t(8 * h + 4 * s4);  // column of the first K pair (re)
@@ -212,6 +277,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       }
       // the raw tile has been read
       mbar_arrive(rempty + b);
+      if (h == 0) scl[(i & 3) * TN + n] = up;
       tm_wait_st();
       tm_fence_before();
       mbar_arrive(xfull + b);
@@ -234,8 +300,10 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       const float2* gpS = reinterpret_cast<const float2*>(gsl + 2 * SLICE);
       const uint32_t u = uint32_t(i >> 1) & 1u;
       if (!mbar_wait_role(tfull + d, u, abort)) break;
+      if (!mbar_wait_role(sready + d, u, abort)) break;
       if (MODE == COL_PEND && !mbar_wait_role(gfull + d, u, abort)) break;
       tm_fence_after();
+      const float up = scl[(i & 3) * TN + n];  // the column's scale (S and D alike)
       const uint32_t ta = tmem + (uint32_t(32 * qd) << 16) + uint32_t(256 + 128 * d + 64 * hh);
       float2 gbc = make_float2(1.f, 0.f);
       const float* grow = gsl;
@@ -253,7 +321,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int k = 2 * (8 * c + q) + hh;
-          float2 y = make_float2(__uint_as_float(r[2 * q]), __uint_as_float(r[2 * q + 1]));
+          float2 y = make_float2(up * __uint_as_float(r[2 * q]), up * __uint_as_float(r[2 * q + 1]));
           if constexpr (MODE == COL_PEND) {
             const int ka = kval(k, NV);
             y = cmul(y, cscale(cmul(gpS[k], gbc), grow[ka < 0 ? -ka : ka]));
@@ -270,7 +338,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
     if (lane == 0) {
       // ---- issuer
       const uint32_t sf = smem_u32(sm + OFF_F);
-      constexpr uint32_t idesc = umma_idesc_bf16(TN, 64);
+      constexpr uint32_t idesc = umma_idesc_f16(TN, 64);
       bool go = mbar_wait_role(fbar, 0, abort);
       int i = 0;
       for (int64_t tile = blockIdx.x; go && tile < ntiles; tile += gridDim.x, ++i) {
@@ -278,6 +346,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         const uint32_t u = uint32_t(i >> 1) & 1u;
         if (!mbar_wait_role(xfull + b, u, abort)) break;
         if (!mbar_wait_role(tempty + b, u ^ 1u, abort)) break;
+        mbar_arrive(sready + b);  // the converters' scales of this tile are visible from here
         tm_fence_after();
         const uint32_t tx = tmem + uint32_t(128 * b), td = tmem + uint32_t(256 + 128 * b);
 #pragma unroll
@@ -297,36 +366,38 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         umma_commit(tfull + b);
       }
     }
-  } else if (warp == TMA_WARP && lane == 0) {
-    // ---- TMA: the F image, then each tile's rows (and the pair's phase rows)
-    mbar_arrive_tx(fbar, FIMG);
+  } else if (warp == TMA_WARP) {
+    if (lane == 0) {
+      // ---- TMA: the F image, then each tile's rows (and the pair's phase rows)
+      mbar_arrive_tx(fbar, FIMG);
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c)
-      bulk_g2s(sm + OFF_F + c * FOP, reinterpret_cast<const char*>(a.fimg) + c * FOP, FOP, fbar);
-    int i = 0;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
-      const int b = i & 1;
-      if (!mbar_wait_role(rempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
-      const int64_t item = tile / TILES_PER_ITEM;
-      const int j0 = int(tile - item * TILES_PER_ITEM) * TN;
-      const int64_t ci = item / a.np;
-      const int64_t pair = a.p0 + (item - ci * a.np);
-      // rows of 64 per grid: f^ of cell c0 + ci, or item `item` of the chunk buffer
-      const int y = int(MODE == COL_PSTART ? (a.c0 + ci) * NV : item * NV);
-      mbar_arrive_tx(rfull + b, RAW + (MODE == COL_PSTART ? PROW : 0));
-      tma_load_2d(sm + OFF_R + b * RAW, &tmap, 2 * j0, y, rfull + b);
-      if constexpr (MODE == COL_PSTART) bulk_g2s(sm + OFF_P + b * PROW, a.ephase + pair * 3 * NV, PROW, rfull + b);
-      if constexpr (MODE == COL_PEND) {
-        // the pair's gain rows into gain buffer b once the epilogue of tile i - 2 is done with it
-        if (!mbar_wait_role(gempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
-        unsigned char* g = sm + OFF_G + b * GROW * 4;
-        mbar_arrive_tx(gfull + b, 2 * SLICE * 4 + PROW);
-        const float* gr = a.gsk + int64_t(pair / a.ns) * KS * SLICE;
-        for (int h = 0; h < 2; ++h) {  // columns j0 .. j0 + 127 span k_b rows j0 / 64 and j0 / 64 + 1
-          const int kb = kval(j0 / NV + h, NV);
-          bulk_g2s(g + h * SLICE * 4, gr + (kb < 0 ? -kb : kb) * SLICE, SLICE * 4, gfull + b);
+      for (int c = 0; c < 4; ++c)
+        bulk_g2s(sm + OFF_F + c * FOP, reinterpret_cast<const char*>(a.fimg) + c * FOP, FOP, fbar);
+      int i = 0;
+      for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        const int b = i & 1;
+        if (!mbar_wait_role(rempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
+        const int64_t item = tile / TILES_PER_ITEM;
+        const int j0 = int(tile - item * TILES_PER_ITEM) * TN;
+        const int64_t ci = item / a.np;
+        const int64_t pair = a.p0 + (item - ci * a.np);
+        // rows of 64 per grid: f^ of cell c0 + ci, or item `item` of the chunk buffer
+        const int y = int(MODE == COL_PSTART ? (a.c0 + ci) * NV : item * NV);
+        mbar_arrive_tx(rfull + b, RAW + (MODE == COL_PSTART ? PROW : 0));
+        tma_load_2d(sm + OFF_R + b * RAW, &tmap, 2 * j0, y, rfull + b);
+        if constexpr (MODE == COL_PSTART) bulk_g2s(sm + OFF_P + b * PROW, a.ephase + pair * 3 * NV, PROW, rfull + b);
+        if constexpr (MODE == COL_PEND) {
+          // the pair's gain rows into gain buffer b once the epilogue of tile i - 2 is done with it
+          if (!mbar_wait_role(gempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
+          unsigned char* g = sm + OFF_G + b * GROW * 4;
+          mbar_arrive_tx(gfull + b, 2 * SLICE * 4 + PROW);
+          const float* gr = a.gsk + int64_t(pair / a.ns) * KS * SLICE;
+          for (int h = 0; h < 2; ++h) {  // columns j0 .. j0 + 127 span k_b rows j0 / 64 and j0 / 64 + 1
+            const int kb = kval(j0 / NV + h, NV);
+            bulk_g2s(g + h * SLICE * 4, gr + (kb < 0 ? -kb : kb) * SLICE, SLICE * 4, gfull + b);
+          }
+          bulk_g2s(g + 2 * SLICE * 4, a.gphase + pair * 3 * NV, PROW, gfull + b);
         }
-        bulk_g2s(g + 2 * SLICE * 4, a.gphase + pair * 3 * NV, PROW, gfull + b);
       }
     }
   }
@@ -345,17 +416,29 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static uint16_t host_bf16(float x) {  // round to nearest even (finite inputs)
-  uint32_t u;
-  memcpy(&u, &x, 4);
-  u += 0x7FFFu + ((u >> 16) & 1u);
-  return uint16_t(u >> 16);
+// IEEE half: round to nearest even, for |x| < 65504 (no overflow handling needed here)
+static uint16_t host_f16(double x) {
+  const uint16_t sign = x < 0 ? 0x8000 : 0;
+  double a = x < 0 ? -x : x;
+  if (a == 0.0) return sign;
+  int e = 0;
+  std::frexp(a, &e);  // a = m 2^e, m in [1/2, 1)
+  int E = e - 1;      // a = 1.f x 2^E
+  if (E < -14) E = -14;  // subnormal range: fixed spacing 2^-24
+  const double q = std::ldexp(a, 10 - E);  // value in units of the last place
+  double r = std::nearbyint(q);             // round half to even (default rounding mode)
+  if (r >= 2048.0) {                         // carried into the next binade
+    r /= 2.0;
+    ++E;
+  }
+  const uint32_t mant = uint32_t(r);
+  if (mant < 1024) return uint16_t(sign | mant);  // subnormal (E == -14)
+  return uint16_t(sign | (uint32_t(E + 15) << 10) | (mant - 1024));
 }
-static float host_bf16_f(uint16_t h) {
-  const uint32_t u = uint32_t(h) << 16;
-  float x;
-  memcpy(&x, &u, 4);
-  return x;
+static double host_f16_d(uint16_t h) {
+  const int E = (h >> 10) & 0x1F, m = h & 0x3FF;
+  const double v = E == 0 ? std::ldexp(double(m), -24) : std::ldexp(double(1024 + m), E - 25);
+  return (h & 0x8000) ? -v : v;
 }
 
 // F_even hi, lo, F_odd hi, lo images (rows o = 2 k' + part, K index kappa, K-major,
@@ -376,8 +459,8 @@ static void build_dft_images(std::vector<uint16_t>& img) {
           const CS w = cs_turn(m, NV);
           const double c = w.c, sn = dir * w.s;
           const double v = (o & 1) == 0 ? (kap < 32 ? c : -sn) : (kap < 32 ? sn : c);
-          const uint16_t h = host_bf16(float(v));
-          const uint16_t l = host_bf16(float(v - double(host_bf16_f(h))));
+          const uint16_t h = host_f16(v);
+          const uint16_t l = host_f16(v - host_f16_d(h));
           const uint32_t off = umma_kmajor_off(o, kap, SBO, LBO) / 2;
           hi[off] = h;
           lo[off] = l;
