@@ -226,7 +226,7 @@ def measure_n64(pkg, device, cells=256, cells_fp64=2):
                      f"hard spheres, e=e0={E64}, 3-Maxwellian mixtures", "cells": cells,
            "mixed": mixed, "unit": UNIT, "tuning": col.plan.tuning}
     # the two first-axis column paths side by side (32 cells each): in-register
-    # CUDA-core FFT and the tensor-core split-BF16 DFT
+    # CUDA-core FFT and the tensor-core split-FP16 DFT
     tuned = col.plan.tuning
     paths, q_path = {}, {}
     nc = min(cells, 32)

@@ -122,7 +122,7 @@ int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stre
  * First-axis column transforms of the n = 64 FP32 pipeline (no reference
  * counterpart; the reference calls FFTW / cuFFT for the whole 3D transform,
  * src/collision/inelastic_collisions.py:212-214): 0 = in-register CUDA-core
- * FFT, 1 = dense 64-point DFT on the tensor cores (tcgen05.mma, split-BF16
+ * FFT, 1 = 64-point DFT on the tensor cores (tcgen05.mma, column-scaled split-FP16
  * operands hi + lo, FP32 accumulation in tensor memory).  Path 1 exists for
  * n = 64, FP32, 3D plans only; the autotuner times both.  get: `stalled`
  * (may be NULL) receives 1 if a tensor-core CTA ever gave up waiting for its

@@ -209,7 +209,7 @@ class Plan:
             self.set_dft_path(dft_path)
 
     def set_dft_path(self, dft_path):
-        """'fft' (CUDA-core FFT) or 'tensor' (tensor-core split-BF16 DFT; n = 64
+        """'fft' (CUDA-core FFT) or 'tensor' (tensor-core split-FP16 DFT; n = 64
         FP32 plans) for the first-axis column transforms, ``pii_plan_set_dft_path``."""
         _lib.check(self._lib.pii_plan_set_dft_path(self.handle, DFT_PATHS[dft_path]), "pii_plan_set_dft_path")
 
