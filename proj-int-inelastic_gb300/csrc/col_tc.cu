@@ -113,6 +113,7 @@ struct ColTcArgs {
   const float2* ephase;  // [Q][3][64]
   const float2* gphase;  // [Q][3][64]
   const float* gsk;      // [n_r][|k_b| < 33][SLICE]: gsinc[r][k_b^2 + k_c^2 + k_a^2]
+  const float* colb;     // PSTART: [cells][N2] max over a of |f^(a, j)|_1 (k_col_bound)
   int ns;
   int64_t items, c0, p0, np;
   int* err;             // set to 1 if a role gave up waiting
@@ -207,6 +208,10 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = i & 1;
       const uint32_t u = uint32_t(i >> 1) & 1u;
+      // PSTART: the cell's column bound, in flight during the waits below
+      float cb = 0.f;
+      if constexpr (MODE == COL_PSTART)
+        cb = a.colb[(a.c0 + (tile / TILES_PER_ITEM) / a.np) * N2 + int(tile % TILES_PER_ITEM) * TN + n];
       // the raw tile is in and operand buffer b is free (MMAs of tile i - 2 done)
       const bool ok = mbar_wait_role(rfull + b, u, abort) && mbar_wait_role(xempty + b, u ^ 1u, abort);
       const float2* raw = reinterpret_cast<const float2*>(sm + OFF_R + b * RAW);
@@ -216,26 +221,29 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         const int j = int(tile % TILES_PER_ITEM) * TN + n;
         if (ok) ebc = cmul(ep[NV + (j >> 6)], ep[2 * NV + (j & 63)]);
       }
-      if (ok) {
-        // pass 1: this half's bound on |x0 e0 +- x1 e1| (L1 norms, no products of complex numbers)
-        float mb = 0.f;
+      float mx = 0.f;
+      if constexpr (MODE == COL_PSTART) {
+        // the cell's column bound (k_col_bound): |x0 e0 +- x1 e1| <= 2 max_a |f^(a, j)|_1 |e_a|_1 |e_bc|_1;
+        // the a-row phases have one modulus (exp(i phi) / n^3), so |e_0|_1 serves every a (a
+        // slightly low bound only moves the scaled values a little above 1: FP16 has the range)
+        if (!ok) break;  // no barrier in this mode: threads may leave one by one
+        mx = 2.f * cb * (1.001f * l1(ep[0])) * l1(ebc);
+      } else {
+        if (ok) {
+          // pass 1: this half's bound on |x0 +- x1| (L1 norms)
+          float mb = 0.f;
 #pragma unroll 8
-        for (int q = 0; q < 16; ++q) {
-          const int ap = 16 * h + q;
-          float t0 = l1(raw[ap * TN + n]), t1 = l1(raw[(ap + 32) * TN + n]);
-          if constexpr (MODE == COL_PSTART) {
-            t0 *= l1(ep[ap]);
-            t1 *= l1(ep[ap + 32]);
+          for (int q = 0; q < 16; ++q) {
+            const int ap = 16 * h + q;
+            mb = fmaxf(mb, l1(raw[ap * TN + n]) + l1(raw[(ap + 32) * TN + n]));
           }
-          mb = fmaxf(mb, t0 + t1);
+          xb[((i & 1) * 2 + h) * TN + n] = mb;
         }
-        xb[((i & 1) * 2 + h) * TN + n] = mb;
+        // exchange with the other half of the column; every exit of this loop is
+        // voted here, so the barrier never waits for a converter that left
+        if (bar_any<1, CONVERTERS>(!ok)) break;
+        mx = fmaxf(xb[((i & 1) * 2 + h) * TN + n], xb[((i & 1) * 2 + (h ^ 1)) * TN + n]);
       }
-      // exchange with the other half of the column; every exit of this loop is
-      // voted here, so the barrier never waits for a converter that left
-      if (bar_any<1, CONVERTERS>(!ok)) break;
-      float mx = fmaxf(xb[((i & 1) * 2 + h) * TN + n], xb[((i & 1) * 2 + (h ^ 1)) * TN + n]);
-      if constexpr (MODE == COL_PSTART) mx *= l1(ebc);
       // power of two bringing the bound into [1/2, 1): exponent arithmetic only
       const int ex = mx > 0.f ? int((__float_as_uint(mx) >> 23) & 0xFF) - 126 : 0;
       const float down = __uint_as_float(uint32_t(127 - ex) << 23), up = __uint_as_float(uint32_t(127 + ex) << 23);
@@ -413,6 +421,24 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
   }
 }
 
+// colb[cell][j] = max over a of |f^(a, j)|_1: the PSTART column bound (f^ is
+// the same for every pair of the cell)
+__global__ void __launch_bounds__(256) k_col_bound(const float2* fhat, float* colb, int64_t cells) {
+  using namespace ctc;
+  const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= cells * N2) return;
+  const int64_t cell = gid / N2;
+  const int j = int(gid - cell * N2);
+  const float2* x = fhat + cell * N3 + j;
+  float m = 0.f;
+#pragma unroll 8
+  for (int a0 = 0; a0 < NV; ++a0) {
+    const float2 v = x[a0 * N2];
+    m = fmaxf(m, fabsf(v.x) + fabsf(v.y));
+  }
+  colb[gid] = m;
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -533,7 +559,22 @@ int col_tc_prepare(pii_plan* p) {
     PII_CUDA(cudaMemcpy(p->dft_gs, gk.data(), gk.size() * sizeof(float), cudaMemcpyHostToDevice));
     p->bytes += int64_t(gk.size() * sizeof(float));
   }
+  if (!p->dft_colb) {
+    PII_CUDA(cudaMalloc(&p->dft_colb, size_t(p->batch_max) * N2 * sizeof(float)));
+    p->bytes += int64_t(p->batch_max) * N2 * sizeof(float);
+  }
   PII_CUDA(cudaDeviceGetAttribute(&p->dft_ctas, cudaDevAttrMultiProcessorCount, p->device));
+  return PII_OK;
+}
+
+int col_tc_bounds(pii_plan* p, int64_t cells, cudaStream_t s) {
+  using namespace ctc;
+  {
+    StageTimer st(p, ST_COL_FWD, s);
+    k_col_bound<<<unsigned((cells * N2 + 255) / 256), 256, 0, s>>>(static_cast<const float2*>(p->fhat),
+                                                                     static_cast<float*>(p->dft_colb), cells);
+  }
+  PII_CHECK_LAUNCH();
   return PII_OK;
 }
 
@@ -550,6 +591,7 @@ int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int
   a.ephase = static_cast<const float2*>(p->tab.ephase);
   a.gphase = static_cast<const float2*>(p->tab.gphase);
   a.gsk = static_cast<const float*>(p->dft_gs);
+  a.colb = static_cast<const float*>(p->dft_colb);
   a.ns = p->ns;
   a.items = items;
   a.c0 = c0;

@@ -24,6 +24,9 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
   using K = CollideKernels<T, NV>;
   const int64_t N = p->N;
   PII_TRY(K::fwd(p, f, 0, cells, s));
+  if constexpr (std::is_same<T, float>::value && NV == 64) {
+    if (p->dft_path == 1) PII_TRY(col_tc_bounds(p, cells, s));  // per-column scale bounds of f^
+  }
   if constexpr (std::is_same<T, float>::value && NV == 32) {
     if (p->gain_path >= 1 && p->gain_path <= 3) {
       if (p->gain_path == 1) {

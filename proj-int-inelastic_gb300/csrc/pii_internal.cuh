@@ -155,6 +155,7 @@ struct pii_plan {
   int* dft_err = nullptr;   // device word: 1 if a k_col_tc CTA gave up waiting for its MMAs
   int dft_ctas = 0;         // resident CTAs of k_col_tc (one per SM)
   void* dft_gs = nullptr;   // gsinc by (r, |k_b|, |k_c|, |k_a|) slices (TMA sources)
+  void* dft_colb = nullptr; // [batch_max][n^2] column bounds max_a |f^|_1 (k_col_bound)
   // TMA tensor maps (CUtensorMap, 128 bytes each) of f^ and of the chunk buffer
   // as 2D FP32 arrays [rows of 64 (a) per grid][8192 floats per row]
   alignas(128) unsigned char dft_tmap[2][128] = {};
@@ -201,6 +202,7 @@ int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // col_tc.cu: tensor-core first-axis DFT of the n = 64 FP32 pipeline
 int col_tc_prepare(pii_plan* p);
 int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int64_t np, cudaStream_t s);
+int col_tc_bounds(pii_plan* p, int64_t cells, cudaStream_t s);
 // transport.cu
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
                    double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);
