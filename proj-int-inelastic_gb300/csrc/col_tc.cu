@@ -223,11 +223,12 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       }
       float mx = 0.f;
       if constexpr (MODE == COL_PSTART) {
-        // the cell's column bound (k_col_bound): |x0 e0 +- x1 e1| <= 2 max_a |f^(a, j)|_1 |e_a|_1 |e_bc|_1;
-        // the a-row phases have one modulus (exp(i phi) / n^3), so |e_0|_1 serves every a (a
-        // slightly low bound only moves the scaled values a little above 1: FP16 has the range)
+        // the cell's column bound (k_col_bound): |x0 e0 +- x1 e1| <= 2 max_a |f^(a, j)|_1 |e_a| |e_bc|_1;
+        // the a-row phases exp(i phi) / n^3 share one modulus, |e_0| (FP32 rounding of the table
+        // can leave a bound a few ulp low: the scaled values then exceed 1 by as much, well
+        // inside FP16 range)
         if (!ok) break;  // no barrier in this mode: threads may leave one by one
-        mx = 2.f * cb * (1.001f * l1(ep[0])) * l1(ebc);
+        mx = 2.f * cb * (1.001f * sqrtf(ep[0].x * ep[0].x + ep[0].y * ep[0].y)) * l1(ebc);
       } else {
         if (ok) {
           // pass 1: this half's bound on |x0 +- x1| (L1 norms)
