@@ -14,7 +14,7 @@ cell-evaluations per step.
 
 Prints one JSON line (rank 0).  Under torchrun (N > 1) every rank runs an
 independent replica (the operator has no data-path collective; cells shard
-with a 2-cell halo, which a single-GPU pool cannot exercise).
+with a 2-cell halo, which one GPU cannot exercise).
 """
 import argparse
 import json
@@ -351,8 +351,8 @@ def run_reference(args):
                    "(bounded sample: alternating left/right Sod cells)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
                          "sample": f"{args.steps} single-cell Q(f,f) evaluations, FP64 NumPy/SciPy restatement of "
-                                   f"the reference operator (the reference itself cannot run on the GPU box: "
-                                   f"pyfftw/cupy absent), scipy.fft workers={workers}"},
+                                   f"the reference operator (the reference itself needs pyfftw/cupy, absent on the "
+                                   f"benchmark host), scipy.fft workers={workers}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -525,7 +525,7 @@ def main():
     N = NV**3
     items_per_collide = NX * NR * NS
     pass_flops = 5.0 * N * math.log2(NV)
-    # per (cell, pair) item; the fused kernel does the whole pair (survey's per-pair term 2*5N log2 N + 16 N)
+    # per (cell, pair) item; the fused kernel does the whole pair (direct-method term 2*5N log2 N + 16 N)
     per_item = {"pair_plane": 4 * pass_flops + 2 * N, "col_pstart": pass_flops + 12 * N,
                 "col_pend": pass_flops + 14 * N, "reduce": 2 * N,
                 "gain_cluster": 2 * 5.0 * N * math.log2(N) + 16 * N,
@@ -562,7 +562,7 @@ def main():
         if tkey in tr:
             roof["traffic"] = tr[tkey].get("dram_bytes_per_launch")
             roof["traffic_source"] = tr[tkey].get("source")
-    # whole-step FLOP rate (algorithmic F per cell-eval, survey formula) for context
+    # whole-step FLOP rate (algorithmic F = (2Q + n_r + 2) 5N log2 N + 16 Q N per cell-eval) for context
     F_cell = (2 * NR * NS + NR + 2) * 5 * N * math.log2(N) + 16 * NR * NS * N
     roof["step_algorithmic_tflops"] = F_cell * value / world / 1e12
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))

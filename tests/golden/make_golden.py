@@ -27,7 +27,7 @@ Run from the repository root:  ``python tests/golden/make_golden.py [stem ...]``
 (all fixtures, or only the named ones; the full set reproduces the committed
 files, the transport fixture drawing from the same generator after op_small).
 Needs the reference checkout (``PII_REFERENCE_ROOT``, default
-/root/reference); the GPU machine never runs this script.
+/root/reference); GPU test runs never execute this script.
 """
 import math
 import os
