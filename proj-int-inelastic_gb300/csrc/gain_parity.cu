@@ -40,7 +40,10 @@ constexpr int TMEM_COLS = 512;
 // without bank conflicts
 constexpr int FPITCH = 36;
 constexpr size_t FS_OFF = size_t(PLANES) * N2 * sizeof(float2);
-constexpr size_t SMEM = FS_OFF + size_t(PLANES) * 32 * FPITCH * sizeof(float) + 16;
+// packed mode: the current radial node's sinc slab gsxc[r] ([153][17] floats, 16-byte padded)
+constexpr int GSC = 153 * 17;
+constexpr size_t GSC_OFF = FS_OFF + size_t(PLANES) * 32 * FPITCH * sizeof(float);
+constexpr size_t SMEM = GSC_OFF + size_t((GSC + 3) / 4 * 4) * sizeof(float) + 16;
 }  // namespace gpar
 
 struct GainParityArgs {
@@ -51,6 +54,7 @@ struct GainParityArgs {
   const float2* epar;    // [Q][2][32]
   const float2* gpar;    // [Q][2][32]
   const float* gsx;      // [n_r][513][20]
+  const float* gsxc;     // [n_r][153][17] (packed mode)
   int ns, Q;
   int QP;                // passes per (cell, parity): Q, or the antipodal pairs when packed
   const int* reps;       // [QP] pair index of each packed pass (packed mode)
@@ -259,6 +263,16 @@ __device__ __forceinline__ void pack_stage_a_col(float2* W, const float2* fh, co
   });
 }
 
+// the column's 17 sinc values |k_a| = 0..16 from the radial node's slab in shared memory
+__device__ __forceinline__ void load_gsc(const float* slab, int j, float (&g)[20]) {
+  int u = kval(j >> 5, 32), v = kval(j & 31, 32);
+  u = u < 0 ? -u : u;
+  v = v < 0 ? -v : v;
+  const float* row = slab + ((u < v ? v * (v + 1) / 2 + u : u * (u + 1) / 2 + v) * 17);
+#pragma unroll
+  for (int q = 0; q < 17; ++q) g[q] = row[q];
+}
+
 // the column's 17 sinc values |k_a| = 0..16 (of 20 padded) from its radial row of gsx
 __device__ __forceinline__ void load_gsx(const float* gsr, int j, float (&g)[20]) {
   const int kb = kval(j >> 5, 32), kc = kval(j & 31, 32);
@@ -336,6 +350,8 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* W = reinterpret_cast<float2*>(smem_raw);
   float* fS = reinterpret_cast<float*>(smem_raw + FS_OFF);
+  float* gsc = reinterpret_cast<float*>(smem_raw + GSC_OFF);
+  int gsc_ir = -1;  // radial node whose slab is in gsc
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + SMEM - 16);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (warp == 0) {
@@ -387,6 +403,16 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
 
     for (int ip = p0; ip < p1; ++ip) {
       const int p = PACK ? a.reps[ip] : ip;
+      if constexpr (PACK) {
+        // the radial node's sinc slab: the previous item's stage C reads ended at its last
+        // barrier; the stage-A barrier below orders these writes before this item's reads
+        const int ir = p / a.ns;
+        if (ir != gsc_ir) {
+          const float* src = a.gsxc + int64_t(ir) * GSC;
+          for (int e = t; e < GSC; e += THREADS) gsc[e] = src[e];
+          gsc_ir = ir;
+        }
+      }
       // (per-pair pointers are formed inside each stage so that none stays
       // live across the register-heavy plane pass)
       // ---- A: the thread's two columns (those it also takes in stage C)
@@ -438,12 +464,12 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
           // |k_b|^2 + |k_c|^2 is the same for j and -j: one sinc row serves both
           // columns of a pair; only the self-conjugate columns differ
           float g[20];
-          load_gsx(gsr, uc.x, g);
+          load_gsc(gsc, uc.x, g);
           if (par == 0)
             pack_stage_c<0, 0>(W, uc.x, gp, g, treg0);
           else
             pack_stage_c<1, 0>(W, uc.x, gp, g, treg0);
-          if (uc.w) load_gsx(gsr, uc.y, g);
+          if (uc.w) load_gsc(gsc, uc.y, g);
           if (par == 0)
             pack_stage_c<0, 1>(W, uc.y, gp, g, treg0 + 64);
           else
@@ -547,7 +573,7 @@ __global__ void __launch_bounds__(256) k_herm_expand_par(float2* G, const float2
 // ---------------------------------------------------------------------------
 int gain_parity_prepare(pii_plan* p) {
   using namespace gpar;
-  if (!p->tab.epar || !p->tab.gpar || !p->tab.gsx || !p->gc_maps) {
+  if (!p->tab.epar || !p->tab.gpar || !p->tab.gsx || !p->tab.gsxc || !p->gc_maps) {
     set_error("gain_parity_prepare: parity tables or column map missing");
     return PII_ERR_ARG;
   }
@@ -625,6 +651,7 @@ int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s, bool packed) {
   a.epar = static_cast<const float2*>(p->tab.epar);
   a.gpar = static_cast<const float2*>(p->tab.gpar);
   a.gsx = static_cast<const float*>(p->tab.gsx);
+  a.gsxc = static_cast<const float*>(p->tab.gsxc);
   a.ns = p->ns;
   a.Q = p->Q;
   a.QP = QP;

@@ -69,12 +69,15 @@ enum Stage {
 //   gpar [Q][2][32] complex  : W^{p k} g_a[k]
 //   gsx  [n_r][513][20] real : gsinc[r][m_bc + q^2] for q = |k_a| <= 16 (0-padded),
 //                              m_bc = k_b^2 + k_c^2: one 80-byte row per column
+//   gsxc [n_r][153][17] real : the same rows by (|k_b|, |k_c|) pair u <= v, index
+//                              v (v + 1) / 2 + u (one radial node: 10.4 KB)
 struct Tables {
   void* ephase = nullptr;
   void* gphase = nullptr;
   void* epar = nullptr;
   void* gpar = nullptr;
   void* gsx = nullptr;
+  void* gsxc = nullptr;
   void* gsinc = nullptr;
   void* lossk = nullptr;
   void* lapl = nullptr;

@@ -175,6 +175,15 @@ static int upload_tables(pii_plan* p) {
         for (int q = 0; q <= 16 && mbc + q * q <= M; ++q)
           gsx[(size_t(ir) * 513 + mbc) * 20 + q] = gs[size_t(ir) * (M + 1) + mbc + q * q];
     PII_TRY(up2(&p->tab.gsx, gsx));
+    // the same by (|k_b|, |k_c|) pair, u = min <= v = max (index v (v + 1) / 2 + u, 153
+    // pairs), 17 values q = 0..16: one radial node's slab is 10.4 KB (shared memory)
+    std::vector<T> gsxc(size_t(nr) * 153 * 17, T(0));
+    for (int ir = 0; ir < nr; ++ir)
+      for (int v = 0; v <= 16; ++v)
+        for (int u = 0; u <= v; ++u)
+          for (int q = 0; q <= 16; ++q)
+            gsxc[(size_t(ir) * 153 + v * (v + 1) / 2 + u) * 17 + q] = gs[size_t(ir) * (M + 1) + u * u + v * v + q * q];
+    PII_TRY(up2(&p->tab.gsxc, gsxc));
   }
   for (int m = 0; m <= M; ++m) {
     lk[m] = T(lk_d[m]);
@@ -208,7 +217,7 @@ static void free_plan(pii_plan* p) {
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
   }
-  void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
+  void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsxc, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
                   p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag,
                   p->dft_img,    p->dft_err,    p->dft_gs,    p->dft_colb};
