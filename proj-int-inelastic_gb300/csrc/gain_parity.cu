@@ -620,8 +620,8 @@ int gain_parity_prepare(pii_plan* p) {
       PII_CUDA(cudaMemcpy(p->ap_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
       p->bytes += int64_t(reps.size() * sizeof(int));
       p->ap_count = int(reps.size());
-      // Nyquist-correction accumulators: cells x ceil(8 SMs / cells) <= 8 SMs + cells CTAs
-      const size_t nq = (size_t(8 * sms) + size_t(p->batch_max)) * 3 * N2 * sizeof(float2);
+      // Nyquist-correction accumulators: cells x ceil(16 SMs / cells) <= 16 SMs + cells CTAs
+      const size_t nq = (size_t(16 * sms) + size_t(p->batch_max)) * 3 * N2 * sizeof(float2);
       PII_CUDA(cudaMalloc(&p->nq_part, nq));
       p->bytes += int64_t(nq);
       PII_TRY(nyq_corr_prepare(p));

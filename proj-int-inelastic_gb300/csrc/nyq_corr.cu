@@ -378,9 +378,24 @@ int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.cells = cells;
   int sms = 0;
   PII_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
-  // about 8 waves of CTAs (one per SM), each with at least 16 antipodal pairs
-  // so that loading the cell's f into shared memory stays a small share
-  a.blocks = int(std::max<int64_t>(1, std::min<int64_t>(std::max(1, a.QP / 16), (8 * int64_t(sms) + cells - 1) / cells)));
+  // 8 to 16 waves of CTAs (one per SM), each with at least 16 antipodal pairs so
+  // that loading the cell's f into shared memory stays a small share; among
+  // those, the CTA count per cell whose last wave is fullest (128 cells on 152
+  // SMs: 19 per cell, 16 whole waves, instead of 10 and a 42 % last wave)
+  const int64_t bmax = std::max(1, a.QP / 16);
+  const int64_t blo = std::min<int64_t>(bmax, std::max<int64_t>(1, (8 * int64_t(sms) + cells - 1) / cells));
+  const int64_t bhi = std::min<int64_t>(bmax, std::max<int64_t>(blo, (16 * int64_t(sms) + cells - 1) / cells));
+  int64_t best = blo;
+  double best_idle = 2.0;
+  for (int64_t b = blo; b <= bhi; ++b) {
+    const int64_t ctas = cells * b, tail = ctas % sms;
+    const double idle = tail == 0 ? 0.0 : double(sms - tail) / double(ctas + sms - tail);
+    if (idle < best_idle - 1e-9) {
+      best_idle = idle;
+      best = b;
+    }
+  }
+  a.blocks = int(best);
   a.part = static_cast<float2*>(p->nq_part);
   {
     StageTimer st(p, ST_NYQ, s);

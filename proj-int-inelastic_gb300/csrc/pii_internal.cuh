@@ -150,7 +150,7 @@ struct pii_plan {
   void* gp_hpart = nullptr;  // its per-item Hermitian slots
   int* ap_reps = nullptr;    // device: representative pair of each antipodal pair (0 if the design is not symmetric)
   int ap_count = 0;
-  void* nq_part = nullptr;   // Nyquist-correction accumulators [<= 2 SMs + batch_max CTAs][3][1024]
+  void* nq_part = nullptr;   // Nyquist-correction accumulators [<= 16 SMs + batch_max CTAs][3][1024]
   // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core
   // FFT (k_col), 1 = tensor-core split-BF16 DFT (k_col_tc)
   int dft_path = 0;
