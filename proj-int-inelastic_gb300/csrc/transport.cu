@@ -26,42 +26,77 @@ struct DfArgs {
   int bc_lo, bc_hi, transport;
 };
 
+// tvd.limit (src/limiters/tvd.py:6-40): r = (upwind wave u * w) / w^2 (0 where
+// w^2 == 0), minmod phi = max(0, min(1, r)), limited wave phi * w.  Written
+// without the division (FP64 divisions are software sequences and FP64
+// throughput bounds the transport kernel on this part): phi * w is 0 where u
+// and w differ in sign (r <= 0), w where |u| >= |w| (r >= 1), else u (r w =
+// u up to the rounding of r) -- within 2 ulp of the divided form.  A NaN wave
+// gives w, as the divided form does (fmin(1, NaN) = 1).
 __device__ __forceinline__ double limited_wave(double w, double wl, double wr, double s) {
-  // tvd.limit: r = (upwind wave * w) / w^2 (0 where w^2 == 0), minmod phi = max(0, min(1, r))
-  const double den = w * w;
-  double r = 0.0;
-  if (den != 0.0) r = (s > 0.0 ? w * wl : wr * w) / den;
-  const double phi = fmax(0.0, fmin(1.0, r));
-  return (w == 0.0) ? w : phi * w;
+  const double u = s > 0.0 ? wl : wr;
+  if (w == 0.0 || u * w <= 0.0) return (w == 0.0) ? w : 0.0;
+  return fabs(u) < fabs(w) ? u : w;
 }
 
-__global__ void __launch_bounds__(256) k_df(DfArgs a) {
-  const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (gid >= a.nx * a.N) return;
-  const int64_t c = gid / a.N;
-  const int64_t j = gid - c * a.N;
-  double d = 0.0;
-  if (a.transport) {
-    const double s = a.v1[j / a.N2];
-    // ghost cells: extrapolation copies the edge cell, periodic wraps (any nx >= 1)
-    auto at = [&](int64_t ci) -> double {
-      if (ci < 0) ci = (a.bc_lo == PII_BC_PERIODIC) ? ((ci % a.nx) + a.nx) % a.nx : 0;
-      if (ci >= a.nx) ci = (a.bc_hi == PII_BC_PERIODIC) ? ci % a.nx : a.nx - 1;
-      return a.f[ci * a.N + j];
-    };
-    const double fm2 = at(c - 2), fm1 = at(c - 1), f0 = a.f[c * a.N + j], fp1 = at(c + 1), fp2 = at(c + 2);
-    const double wm2 = fm1 - fm2, wm1 = f0 - fm1, w0 = fp1 - f0, wp1 = fp2 - fp1;
-    const double dtdx = a.dtdx;
-    d = -dtdx * (fmin(s, 0.0) * w0 + fmax(s, 0.0) * wm1);
-    const double sabs = fabs(s);
-    const double om = 1.0 - sabs * dtdx;
-    const double cf = 0.5 * sabs * om;
-    const double Fl = cf * limited_wave(wm1, wm2, w0, s);
+// ghost cell index: extrapolation copies the edge cell, periodic wraps (any nx >= 1)
+__device__ __forceinline__ int64_t ghost_cell(int64_t ci, int64_t nx, int bc_lo, int bc_hi) {
+  if (ci < 0) {
+    if (bc_lo != PII_BC_PERIODIC) return 0;
+    while (ci < 0) ci += nx;
+  }
+  if (ci >= nx) {
+    if (bc_hi != PII_BC_PERIODIC) return nx - 1;
+    while (ci >= nx) ci -= nx;
+  }
+  return ci;
+}
+
+// One thread per velocity point walks the cells in x with a 5-cell window: each
+// f value is loaded once and each interface flux F_{i+1/2} is computed once
+// (cell i's right flux is cell i + 1's left flux; the same expressions, so the
+// values are those of a per-cell evaluation).  FP64 throughput bounds this
+// kernel on this part, so per-point work is what counts.
+__global__ void __launch_bounds__(128) k_df(DfArgs a) {
+  const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;  // velocity point
+  if (j >= a.N) return;
+  const int64_t nx = a.nx, N = a.N;
+  if (!a.transport) {
+    for (int64_t c = 0; c < nx; ++c) {
+      const int64_t gid = c * N + j;
+      a.df[gid] = a.q ? a.q[gid] * (a.dt / a.kn) : 0.0;
+    }
+    return;
+  }
+  const double s = a.v1[j / a.N2];
+  const double dtdx = a.dtdx;
+  const double qs = a.dt / a.kn;  // dt Q / kn as Q (dt / kn): a multiply per point, not a division
+  const double sabs = fabs(s);
+  const double om = 1.0 - sabs * dtdx;
+  const double cf = 0.5 * sabs * om;
+  const double* fj = a.f + j;
+  auto fat = [&](int64_t ci) { return fj[ghost_cell(ci, nx, a.bc_lo, a.bc_hi) * N]; };
+  const double fm2 = fat(-2), fm1 = fat(-1), f0 = fj[0];
+  double fp1 = fat(1), fp2 = fat(2);
+  double wm2 = fm1 - fm2, wm1 = f0 - fm1, w0 = fp1 - f0, wp1 = fp2 - fp1;
+  double Fl = cf * limited_wave(wm1, wm2, w0, s);
+  for (int64_t c = 0; c < nx; ++c) {
+    const int64_t gid = c * N + j;
+    double d = -dtdx * (fmin(s, 0.0) * w0 + fmax(s, 0.0) * wm1);
     const double Fr = cf * limited_wave(w0, wm1, wp1, s);
     d -= dtdx * (Fr - Fl);
+    if (a.q) d += a.q[gid] * qs;
+    a.df[gid] = d;
+    if (c + 1 < nx) {  // slide: the waves of cell c + 1 (differences of the same values)
+      fp1 = fp2;
+      fp2 = fat(c + 3);
+      wm2 = wm1;
+      wm1 = w0;
+      w0 = wp1;
+      wp1 = fp2 - fp1;
+      Fl = Fr;
+    }
   }
-  if (a.q) d += a.dt * a.q[gid] / a.kn;
-  a.df[gid] = d;
 }
 
 __global__ void __launch_bounds__(256) k_axpy3(double* f, const double* d, double s0, double s1, double s2,
@@ -242,10 +277,9 @@ int transport_impl(pii_plan* p, const double* f, const double* q, double* df, in
   a.dtdx = dx > 0.0 ? dt / dx : 0.0;
   a.bc_lo = bc_lo;
   a.bc_hi = bc_hi;
-  const int64_t total = nx * p->N;
   {
     StageTimer st(p, ST_DF, s);
-    k_df<<<unsigned((total + 255) / 256), 256, 0, s>>>(a);
+    k_df<<<unsigned((p->N + 127) / 128), 128, 0, s>>>(a);
   }
   PII_CHECK_LAUNCH();
   return PII_OK;
