@@ -1,6 +1,6 @@
 // Column pass along the first velocity axis of the n = 64 pipeline on the
 // tensor cores: the 64-point DFT of every (b, c) column as a dense GEMM with
-// split-BF16 operands and FP32 accumulation in tensor memory.
+// split-FP16 operands and FP32 accumulation in tensor memory.
 //
 // One item (cell, pair) is a 64 x 4096 complex array X[a][j] (j = (b, c)); its
 // transform along a, Y[k][j] = sum_a W^{k a} X[a][j] with W = exp(DIR 2 pi i / 64)
@@ -81,7 +81,7 @@ constexpr int ISSUER_WARP = (CONVERTERS + EPILOGUE) / 32, TMA_WARP = ISSUER_WARP
 constexpr int THREADS = CONVERTERS + EPILOGUE + 64;
 constexpr int TN = 128;                     // columns per tile (MMA M)
 constexpr int TILES_PER_ITEM = N2 / TN;     // 32
-constexpr uint32_t SBO = 1024, LBO = 128;   // K = 64 bf16 per row: 8 core matrices of 128 B
+constexpr uint32_t SBO = 1024, LBO = 128;   // K = 64 16-bit elements per row: 8 core matrices of 128 B
 constexpr int FOP = 64 * 64 * 2;            // bytes of one 64 x 64 FP16 matrix F_g (hi or lo)
 constexpr int FIMG = 4 * FOP;               // F_even hi, F_even lo, F_odd hi, F_odd lo
 constexpr int RAW = NV * TN * 8;            // one raw tile: 64 rows of 128 complex columns

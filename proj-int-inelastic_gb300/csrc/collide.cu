@@ -111,7 +111,8 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
 // Autotuner: time the candidate kernel choices for `cells` cells on scratch
 // inputs and keep the fastest.  Candidates: gain path (a-parity / cluster /
 // pipeline, where the fused kernels exist), work items per resident cluster or
-// CTA, pipeline chunk size.
+// CTA, pipeline chunk size, and for n = 64 FP32 plans the column-transform
+// path (CUDA-core FFT or tensor-core DFT).
 extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stream) {
   using namespace pii;
   if (!plan || cells <= 0 || cells > plan->batch_max) {
@@ -129,7 +130,8 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
     set_error("pii_plan_autotune: out of memory");
     return PII_ERR_CUDA;
   }
-  // a smooth positive state: 1 + small ramp (values do not change the timing)
+  // zeros: no kernel branches on the values (a zero column of the tensor-core
+  // DFT takes scale 1 and the same MMAs), so they do not change the timing
   cudaMemsetAsync(f, 0, bytes, s);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -244,7 +246,7 @@ extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
 
 extern "C" int pii_plan_set_dft_path(pii_plan* plan, int path) {
   if (!plan || path < 0 || path > 1) {
-    pii::set_error("pii_plan_set_dft_path: path must be 0 (CUDA-core FFT) or 1 (tensor-core split-BF16 DFT)");
+    pii::set_error("pii_plan_set_dft_path: path must be 0 (CUDA-core FFT) or 1 (tensor-core split-FP16 DFT)");
     return PII_ERR_ARG;
   }
   if (path == 1 && !plan->dft_img) {

@@ -152,7 +152,7 @@ struct pii_plan {
   int ap_count = 0;
   void* nq_part = nullptr;   // Nyquist-correction accumulators [<= 16 SMs + batch_max CTAs][3][1024]
   // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core
-  // FFT (k_col), 1 = tensor-core split-BF16 DFT (k_col_tc)
+  // FFT (k_col), 1 = tensor-core split-FP16 DFT (k_col_tc)
   int dft_path = 0;
   void* dft_img = nullptr;  // DFT matrix images (A_hi | A_lo) for DIR = +1 and -1
   int* dft_err = nullptr;   // device word: 1 if a k_col_tc CTA gave up waiting for its MMAs

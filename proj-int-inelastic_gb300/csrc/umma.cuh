@@ -3,7 +3,7 @@
 // the issue / commit instructions and a bounded mbarrier wait.
 //
 // Operand layout used throughout ("K-major, no swizzle"): a matrix of R rows
-// (M or N) by K bf16 elements is stored as 8 x 8 core matrices of 128
+// (M or N) by K 16-bit elements (bf16 or fp16) is stored as 8 x 8 core matrices of 128
 // contiguous bytes (8 rows of 16 bytes); core matrix (r / 8, k / 8) sits at
 // (r / 8) * SBO + (k / 8) * LBO bytes from the operand's start, element
 // (r % 8, k % 8) at 16 (r % 8) + 2 (k % 8) within it.

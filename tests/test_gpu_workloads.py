@@ -127,7 +127,7 @@ def test_large_grid_n64_full_quadrature():
 
 def test_large_grid_n64_tensor_core_dft():
     """The first-axis column transforms of the n = 64 pipeline on the tensor
-    cores (split-BF16 DFT, FP32 accumulation) against the FP64 path, next to
+    cores (split-FP16 DFT, FP32 accumulation) against the FP64 path, next to
     the CUDA-core FFT path; the full 48 x 70 quadrature on two cells."""
     pkg = _pkg()
     s = 20.0 / (3.0 + math.sqrt(2.0))  # L = 10
