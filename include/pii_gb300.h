@@ -147,6 +147,16 @@ int pii_collide(pii_plan* plan, const double* f, double* q, int64_t cells, int w
                 double heat_bath, int mass_fix, void* stream);
 
 /*
+ * out = Lap_v f per cell, the spectral Laplacian Re IFFT(-pi^2 |k|^2 / L^2 FFT(f))
+ * of FSInelasticVHSCollision.laplacian (src/collision/inelastic_collisions.py:
+ * 229-230, the table of :69), with the transforms of pii_collide in the plan's
+ * working precision (FP64 plans: FP64).  pii_collide adds heat_bath times the
+ * same term inside its own final transform.  f and out: cells x n^dim FP64
+ * device arrays (may not alias).
+ */
+int pii_laplacian(pii_plan* plan, const double* f, double* out, int64_t cells, void* stream);
+
+/*
  * Transport increment of the second-order upwind + minmod TVD scheme in x,
  * df = -dt/dx (A-dq + A+dq) - dt/dx (F_{i+1/2} - F_{i-1/2}), two ghost cells.
  * Replaces BoltzmannSolver1D.df_advection (src/boltzmann.py:177-205) with the

@@ -50,6 +50,7 @@ SIGNATURES = {
     "pii_plan_set_dft_path": (_c_int, [_vp, _c_int]),
     "pii_plan_get_dft_path": (_c_int, [_vp, _pint, _pint]),
     "pii_collide": (_c_int, [_vp, _vp, _vp, _c_i64, _c_int, _c_dbl, _c_int, _vp]),
+    "pii_laplacian": (_c_int, [_vp, _vp, _vp, _c_i64, _vp]),
     "pii_transport_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _vp]),
     "pii_boltzmann_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _c_dbl, _c_int,
                                   _c_int, _vp]),

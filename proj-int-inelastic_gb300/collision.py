@@ -348,15 +348,19 @@ class FSInelasticVHSCollision:
         pin[0].numpy()[...] = a
         return pin[0].to(f"cuda:{self._device}", non_blocking=True), True
 
-    def _run(self, input_f, with_loss, heat_bath):
+    def _run(self, input_f, with_loss, heat_bath, laplacian=False):
         f, was_np = self._as_device(input_f)
         lead = f.shape[:-self.ndim]
         cells = int(np.prod(lead)) if len(lead) else 1
         plan = self._ensure_plan(cells)
         q = torch.empty_like(f)
-        st = plan._lib.pii_collide(plan.handle, f.data_ptr(), q.data_ptr(), cells, int(bool(with_loss)),
-                                   float(heat_bath or 0.0), int(self.mass_fix), _stream_handle())
-        _lib.check(st, "pii_collide")
+        if laplacian:
+            st = plan._lib.pii_laplacian(plan.handle, f.data_ptr(), q.data_ptr(), cells, _stream_handle())
+            _lib.check(st, "pii_laplacian")
+        else:
+            st = plan._lib.pii_collide(plan.handle, f.data_ptr(), q.data_ptr(), cells, int(bool(with_loss)),
+                                       float(heat_bath or 0.0), int(self.mass_fix), _stream_handle())
+            _lib.check(st, "pii_collide")
         self._input_shape = tuple(f.shape)
         if was_np:
             out = self._pinned[tuple(f.shape)][1]
@@ -378,10 +382,10 @@ class FSInelasticVHSCollision:
         return self._run(input_f, with_loss, 0.0)
 
     def laplacian(self, input_f):
-        """Heat-bath Laplacian (src/collision/inelastic_collisions.py:229-230)."""
-        with_hb = self._run(input_f, False, 1.0)
-        gain = self._run(input_f, False, 0.0)
-        return with_hb - gain
+        """Heat-bath Laplacian (src/collision/inelastic_collisions.py:229-230):
+        one forward and one inverse transform in the plan's precision
+        (``pii_laplacian``)."""
+        return self._run(input_f, False, 0.0, laplacian=True)
 
     def close(self):
         if self._plan is not None:

@@ -65,6 +65,28 @@ static int collide_n(pii_plan* p, const double* f, double* q, int64_t cells, int
   }
 }
 
+// Lap_v f alone: the forward transform, a zero gain sum and the finishing
+// inverse transform with heat_bath = 1 and no loss term
+template <typename T, int NV>
+static int laplacian_t(pii_plan* p, const double* f, double* out, int64_t cells, cudaStream_t s) {
+  PII_TRY((CollideKernels<T, NV>::fwd(p, f, 0, cells, s)));
+  PII_CUDA(cudaMemsetAsync(p->G, 0, size_t(cells) * size_t(p->N) * 2 * sizeof(T), s));
+  return finish_all<T, NV>(p, f, out, cells, 0, 1.0, s);
+}
+
+template <typename T>
+static int laplacian_n(pii_plan* p, const double* f, double* out, int64_t cells, cudaStream_t s) {
+  switch (p->n) {
+    case 8: return laplacian_t<T, 8>(p, f, out, cells, s);
+    case 16: return laplacian_t<T, 16>(p, f, out, cells, s);
+    case 24: return laplacian_t<T, 24>(p, f, out, cells, s);
+    case 32: return laplacian_t<T, 32>(p, f, out, cells, s);
+    case 48: return laplacian_t<T, 48>(p, f, out, cells, s);
+    case 64: return laplacian_t<T, 64>(p, f, out, cells, s);
+    default: set_error("laplacian: unsupported n = %d", p->n); return PII_ERR_ARG;
+  }
+}
+
 int prepare_impl(pii_plan* p) {
   if (p->dim == 2) return PII_OK;  // the 2D kernels set their attributes on first use
   const bool f32 = p->precision == PII_PREC_FP32;
@@ -276,6 +298,29 @@ extern "C" int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stall
     }
   }
   return PII_OK;
+}
+
+extern "C" int pii_laplacian(pii_plan* plan, const double* f, double* out, int64_t cells, void* stream) {
+  using namespace pii;
+  if (!plan || !f || !out) {
+    set_error("pii_laplacian: NULL argument");
+    return PII_ERR_ARG;
+  }
+  if (cells <= 0 || cells > plan->batch_max) {
+    set_error("pii_laplacian: cells = %lld outside [1, batch_max = %lld]", (long long)cells,
+              (long long)plan->batch_max);
+    return PII_ERR_SIZE;
+  }
+  if (f == out) {
+    set_error("pii_laplacian: f and out must not alias");
+    return PII_ERR_ARG;
+  }
+  PII_CUDA(cudaSetDevice(plan->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool f32 = plan->precision == PII_PREC_FP32;
+  if (plan->dim == 2)
+    return f32 ? laplacian2d_f32(plan, f, out, cells, s) : laplacian2d_f64(plan, f, out, cells, s);
+  return f32 ? laplacian_n<float>(plan, f, out, cells, s) : laplacian_n<double>(plan, f, out, cells, s);
 }
 
 extern "C" int pii_collide(pii_plan* plan, const double* f, double* q, int64_t cells, int with_loss,

@@ -252,6 +252,22 @@ struct Collide2D {
     return PII_OK;
   }
 
+  // Lap_v f alone: forward transform, zero gain sum, finishing pass with heat_bath = 1, no loss
+  static int laplacian(pii_plan* p, const double* f, double* out, int64_t cells, cudaStream_t s) {
+    using V = c2<T>;
+    constexpr int PPB = Geo2<NV>::PPB, TH = Geo2<NV>::THREADS;
+    PII_TRY(prepare());
+    const int smem = PPB * NV * Geo2<NV>::LD * int(sizeof(V));
+    const unsigned cell_blocks = unsigned((cells + PPB - 1) / PPB);
+    k2_fwd<T, NV><<<cell_blocks, TH, smem, s>>>(f, static_cast<V*>(p->fhat), static_cast<T*>(p->fT), cells);
+    PII_CHECK_LAUNCH();
+    PII_CUDA(cudaMemsetAsync(p->G, 0, size_t(cells) * size_t(Geo2<NV>::N2) * sizeof(V), s));
+    k2_finish<T, NV><<<cell_blocks, TH, smem, s>>>(static_cast<const V*>(p->G), static_cast<const V*>(p->fhat), f,
+                                                    out, cells, 0, 1.0, p->tab);
+    PII_CHECK_LAUNCH();
+    return PII_OK;
+  }
+
   static int run(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb, cudaStream_t s) {
     using V = c2<T>;
     constexpr int N2 = Geo2<NV>::N2, PPB = Geo2<NV>::PPB, TH = Geo2<NV>::THREADS;

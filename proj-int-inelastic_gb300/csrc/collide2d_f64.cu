@@ -16,4 +16,16 @@ int collide2d_f64(pii_plan* p, const double* f, double* q, int64_t cells, int wi
   }
 }
 
+int laplacian2d_f64(pii_plan* p, const double* f, double* out, int64_t cells, cudaStream_t s) {
+  switch (p->n) {
+    case 8: return Collide2D<double, 8>::laplacian(p, f, out, cells, s);
+    case 16: return Collide2D<double, 16>::laplacian(p, f, out, cells, s);
+    case 24: return Collide2D<double, 24>::laplacian(p, f, out, cells, s);
+    case 32: return Collide2D<double, 32>::laplacian(p, f, out, cells, s);
+    case 48: return Collide2D<double, 48>::laplacian(p, f, out, cells, s);
+    case 64: return Collide2D<double, 64>::laplacian(p, f, out, cells, s);
+    default: set_error("laplacian (2D): unsupported n = %d", p->n); return PII_ERR_ARG;
+  }
+}
+
 }  // namespace pii

@@ -196,6 +196,8 @@ int gain_cluster_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // collide2d_f32.cu / collide2d_f64.cu: the 2D-velocity operator
 int collide2d_f32(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb, cudaStream_t s);
 int collide2d_f64(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb, cudaStream_t s);
+int laplacian2d_f32(pii_plan* p, const double* f, double* out, int64_t cells, cudaStream_t s);
+int laplacian2d_f64(pii_plan* p, const double* f, double* out, int64_t cells, cudaStream_t s);
 // gain_parity.cu
 int gain_parity_prepare(pii_plan* p);
 int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s, bool packed);

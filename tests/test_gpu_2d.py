@@ -45,6 +45,24 @@ def test_operator_2d_golden(golden, case, precision, tol):
     assert rel_linf(q0.cpu().numpy(), d[f"case{case}_gain"][0]) < tol
 
 
+@pytest.mark.parametrize("precision,tol", [("double", 1e-12), ("mixed", 1e-5)])
+def test_laplacian_2d_vs_oracle(precision, tol):
+    """``laplacian`` (src/collision/inelastic_collisions.py:229-230) of a 2D
+    plan through pii_laplacian against the oracle's FP64 spectral Laplacian."""
+    from oracle import fs_inelastic as fo
+
+    pkg = _pkg()
+    nv, s = 32, 16.0 / (3.0 + math.sqrt(2.0))
+    m = fo.Mesh(nv, s, 4, dim=2, nphi=8)
+    op = fo.FSInelasticVHS(m, 0.8, 0.8, 0.0)
+    x, y = np.meshgrid(m.v, m.v, indexing="ij")
+    f = np.stack([np.exp(-((x - 0.5) ** 2 + y**2) / 2.0), 0.5 * np.exp(-(x**2 + (y + 1.0) ** 2) / 1.5)])
+    ref = op.laplacian(f)
+    cfg = config_2d(nv, s, 4, 8, 0.8, 0.8, 0.0)
+    col = pkg.FSInelasticVHSCollision(cfg, pkg.SpectralMesh(cfg), precision=precision)
+    assert rel_linf(col.laplacian(f), ref) < tol
+
+
 def test_cooling_law_2d_maxwell_molecules():
     """-dT/dt = (1 - e^2) rho T / 4 in 2D as well (the law CONSP_M integrates,
     src/boltzmann.py:103-105), on the GPU FP64 path."""

@@ -45,6 +45,27 @@ def test_operator_small_golden(golden, case, precision):
 
 
 @pytest.mark.parametrize("precision", ["double", "mixed"])
+@pytest.mark.parametrize("nv", [16, 32])
+def test_laplacian_vs_oracle(nv, precision):
+    """``laplacian`` (src/collision/inelastic_collisions.py:229-230) through
+    pii_laplacian against the oracle's FP64 spectral Laplacian: two cells,
+    NumPy in / out and torch in / out."""
+    from oracle import fs_inelastic as fo
+
+    m = fo.Mesh(nv, L8_S, 4, 6)
+    op = fo.FSInelasticVHS(m, 0.8, 0.8, 1.0)
+    f = np.stack([maxwellian(m.v, 1.0, (0.5, -0.3, 0.2), 1.2), maxwellian(m.v, 0.7, (-1.0, 1.0, 0.0), 0.6)])
+    ref = op.laplacian(f)
+    sm, col = _op((nv, 4, 6, 0.8, 0.8, 1.0, L8_S), precision)
+    assert rel_linf(col.laplacian(f), ref) < TOL[precision]
+    ft = torch.as_tensor(f, device="cuda:0")
+    lt = col.laplacian(ft)
+    assert isinstance(lt, torch.Tensor) and lt.is_cuda and lt.shape == ft.shape
+    assert rel_linf(lt.cpu().numpy(), ref) < TOL[precision]
+    assert rel_linf(col.laplacian(f[1]), ref[1]) < TOL[precision]  # (n, n, n) input
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
 def test_operator_c32_two_beam_golden(golden, precision):
     d = golden("op_c32.npz")
     sm, col = _op(d["params"], precision)
