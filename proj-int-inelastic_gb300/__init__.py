@@ -8,10 +8,11 @@ sm_103a CUDA kernels in ``libpii_gb300.so`` (C ABI: ``include/pii_gb300.h``).
 from . import _lib
 from .collision import FSInelasticVHSCollision, Plan, SpectralMesh, get_sphrquadrule
 from .ensemble import Ensemble
-from .solver import (BC, BoltzmannFastSweep, BoltzmannSolver, BoltzmannSolver0D, BoltzmannSolver1D,
-                     IterativeBoltzmannSolver, Solution, Solver, State)
+from .solver import (BC, BoltzmannFastSweep, BoltzmannSolver, BoltzmannSolver0D, BoltzmannSolver1D, Grid,
+                     IterativeBoltzmannSolver, Solution, Solver, State, maxwellian)
 
 __all__ = [
     "BC", "BoltzmannFastSweep", "BoltzmannSolver", "Ensemble", "BoltzmannSolver0D", "BoltzmannSolver1D", "FSInelasticVHSCollision",
-    "IterativeBoltzmannSolver", "Plan", "Solution", "Solver", "SpectralMesh", "State", "get_sphrquadrule",
+    "Grid", "IterativeBoltzmannSolver", "Plan", "Solution", "Solver", "SpectralMesh", "State", "get_sphrquadrule",
+    "maxwellian",
 ]

@@ -2,13 +2,18 @@
 
 * ``BC``, ``Solver``, ``BoltzmannSolver``, ``BoltzmannSolver1D`` keep the
   attributes and methods of src/solver.py:1-146 and src/boltzmann.py:16-205
-  (``kn``, ``dt``, ``time_integrator`` in {"Euler", "PFE", "TPI2", "TPI3"},
-  ``inner_steps``, ``inner_dt``, ``bc_lower`` / ``bc_upper`` / ``all_bcs``,
-  ``step``, ``df``, ``df_advection``, ``evolve_to_time``).
+  (``kn``, ``dt``, ``time_integrator`` in {"Euler", "PFE", "TPI2", "TPI3",
+  "CONSP", "CONSP_M"}, ``inner_steps``, ``inner_dt``, ``bc_lower`` /
+  ``bc_upper`` / ``all_bcs``, ``step`` and the per-integrator ``euler_step``,
+  ``proj_euler_step``, ``tel_proj_step2``, ``tel_proj_step3``,
+  ``convex_splitting_step``, ``convex_splitting_maxwellian_step``, ``df``,
+  ``df_advection``, ``evolve_to_time``), and ``maxwellian`` of
+  src/boltzmann.py:9-13.
 * ``State`` / ``Solution`` hold f as a torch CUDA FP64 tensor of shape
   (n_x, n, n, n) or (n_x, n, n) (3D or 2D velocity; no n_x for a
-  space-homogeneous problem), with FP64 moments ``rho``, ``u``, ``T``
-  (src/state.py, src/solution.py).
+  space-homogeneous problem), with FP64 moments ``rho``, ``u``, ``T``, the
+  reference's helpers and ``state.grid`` (``Grid``: per-axis cells, centres,
+  nodes, ``c_centers``) (src/state.py, src/solution.py, src/geometry.py).
 * ``IterativeBoltzmannSolver`` keeps ``solve`` / ``step``
   (src/iter_solver.py:9-35); ``BoltzmannFastSweep`` is its Gauss-Seidel
   upwind sweep (src/iter_solver.py:38-62) on the GPU.
@@ -30,6 +35,19 @@ from .collision import FSInelasticVHSCollision
 
 _INTEGRATORS = {"Euler": _lib.INT_EULER, "PFE": _lib.INT_PFE, "TPI2": _lib.INT_TPI2, "TPI3": _lib.INT_TPI3}
 _LEVELS = {"Euler": 0, "PFE": 1, "TPI2": 2, "TPI3": 3}
+_METHODS = {"Euler": "euler_step", "PFE": "proj_euler_step", "TPI2": "tel_proj_step2", "TPI3": "tel_proj_step3",
+            "CONSP": "convex_splitting_step", "CONSP_M": "convex_splitting_maxwellian_step"}
+
+
+def maxwellian(vx, vy, rho, u, T):
+    """The reference solver's ``maxwellian`` (src/boltzmann.py:9-13): the 2D
+    Maxwellian with bulk velocity (u, 0) for per-cell rho, u, T on the velocity
+    coordinates vx, vy (e.g. ``state.c_centers[1:]``); NumPy, or torch tensors."""
+    rho = rho[:, None, None]
+    u = u[:, None, None]
+    T = T[:, None, None]
+    exp = torch.exp if isinstance(vx, torch.Tensor) else np.exp
+    return rho / (2 * math.pi * T) * exp(-((vx - u) ** 2 + vy**2) / (2 * T))
 
 
 class BC:
@@ -37,32 +55,136 @@ class BC:
     periodic = _lib.BC_PERIODIC
 
 
+class Grid:
+    """The state's grid (src/geometry.py:45-172, one ``Dimension`` per axis, x
+    axes first, then velocity): per-axis ``num_cells``, ``lower``, ``upper``,
+    ``delta``, ``centers``, ``nodes`` (lists over the axes), ``num_dim``,
+    ``num_dim_x``, and ``c_centers`` / ``c_nodes``, the per-axis coordinates
+    broadcast over the whole grid (host NumPy, built on first use as the
+    reference does)."""
+
+    def __init__(self, num_cells, lower, upper, num_dim_x):
+        self.num_cells = [int(n) for n in num_cells]
+        self.lower = [float(x) for x in lower]
+        self.upper = [float(x) for x in upper]
+        self.num_dim_x = int(num_dim_x)
+        # Dimension.delta / centers / nodes (src/geometry.py:176-194)
+        self.delta = [(u - lo) / float(n) for lo, u, n in zip(self.lower, self.upper, self.num_cells)]
+        self._c_centers = None
+        self._c_nodes = None
+
+    @property
+    def num_dim(self):
+        return len(self.num_cells)
+
+    @property
+    def centers(self):
+        return [np.array([lo + (i + 0.5) * d for i in range(n)])
+                for lo, d, n in zip(self.lower, self.delta, self.num_cells)]
+
+    @property
+    def nodes(self):
+        return [np.array([lo + i * d for i in range(n + 1)]) for lo, d, n in zip(self.lower, self.delta, self.num_cells)]
+
+    @property
+    def c_centers(self):
+        if self._c_centers is None:
+            self._c_centers = list(np.meshgrid(*self.centers, indexing="ij"))
+        return self._c_centers
+
+    @property
+    def c_nodes(self):
+        if self._c_nodes is None:
+            self._c_nodes = list(np.meshgrid(*self.nodes, indexing="ij"))
+        return self._c_nodes
+
+
 class State:
-    """Phase-space state: f on the GPU, FP64 (src/state.py:6-122)."""
+    """Phase-space state: f on the GPU, FP64 (src/state.py:6-122).  Grid
+    attributes (``num_cells``, ``lower``, ``upper``, ``delta``, ``centers``,
+    ``nodes``, ``c_centers``, ``c_nodes``, ``num_dim``, ``num_dim_x``) are read
+    from ``state.grid`` as in the reference (src/state.py:10-29)."""
+
+    _GRID_KEYS = ("num_dim", "num_dim_x", "c_centers", "c_nodes", "num_cells", "lower", "upper", "delta", "centers",
+                  "nodes")
 
     def __init__(self, num_cells, lower, upper, num_dim_x, device=0):
-        self.num_cells = list(num_cells)
-        self.lower = list(lower)
-        self.upper = list(upper)
-        self.num_dim_x = int(num_dim_x)
-        self.delta = [(u - lo) / n for lo, u, n in zip(self.lower, self.upper, self.num_cells)]
+        self.grid = Grid(num_cells, lower, upper, num_dim_x)
         self.device = int(device)
         self.t = 0.0
-        self.f = torch.zeros(self.num_cells, dtype=torch.float64, device=f"cuda:{self.device}")
         self.problem_data = {}
+        self.f = self.new_array().zero_()
 
-    def centers(self, axis):
-        lo, d, n = self.lower[axis], self.delta[axis], self.num_cells[axis]
-        return np.array([lo + (i + 0.5) * d for i in range(n)])
+    def __getattr__(self, key):
+        grid = self.__dict__.get("grid")
+        if grid is not None and key in State._GRID_KEYS:
+            return getattr(grid, key)
+        raise AttributeError(f"'State' object has no attribute '{key}'")
+
+    def new_array(self):
+        """An uninitialised f of the grid's shape (src/state.py:66-69): FP64 on the state's GPU."""
+        return torch.empty(self.grid.num_cells, dtype=torch.float64, device=f"cuda:{self.device}")
+
+    def get_f_global(self):
+        """A copy of f (src/state.py:88-89)."""
+        return self.f.clone()
+
+    def sum_f(self, f):
+        """Velocity integral per cell (src/state.py:91-92, written there for 2D
+        velocity): the sum over the dim_v velocity axes times the cell volume.
+        Torch in -> torch out, NumPy in -> NumPy out."""
+        d = self.dim_v
+        axes = tuple(range(-d, 0))
+        vol = 1.0
+        for dv in self.grid.delta[-d:]:
+            vol *= dv
+        if isinstance(f, torch.Tensor):
+            return f.sum(dim=axes) * vol
+        return np.sum(f, axis=axes) * vol
+
+    def set_f_from_fbc(self, num_ghost, fbc):
+        """f = the interior of the ghosted array fbc (src/state.py:94-107)."""
+        if self.grid.num_dim_x == 1:
+            self.f = fbc[num_ghost:-num_ghost]
+        elif self.grid.num_dim_x == 2:
+            self.f = fbc[num_ghost:-num_ghost, num_ghost:-num_ghost]
+        else:
+            raise Exception("Assumption (1 <= num_dim_x <= 2) violated.")
+
+    def get_fbc_from_f(self, num_ghost, fbc):
+        """Copy f into the interior of fbc (src/state.py:109-120)."""
+        if self.grid.num_dim_x == 1:
+            fbc[num_ghost:-num_ghost] = self.f
+        elif self.grid.num_dim_x == 2:
+            fbc[num_ghost:-num_ghost, num_ghost:-num_ghost] = self.f
+        else:
+            raise Exception("Assumption (1 <= num_dim <= 2) violated.")
+
+    def __copy__(self):
+        new = State.__new__(State)
+        new.__dict__.update(self.__dict__)
+        return new
+
+    def __deepcopy__(self, memo):
+        """A new state with copies of the grid, t, problem_data and f (src/state.py:74-86)."""
+        import copy
+
+        new = State.__new__(State)
+        new.grid = copy.deepcopy(self.grid, memo)
+        new.device = self.device
+        new.t = self.t
+        new.problem_data = copy.deepcopy(self.problem_data, memo)
+        new.f = self.f.clone()
+        return new
 
     @property
     def dim_v(self):
-        return len(self.num_cells) - self.num_dim_x
+        return self.grid.num_dim - self.grid.num_dim_x
 
     @property
     def v(self):
         """Velocity centres (same on every velocity axis)."""
-        return self.centers(self.num_dim_x)
+        return self.grid.centers[self.grid.num_dim_x]
 
     @property
     def v1(self):
@@ -70,7 +192,7 @@ class State:
 
     @property
     def dv(self):
-        return self.delta[self.num_dim_x]
+        return self.grid.delta[self.grid.num_dim_x]
 
     def moments(self):
         """FP64 (rho, u[dim], T) per cell from ``pii_moments``: State.rho / u / T
@@ -172,10 +294,22 @@ class Solution:
     def f(self):
         return self.state.f
 
+    @property
+    def grid(self):
+        return self.state.grid
+
+    def set_all_states(self, attr, value, overwrite=True):
+        """src/solution.py:36-38."""
+        if getattr(self.state, attr) is None or overwrite:
+            setattr(self.state, attr, value)
+
     def __getattr__(self, key):
-        if key in ("rho", "u", "T", "num_cells", "lower", "upper", "delta", "num_dim_x", "v", "dim_v"):
-            return getattr(self.state, key)
-        raise AttributeError(key)
+        if key in ("rho", "u", "T", "num_dim", "num_dim_x", "c_nodes", "c_centers", "num_cells", "lower", "upper",
+                   "delta", "centers", "nodes", "v", "dim_v", "problem_data"):
+            state = self.__dict__.get("state")
+            if state is not None:
+                return getattr(state, key)
+        raise AttributeError(f"'Solution' object has no attribute '{key}'")
 
 
 class Solver:
@@ -300,6 +434,38 @@ class BoltzmannSolver(Solver):
                 raise ValueError("The penalty parameter, e or tau are not given. Please specify it!")
         elif ti not in _INTEGRATORS:
             raise NotImplementedError("This time integrator is not implemented.")
+        getattr(self, _METHODS[ti])(solution, take_one_step, tstart, tend)
+        self._steps_done = getattr(self, "_steps_done", 0) + 1
+        if self.check_every and self._steps_done % self.check_every == 0:
+            self.check_state(state)
+
+    # the reference's per-integrator steps (src/boltzmann.py:82-158), each one
+    # macro-step of self.dt whatever self.time_integrator names
+    def euler_step(self, solution, take_one_step, tstart, tend):
+        """f += df(dt) (src/boltzmann.py:82-84)."""
+        self._integrate(solution.state, "Euler")
+
+    def convex_splitting_step(self, solution, take_one_step, tstart, tend):
+        """f += dt / (kn + P dt) Q(f), then f += transport(f, dt) (src/boltzmann.py:86-94)."""
+        self._integrate(solution.state, "CONSP")
+
+    def convex_splitting_maxwellian_step(self, solution, take_one_step, tstart, tend):
+        """CONSP plus the penalised Maxwellian relaxation term (src/boltzmann.py:96-118)."""
+        self._integrate(solution.state, "CONSP_M")
+
+    def proj_euler_step(self, solution, take_one_step, tstart, tend):
+        """K inner Euler steps of inner_dt[0], then f += (dt / inner_dt[0] - K) df (src/boltzmann.py:120-128)."""
+        self._integrate(solution.state, "PFE")
+
+    def tel_proj_step2(self, solution, take_one_step, tstart, tend):
+        """Two-level telescopic projective step (src/boltzmann.py:130-140)."""
+        self._integrate(solution.state, "TPI2")
+
+    def tel_proj_step3(self, solution, take_one_step, tstart, tend):
+        """Three-level telescopic projective step (src/boltzmann.py:142-158)."""
+        self._integrate(solution.state, "TPI3")
+
+    def _integrate(self, state, ti):
         if isinstance(self.collision, FSInelasticVHSCollision):
             if ti in ("CONSP", "CONSP_M"):
                 self._fused_splitting(state, ti)
@@ -309,9 +475,6 @@ class BoltzmannSolver(Solver):
             if ti == "CONSP_M":
                 raise NotImplementedError("CONSP_M needs the GB300 collision operator")
             self._generic_step(state, ti)
-        self._steps_done = getattr(self, "_steps_done", 0) + 1
-        if self.check_every and self._steps_done % self.check_every == 0:
-            self.check_state(state)
 
     def check_state(self, state):
         """FP64 guard: raise FloatingPointError if f holds NaN / Inf, and
@@ -380,7 +543,8 @@ class BoltzmannSolver(Solver):
         f = state.f
         dt, K, h = self.dt, self.inner_steps, self.inner_dt
         if ti == "CONSP":
-            f += dt / (self.kn + self.penalty * dt) * self._q(state)
+            if self.collision is not None:
+                f += dt / (self.kn + self.penalty * dt) * self._q(state)
             f += self.df_advection(state, dt)
         elif ti == "Euler":
             f += self.df(state, dt)

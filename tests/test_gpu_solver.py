@@ -243,3 +243,66 @@ def test_state_guard_detects_nonfinite_and_mass_drift():
     solver._mass0 = None
     solver.evolve_to_time(sol, sol.t + 4e-3)
     assert torch.isfinite(sol.f).all()
+
+
+@pytest.mark.parametrize("name,integ,method", [("pfe", "PFE", "proj_euler_step"), ("tpi2", "TPI2", "tel_proj_step2"),
+                                               ("euler", "Euler", "euler_step")])
+def test_per_integrator_methods_fused(golden, name, integ, method):
+    """The reference's per-integrator methods (src/boltzmann.py:82-158) on the
+    GB300 operator: one call of e.g. ``proj_euler_step`` is the macro-step
+    ``step`` runs for that ``time_integrator`` (the same native call), and
+    matches the reference's run over its time span."""
+    pkg = _pkg()
+    d = golden("solver1d.npz")
+    nv, nr, ns, e, e0, g, s, nx = d["params"]
+    cfg = op_config(nv, s, nr, ns, e, e0, g)
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="double")
+    dt, tend, kn, dx = d[f"{name}_meta"]
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": int(nx), "nv": int(nv)})
+    sol.state.f.copy_(torch.as_tensor(d[f"{name}_f0"]))
+    solver = pkg.BoltzmannSolver1D(float(kn), collision_operator=col)
+    solver.all_bcs = pkg.BC.extrap if name != "tpi2" else pkg.BC.periodic
+    solver.time_integrator = "Euler" if integ != "Euler" else "PFE"  # the method runs its own integrator
+    solver.inner_steps = [int(k) for k in d[f"{name}_K"]]
+    solver.inner_dt = [float(h) for h in d[f"{name}_h"]]
+    solver.dt = float(dt)
+    solver.setup(sol)
+    steps = int(round((float(tend)) / float(dt)))
+    for _ in range(steps):
+        getattr(solver, method)(sol, False, 0.0, float(tend))
+    torch.cuda.synchronize()
+    assert rel_linf(sol.f.cpu().numpy(), d[f"{name}_f"]) < 1e-11
+
+
+def test_state_helpers_and_grid():
+    """State / Solution helpers of the reference (src/state.py:31-120,
+    src/solution.py:36-46, src/geometry.py): grid attributes, sum_f against the
+    FP64 moments, get_f_global and deepcopy as copies, ghost-array copies."""
+    import copy
+
+    pkg = _pkg()
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": 8.0, "nx": 4, "nv": 8})
+    st = sol.state
+    assert sol.grid is st.grid and st.num_dim == 4 and st.num_dim_x == 1 and sol.num_cells == [4, 8, 8, 8]
+    _, vx, vy, vz = st.c_centers
+    f0 = np.exp(-((vx - 0.3) ** 2 + vy**2 + vz**2) / 2.0) * (1.0 + st.c_centers[0])
+    st.f.copy_(torch.as_tensor(f0))
+    rho = st.sum_f(st.f)
+    assert isinstance(rho, torch.Tensor) and rho.shape == (4,)
+    assert np.abs(rho.cpu().numpy() - st.rho).max() < 1e-12 * np.abs(st.rho).max()
+    assert np.allclose(st.sum_f(f0), st.rho, rtol=1e-12, atol=0)
+    g = st.get_f_global()
+    g += 1.0
+    assert torch.equal(st.f, torch.as_tensor(f0, device=st.f.device))
+    st2 = copy.deepcopy(st)
+    st2.f += 1.0
+    assert torch.equal(st.f, torch.as_tensor(f0, device=st.f.device)) and st2.grid is not st.grid
+    fbc = torch.zeros((8, 8, 8, 8), dtype=torch.float64, device=st.f.device)
+    st.get_fbc_from_f(2, fbc)
+    assert torch.equal(fbc[2:-2], st.f) and float(fbc[:2].abs().max()) == 0.0
+    st.set_f_from_fbc(2, fbc)
+    assert torch.equal(st.f, fbc[2:-2])
+    sol.set_all_states("t", 0.25)
+    assert sol.t == 0.25 and st.t == 0.25
+    assert st.new_array().shape == (4, 8, 8, 8)
