@@ -165,6 +165,12 @@ GAIN_PATHS = {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3}
 DFT_PATHS = {"fft": 0, "tensor": 1}
 
 
+def _code(table, name, what):
+    if name not in table:
+        raise ValueError(f"{what} must be one of {sorted(table)}, got {name!r}")
+    return table[name]
+
+
 class Plan:
     """Owner of one ``pii_plan`` (device tables + workspace for batch_max cells)."""
 
@@ -190,7 +196,8 @@ class Plan:
         self.handle = h.value
         self._lib = lib
         if gain_path is not None:
-            _lib.check(lib.pii_plan_set_gain_path(self.handle, GAIN_PATHS[gain_path]), "pii_plan_set_gain_path")
+            _lib.check(lib.pii_plan_set_gain_path(self.handle, _code(GAIN_PATHS, gain_path, "gain_path")),
+                       "pii_plan_set_gain_path")
 
     def autotune(self, cells):
         """Time the kernel choices for `cells` cells and keep the fastest
@@ -203,15 +210,16 @@ class Plan:
     def set_tuning(self, gain_path, items_per_cluster, chunk_points, dft_path=None, **_):
         """Restore choices (as returned by :attr:`tuning`), ``pii_plan_set_tuning``
         (and ``pii_plan_set_dft_path`` when `dft_path` is given)."""
-        _lib.check(self._lib.pii_plan_set_tuning(self.handle, GAIN_PATHS[gain_path], int(items_per_cluster),
-                                                 int(chunk_points)), "pii_plan_set_tuning")
+        _lib.check(self._lib.pii_plan_set_tuning(self.handle, _code(GAIN_PATHS, gain_path, "gain_path"),
+                                                 int(items_per_cluster), int(chunk_points)), "pii_plan_set_tuning")
         if dft_path is not None:
             self.set_dft_path(dft_path)
 
     def set_dft_path(self, dft_path):
         """'fft' (CUDA-core FFT) or 'tensor' (tensor-core split-FP16 DFT; n = 64
         FP32 plans) for the first-axis column transforms, ``pii_plan_set_dft_path``."""
-        _lib.check(self._lib.pii_plan_set_dft_path(self.handle, DFT_PATHS[dft_path]), "pii_plan_set_dft_path")
+        _lib.check(self._lib.pii_plan_set_dft_path(self.handle, _code(DFT_PATHS, dft_path, "dft_path")),
+                   "pii_plan_set_dft_path")
 
     @property
     def dft_stalled(self):
@@ -267,10 +275,12 @@ class FSInelasticVHSCollision:
     * ``mass_fix``   -- subtract the per-cell mean of Q in FP64 (k = 0 mode);
     * ``batch_max``  -- initial cell capacity of the plan (grown on demand);
     * ``device``     -- CUDA device index;
-    * ``gain_path``  -- "parity" (fused a-parity kernel with a tensor-memory
-      accumulator, the default for n = 32 in mixed precision), "cluster" (fused
-      2-CTA-cluster kernel, n = 32 mixed) or "pipeline" (column / plane passes,
-      every case); all evaluate the same operator.
+    * ``gain_path``  -- for n = 32 in mixed precision: "packed" (the fused
+      a-parity kernel on antipodal direction pairs plus the Nyquist-plane
+      correction, the default where the design is antipodally symmetric),
+      "parity" (fused a-parity kernel with a tensor-memory accumulator, the
+      default otherwise) or "cluster" (fused 2-CTA-cluster kernel); "pipeline"
+      (column / plane passes) in every case.  All evaluate the same operator.
     """
 
     collision_model = "vhs"

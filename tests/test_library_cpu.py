@@ -156,6 +156,9 @@ def test_python_tuning_maps():
 
     assert collision.GAIN_PATHS == {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3}
     assert collision.DFT_PATHS == {"fft": 0, "tensor": 1}
+    assert collision._code(collision.GAIN_PATHS, "packed", "gain_path") == 3
+    with pytest.raises(ValueError, match="gain_path must be one of"):
+        collision._code(collision.GAIN_PATHS, "fast", "gain_path")
     assert set(pkg._lib.SIGNATURES) >= {"pii_plan_set_dft_path", "pii_plan_get_dft_path"}
 
 
