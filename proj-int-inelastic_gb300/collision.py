@@ -17,6 +17,7 @@ path: ``device`` is accepted for signature compatibility only.
 """
 import math
 import os
+import re
 
 import numpy as np
 import torch
@@ -26,25 +27,71 @@ from . import _lib
 _DESIGNS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "sphere_designs.npz")
 
 
-def get_sphrquadrule(sstype, rule=None, npts=None, qdeg=None):
-    """Symmetric spherical design by point count or strength.
+class SphericalQuadRule:
+    """A spherical quadrature rule: ``pts`` (m x 3 unit vectors) and ``wts``
+    (one weight per point, or empty when the rule carries none), the two
+    attributes of the reference's rule objects
+    (src/collision/spherical_design/__init__.py:7-40)."""
 
-    Mirrors ``get_sphrquadrule`` (src/collision/spherical_design/__init__.py:91-116)
-    for the stored Womersley symmetric designs: select by ``npts`` (exact) or
-    the smallest design with strength >= ``qdeg``.  ``rule`` may also be an
-    (m, 3) array of unit vectors (a tabulated rule).
+    def __init__(self, pts, wts=()):
+        self.pts = np.asarray(pts, np.float64).reshape(-1, 3)
+        self.wts = np.asarray(wts, np.float64).reshape(-1)
+
+
+def _parse_tabulated(text):
+    """Points (and optional weights) of a tabulated rule: one record ``x y z``
+    or ``x y z w`` per line or per parenthesised group, numbers separated by
+    blanks or commas, optionally enclosed in [ ] (the text format read at
+    src/collision/spherical_design/__init__.py:8-40)."""
+    body = text.strip()
+    if body.startswith("[") and body.endswith("]"):
+        body = body[1:-1]
+    records = re.findall(r"\(([^()]*)\)", body) if "(" in body else body.splitlines()
+    pts, wts = [], []
+    for rec in records:
+        vals = [float(x) for x in rec.replace(",", " ").split()]
+        if not vals:
+            continue
+        if len(vals) == 3:
+            pts.append(vals)
+        elif len(vals) == 4:
+            pts.append(vals[:3])
+            wts.append(vals[3])
+        else:
+            raise ValueError("Invalid points in quadrature rule")
+    if wts and len(wts) != len(pts):
+        raise ValueError("Invalid number of weights")
+    return SphericalQuadRule(pts, wts)
+
+
+def get_sphrquadrule(sstype, rule=None, npts=None, qdeg=None, flags=None):
+    """Symmetric spherical design, as ``get_sphrquadrule``
+    (src/collision/spherical_design/__init__.py:91-116): returns a rule with
+    ``pts`` / ``wts``.
+
+    * ``rule`` a name (``"womersley"``, or None): the stored Womersley
+      symmetric design with exactly ``npts`` points (the strongest if several),
+      or the one with the fewest points of strength >= ``qdeg``;
+    * ``rule`` a tabulated rule (text of ``x y z [w]`` records), or an (m, 3)
+      array of unit vectors: that point set, checked against ``npts``.
     """
     if sstype != "symmetric":
         raise ValueError(f"unknown spherical design type {sstype!r}")
+    tabulated = None
     if rule is not None and not isinstance(rule, str):
-        pts = np.asarray(rule, np.float64).reshape(-1, 3)
-        if npts and npts != len(pts):
+        tabulated = SphericalQuadRule(rule)
+    elif rule and not re.fullmatch(r"[A-Za-z0-9_\-~+]+", rule):
+        tabulated = _parse_tabulated(rule)
+    if tabulated is not None:
+        if npts and npts != len(tabulated.pts):
             raise ValueError("Invalid number of points in provided rule")
-        return pts
-    if rule not in (None, "womersley"):
-        raise ValueError("No suitable spherical quadrature rule found")
+        if qdeg and not len(tabulated.wts):
+            raise ValueError("Provided rule has no quadrature weights")
+        return tabulated
     if not npts and not qdeg:
         raise ValueError("Must specify either npts or qdeg")
+    if rule not in (None, "", "womersley"):
+        raise ValueError("No suitable spherical quadrature rule found")
     d = np.load(_DESIGNS)
     best = None
     for key in d.files:
@@ -57,7 +104,7 @@ def get_sphrquadrule(sstype, rule=None, npts=None, qdeg=None):
                 best = (key, m, q)
     if best is None:
         raise ValueError("No suitable spherical quadrature rule found")
-    return d[best[0]].copy()
+    return SphericalQuadRule(d[best[0]].copy())
 
 
 class SpectralMesh:
@@ -87,7 +134,7 @@ class SpectralMesh:
             sp = config["spherical-design-rule"]
             self._ssrule = sp.get("ssrule", "womersley")
             self._nsphr = int(sp["nsphr"])
-            self._spts = get_sphrquadrule("symmetric", rule=sp.get("points", self._ssrule), npts=self._nsphr)
+            self._spts = get_sphrquadrule("symmetric", rule=sp.get("points", self._ssrule), npts=self._nsphr).pts
             self._wspts = 4 * math.pi / self._nsphr
         else:
             raise ValueError("Dimension must be 2 or 3.")

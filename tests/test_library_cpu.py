@@ -1,5 +1,6 @@
 """CPU-side checks of the C-ABI library and the host layer (no GPU compute)."""
 import ctypes
+import math
 import os
 import re
 
@@ -82,13 +83,47 @@ def test_spectral_mesh_matches_oracle():
 def test_sphere_design_selection():
     import proj_int_inelastic_gb300 as pkg
 
-    assert pkg.get_sphrquadrule("symmetric", "womersley", npts=32).shape == (32, 3)
+    r32 = pkg.get_sphrquadrule("symmetric", "womersley", npts=32)
+    assert r32.pts.shape == (32, 3) and r32.wts.shape == (0,)
     # smallest design of strength >= 8 is the 48-point strength-9 design
-    assert pkg.get_sphrquadrule("symmetric", "womersley", qdeg=8).shape == (48, 3)
+    assert pkg.get_sphrquadrule("symmetric", "womersley", qdeg=8).pts.shape == (48, 3)
     with pytest.raises(ValueError):
         pkg.get_sphrquadrule("symmetric", "womersley", npts=64)  # no 64-point rule exists
+    with pytest.raises(ValueError, match="Must specify"):
+        pkg.get_sphrquadrule("symmetric", "womersley")
     pts = np.eye(3)
-    assert np.array_equal(pkg.get_sphrquadrule("symmetric", pts, npts=3), pts)
+    assert np.array_equal(pkg.get_sphrquadrule("symmetric", pts, npts=3).pts, pts)
+
+
+def test_tabulated_sphere_rules():
+    """Tabulated rules given as text (src/collision/spherical_design/__init__.py:
+    8-40,94-109): records per line or per parenthesised group, optional weights;
+    the reference's checks on counts and weights."""
+    import proj_int_inelastic_gb300 as pkg
+
+    pts = np.array([[1.0, 0.0, 0.0], [-1.0, 0.0, 0.0], [0.0, 0.6, 0.8], [0.0, -0.6, -0.8]])
+    lines = "\n".join(" ".join(repr(float(x)) for x in p) for p in pts)
+    for text in (lines, "\n" + lines + "\n\n",
+                 ", ".join("(" + ", ".join(repr(float(x)) for x in p) + ")" for p in pts),
+                 "[" + ", ".join("(" + ", ".join(repr(float(x)) for x in p) + ")" for p in pts) + "]"):
+        r = pkg.get_sphrquadrule("symmetric", text, npts=4)
+        assert np.array_equal(r.pts, pts) and r.wts.shape == (0,), text
+    w = "\n".join(" ".join(repr(float(x)) for x in p) + " 3.14159" for p in pts)
+    r = pkg.get_sphrquadrule("symmetric", w, qdeg=1)
+    assert np.array_equal(r.pts, pts) and np.all(r.wts == 3.14159)
+    with pytest.raises(ValueError, match="Invalid number of points"):
+        pkg.get_sphrquadrule("symmetric", lines, npts=6)
+    with pytest.raises(ValueError, match="no quadrature weights"):
+        pkg.get_sphrquadrule("symmetric", lines, qdeg=2)
+    with pytest.raises(ValueError, match="Invalid points"):
+        pkg.get_sphrquadrule("symmetric", "1 0\n0 1")
+    with pytest.raises(ValueError, match="Invalid number of weights"):
+        pkg.get_sphrquadrule("symmetric", "1 0 0 0.5\n0 1 0")
+    # a tabulated rule in the config drives the mesh (a 4-direction design)
+    cfg = op_config(16, L8_S, 4, 4, 0.9, 0.9, 1.0)
+    cfg["spherical-design-rule"]["ssrule"] = lines
+    sig, wsig = pkg.SpectralMesh(cfg).circ_or_sphr_quad()
+    assert np.array_equal(sig, pts) and wsig == math.pi
 
 
 def test_config_errors():
