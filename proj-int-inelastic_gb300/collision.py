@@ -406,6 +406,12 @@ class FSInelasticVHSCollision:
         return pin[0].to(f"cuda:{self._device}", non_blocking=True), True
 
     def _run(self, input_f, with_loss, heat_bath, laplacian=False):
+        n, d = self.sm.nv, self.ndim
+        if len(input_f.shape) >= d and tuple(input_f.shape[-d:]) == (n,) * d and int(np.prod(input_f.shape)) == 0:
+            # an empty batch of cells: an empty result, as the reference's transforms give
+            if isinstance(input_f, torch.Tensor):
+                return torch.empty(tuple(input_f.shape), dtype=torch.float64, device=input_f.device)
+            return np.empty(tuple(input_f.shape), dtype=np.float64)
         f, was_np = self._as_device(input_f)
         lead = f.shape[:-self.ndim]
         cells = int(np.prod(lead)) if len(lead) else 1

@@ -66,6 +66,32 @@ def test_laplacian_vs_oracle(nv, precision):
 
 
 @pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_conservation_and_dissipation(precision):
+    """Moments of Q = Q+ - Q- on a two-beam state at n = 32: mass and momentum
+    are conserved to spectral accuracy for any e, energy for e = 1, and e < 1
+    dissipates energy.  (The oracle gives, as fractions of the scale
+    sum |Q| (1 + |v|^2) dv: mass 2e-5, momentum 1.5e-5, energy 7e-5 at e = 1,
+    and an energy moment of -0.17 at e = 0.8.)"""
+    for e in (1.0, 0.8):
+        sm, col = _op((32, 16, 32, e, e, 1.0, L8_S), precision)
+        v = sm.v_center
+        f = maxwellian(v, 1.0, (0.8, 0.0, 0.0), 0.8) + maxwellian(v, 1.0, (-0.8, 0.2, 0.0), 1.0)
+        q = col.collide(f, with_loss=True)
+        V = np.meshgrid(v, v, v, indexing="ij")
+        dv = sm.delta**3
+        v2 = V[0] ** 2 + V[1] ** 2 + V[2] ** 2
+        scale = (np.abs(q) * (1 + v2)).sum() * dv
+        mass = q.sum() * dv / scale
+        mom = [(q * V[i]).sum() * dv / scale for i in range(3)]
+        energy = (q * v2 / 2).sum() * dv / scale
+        assert abs(mass) < 1e-4 and max(abs(x) for x in mom) < 1e-4, (e, mass, mom)
+        if e == 1.0:
+            assert abs(energy) < 2e-4, energy
+        else:
+            assert energy < -0.1, energy
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
 def test_operator_c32_two_beam_golden(golden, precision):
     d = golden("op_c32.npz")
     sm, col = _op(d["params"], precision)

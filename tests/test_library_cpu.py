@@ -144,6 +144,14 @@ def test_config_errors():
     assert col.precision == "mixed" and col.default_with_loss is False
     cfg2 = dict(cfg, config={"precision": "double"})
     assert pkg.FSInelasticVHSCollision(cfg2, sm).precision == "double"
+    # an empty batch gives an empty result without touching a GPU; wrong trailing axes raise
+    for shape in ((0, 16, 16, 16), (3, 0, 16, 16, 16)):
+        out = col(np.empty(shape))
+        assert isinstance(out, np.ndarray) and out.shape == shape and out.dtype == np.float64
+        assert col.collide(np.empty(shape), with_loss=True).shape == shape
+        assert col.laplacian(np.empty(shape)).shape == shape
+    with pytest.raises(ValueError):
+        col(np.empty((0, 8, 8, 8)))
 
 
 def test_solver_host_logic():
