@@ -404,10 +404,12 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
     for (int ip = p0; ip < p1; ++ip) {
       const int p = PACK ? a.reps[ip] : ip;
       if constexpr (PACK) {
-        // the radial node's sinc slab: the previous item's stage C reads ended at its last
-        // barrier; the stage-A barrier below orders these writes before this item's reads
+        // the radial node's sinc slab (every 16 passes; ir is the same in every thread):
+        // the barrier ends the previous item's stage C reads of the old slab, the
+        // stage-A barrier below orders these writes before this item's reads
         const int ir = p / a.ns;
         if (ir != gsc_ir) {
+          __syncthreads();
           const float* src = a.gsxc + int64_t(ir) * GSC;
           for (int e = t; e < GSC; e += THREADS) gsc[e] = src[e];
           gsc_ir = ir;
@@ -479,8 +481,13 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
           par_stage_c<1>(W, uc.y, gp, gpp, gsr, treg0 + 64);
         }
       }
-      __syncthreads();  // the next pair's stage A overwrites the planes
+      // No barrier here: a thread's stage A of the next pair writes exactly the
+      // plane entries (its columns j and -j, all 16 planes) that its own stage C
+      // has just read, and its accumulator lanes are its own, so threads may run
+      // ahead into the next pair's loads; the barrier after stage A orders the
+      // planes before the plane pass.
     }
+    __syncthreads();  // every stage C has read the planes before they hold the parked slots
     // ---- write the work item's Hermitian slots (x 1/2; packed: x 1, its
     // coefficient is 2 s).  Every thread of a
     // warp issues the same TMEM loads (they are warp-collective); values are
