@@ -242,13 +242,13 @@ __global__ void __launch_bounds__(Geo2<NV>::THREADS) k2_finish(const c2<T>* G, c
 template <typename T, int NV>
 struct Collide2D {
   static int prepare() {
-    static bool done = false;
-    if (done) return PII_OK;
+    static PerDeviceOnce once;
+    if (once.done()) return PII_OK;
     const int bytes = Geo2<NV>::PPB * NV * Geo2<NV>::LD * int(sizeof(c2<T>));
     PII_CUDA(cudaFuncSetAttribute(k2_fwd<T, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     PII_CUDA(cudaFuncSetAttribute(k2_pair<T, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     PII_CUDA(cudaFuncSetAttribute(k2_finish<T, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    done = true;
+    once.set();
     return PII_OK;
   }
 

@@ -352,13 +352,13 @@ __global__ void __launch_bounds__(256) k_reduce(c2<T>* G, const c2<T>* buf, int6
 template <typename T, int NV>
 static int set_smem_attrs() {
   using V = c2<T>;
-  static bool done = false;
-  if (done) return PII_OK;
+  static PerDeviceOnce once;
+  if (once.done()) return PII_OK;
   const int bytes = Geo<NV>::PPB * NV * Geo<NV>::LD * int(sizeof(V));
   PII_CUDA(cudaFuncSetAttribute(k_fwd_plane<T, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   PII_CUDA(cudaFuncSetAttribute(k_pair_plane<T, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   PII_CUDA(cudaFuncSetAttribute(k_finish<T, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  done = true;
+  once.set();
   return PII_OK;
 }
 

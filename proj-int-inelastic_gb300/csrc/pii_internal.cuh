@@ -18,6 +18,20 @@ void set_error(const char* fmt, ...);
 // kernels enqueued by the library (eager launches + kernel nodes of graph replays)
 extern std::atomic<int64_t> g_launches;
 
+// Once per device: kernel attributes (cudaFuncSetAttribute) belong to the
+// current device, so a process with plans on several GPUs sets them on each.
+struct PerDeviceOnce {
+  std::atomic<uint64_t> mask{0};
+  bool done() const {
+    int d = 0;
+    return cudaGetDevice(&d) == cudaSuccess && d >= 0 && d < 64 && (mask.load() >> d & 1u);
+  }
+  void set() {
+    int d = 0;
+    if (cudaGetDevice(&d) == cudaSuccess && d >= 0 && d < 64) mask.fetch_or(uint64_t(1) << d);
+  }
+};
+
 // modes of the first-axis column pass (collide_kernels.cuh, col_tc.cu)
 enum ColMode { COL_FWD = 0, COL_PSTART = 1, COL_PEND = 2, COL_IPREP = 3 };
 
