@@ -43,7 +43,11 @@ constexpr size_t FS_OFF = size_t(PLANES) * N2 * sizeof(float2);
 // packed mode: the current radial node's sinc slab gsxc[r] ([153][17] floats, 16-byte padded)
 constexpr int GSC = 153 * 17;
 constexpr size_t GSC_OFF = FS_OFF + size_t(PLANES) * 32 * FPITCH * sizeof(float);
-constexpr size_t SMEM = GSC_OFF + size_t((GSC + 3) / 4 * 4) * sizeof(float) + 16;
+// packed mode: per-axis phase and gain rows of the pairs, [2 buffers][phase, gain][96]
+// (float2), copied one stage ahead of their use with cp.async
+constexpr size_t ROW_OFF = GSC_OFF + size_t((GSC + 3) / 4 * 4) * sizeof(float);
+constexpr size_t SMEM = ROW_OFF + size_t(2 * 2 * 96) * sizeof(float2) + 16;
+static_assert(ROW_OFF % 16 == 0, "cp.async destinations are 16-byte aligned");
 }  // namespace gpar
 
 struct GainParityArgs {
@@ -183,6 +187,14 @@ __device__ __forceinline__ void par_stage_c(const float2* W, int j, const float2
 // where ~ conjugates the factor of a Nyquist component; k_a = 16 takes the
 // two-term form directly.
 __device__ __forceinline__ float2 cconj(float2 v) { return make_float2(v.x, -v.y); }
+
+// 16-byte global -> shared copy that completes asynchronously (cp.async); the
+// issuing thread's cp_async_wait_all and a barrier make it visible to the CTA
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 struct PackCol {
   float cp, cm, t16;  // t(k_a, j) = e_a.x cp + e_a.y cm (k_a != 16); t(16, j) = t16
@@ -351,6 +363,8 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
   float2* W = reinterpret_cast<float2*>(smem_raw);
   float* fS = reinterpret_cast<float*>(smem_raw + FS_OFF);
   float* gsc = reinterpret_cast<float*>(smem_raw + GSC_OFF);
+  // packed mode: phase row of buffer b at rows + 192 b, gain row at rows + 192 b + 96
+  float2* rows = reinterpret_cast<float2*>(smem_raw + ROW_OFF);
   int gsc_ir = -1;  // radial node whose slab is in gsc
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + SMEM - 16);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -400,6 +414,12 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
         fS[(m * 32 + c) * FPITCH + b] = fc[(2 * m + par) * N2 + b * 32 + c];
       }
     }
+    if constexpr (PACK) {
+      // the first pass's phase row (later ones are copied one pass ahead)
+      if (t < 48) cp_async16(rows + 192 * (p0 & 1) + 2 * t, a.ephase + int64_t(a.reps[p0]) * 96 + 2 * t);
+      cp_async_wait_all();
+      __syncthreads();
+    }
 
     for (int ip = p0; ip < p1; ++ip) {
       const int p = PACK ? a.reps[ip] : ip;
@@ -414,12 +434,22 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
           for (int e = t; e < GSC; e += THREADS) gsc[e] = src[e];
           gsc_ir = ir;
         }
+        // this pass's gain row (read in stage C) and the next pass's phase row
+        // (its stage A), landing while stages A and B run.  Buffer parity = pass
+        // parity: the buffers written here were last read in stage A of the
+        // previous pass and stage C of the one before, both behind a barrier
+        // already passed (a thread still in the previous stage C reads the other
+        // gain buffer).
+        if (t >= 48 && t < 96)
+          cp_async16(rows + 192 * (ip & 1) + 96 + 2 * (t - 48), a.gphase + int64_t(p) * 96 + 2 * (t - 48));
+        if (t < 48 && ip + 1 < p1)
+          cp_async16(rows + 192 * ((ip + 1) & 1) + 2 * t, a.ephase + int64_t(a.reps[ip + 1]) * 96 + 2 * t);
       }
       // (per-pair pointers are formed inside each stage so that none stays
       // live across the register-heavy plane pass)
       // ---- A: the thread's two columns (those it also takes in stage C)
       {
-        const float2* ep = a.ephase + int64_t(p) * 96;
+        const float2* ep = PACK ? rows + 192 * (ip & 1) : a.ephase + int64_t(p) * 96;
         const float2* epp = a.epar + (int64_t(p) * 2 + par) * 32;
         const int4 uc = a.ucols[t];
         if (warp < 15) {  // column pairs {j, -j}: rows 1..15 and 31..17
@@ -454,10 +484,11 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       __syncthreads();
       // ---- B: warp `warp` owns local plane `warp` (a = 2 warp + par)
       plane_pass<true>(W + warp * N2, fS + (warp * 32 + lane) * FPITCH, lane);
+      if constexpr (PACK) cp_async_wait_all();  // the rows copied at the top of this pass
       __syncthreads();
       // ---- C: the thread's two columns (the previous pair's TMEM stores are complete first)
       {
-        const float2* gp = a.gphase + int64_t(p) * 96;
+        const float2* gp = PACK ? rows + 192 * (ip & 1) + 96 : a.gphase + int64_t(p) * 96;
         const float2* gpp = a.gpar + (int64_t(p) * 2 + par) * 32;
         const float* gsr = a.gsx + int64_t(p / a.ns) * (513 * 20);
         const int4 uc = a.ucols[t];
