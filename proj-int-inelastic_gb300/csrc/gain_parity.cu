@@ -188,14 +188,6 @@ __device__ __forceinline__ void par_stage_c(const float2* W, int j, const float2
 // two-term form directly.
 __device__ __forceinline__ float2 cconj(float2 v) { return make_float2(v.x, -v.y); }
 
-// 16-byte global -> shared copy that completes asynchronously (cp.async); the
-// issuing thread's cp_async_wait_all and a barrier make it visible to the CTA
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 struct PackCol {
   float cp, cm, t16;  // t(k_a, j) = e_a.x cp + e_a.y cm (k_a != 16); t(16, j) = t16
 };

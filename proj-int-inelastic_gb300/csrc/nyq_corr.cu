@@ -35,13 +35,15 @@ constexpr int THREADS = 512;
 constexpr int PB = 2;        // antipodal pairs per batch
 constexpr int PL = 32 * 33;  // plane footprint: rows padded to 33 (row and column access conflict-free)
 // shared memory: f of the cell [a][b][c ^ b] (float), f^ on the three Nyquist
-// planes [3][N2] (float2), P[PB][3] planes (float2), the batch's phase / gain
-// rows [PB][2][96] and their row factors [PB][2][6 x 32] (float2); the
+// planes [3][N2] (float2), P[PB][3] planes (float2), the phase / gain rows of
+// two batches [2][PB][2][96] (the next batch's copied by cp.async while this
+// one runs) and the batch's row factors [PB][2][6 x 32] (float2); the
 // correction accumulator lives in registers (each thread owns the same points
 // in every batch)
 constexpr size_t OFF_P = size_t(N3) * sizeof(float) + size_t(3 * N2) * sizeof(float2);
-constexpr size_t SMEM = OFF_P + size_t(3 * PB) * PL * sizeof(float2) + size_t(PB) * 2 * 96 * sizeof(float2) +
+constexpr size_t SMEM = OFF_P + size_t(3 * PB) * PL * sizeof(float2) + size_t(2 * PB) * 2 * 96 * sizeof(float2) +
                         size_t(PB) * 2 * 6 * 32 * sizeof(float2);
+static_assert((OFF_P + size_t(3 * PB) * PL * sizeof(float2)) % 16 == 0, "cp.async destinations are 16-byte aligned");
 constexpr int PTS = 3 * N2 / THREADS;  // Nyquist points per thread
 __device__ __forceinline__ int sw(int r, int c) { return r * 33 + c; }
 __device__ __forceinline__ int fidx(int a, int b, int c) { return a * N2 + b * 32 + (c ^ b); }
@@ -186,8 +188,8 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
   float* fS = reinterpret_cast<float*>(smem_raw);  // f(a, b, c) at fidx(a, b, c)
   float2* Fh = reinterpret_cast<float2*>(fS + N3);  // [3][N2]: f^(16,r,c), f^(r,16,c), f^(r,c,16)
   float2* P = reinterpret_cast<float2*>(smem_raw + OFF_P);  // [PB][3] planes: P, then R, then U
-  float2* Rows = P + PB * 3 * PL;                            // [PB][2][96]: phase rows, gain rows
-  float2* Fac = Rows + PB * 2 * 96;                          // [PB][2][6 x 32] row factors
+  float2* RowsBuf = P + PB * 3 * PL;                         // [2][PB][2][96]: phase rows, gain rows
+  float2* Fac = RowsBuf + 2 * PB * 2 * 96;                   // [PB][2][6 x 32] row factors
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int64_t cell = blockIdx.x / a.blocks;
   const int blk = int(blockIdx.x - cell * a.blocks);
@@ -201,18 +203,33 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
     const int plane = i >> 10, r = (i >> 5) & 31, c = i & 31;
     Fh[i] = fh[plane == 0 ? (16 * N2 + r * 32 + c) : plane == 1 ? (r * N2 + 16 * 32 + c) : (r * N2 + c * 32 + 16)];
   }
+  // rows of the nbn pairs from jb into buffer b: 16-byte copies (a row is 48),
+  // zeros for absent pairs
+  auto stage_rows = [&](int jb, int nbn, int b) {
+    float2* dst = RowsBuf + b * PB * 192;
+    for (int i = t; i < PB * 2 * 48; i += THREADS) {
+      const int sidx = i / 96, w = (i / 48) & 1, e = 2 * (i % 48);
+      float2* d = dst + sidx * 192 + w * 96 + e;
+      if (sidx < nbn) {
+        cp_async16(d, (w == 0 ? a.ephase : a.gphase) + int64_t(a.reps[jb + sidx]) * 96 + e);
+      } else {
+        d[0] = make_float2(0.f, 0.f);
+        d[1] = make_float2(0.f, 0.f);
+      }
+    }
+  };
+  if (i0 < i1) stage_rows(i0, min(PB, i1 - i0), 0);
+  cp_async_wait_all();
   float2 acc[PTS];
 #pragma unroll
   for (int k = 0; k < PTS; ++k) acc[k] = make_float2(0.f, 0.f);
   __syncthreads();
 
-  for (int ib = i0; ib < i1; ib += PB) {
+  for (int ib = i0, bp = 0; ib < i1; ib += PB, bp ^= 1) {
     const int nb = min(PB, i1 - ib);
-    for (int i = t; i < PB * 2 * 96; i += THREADS) {
-      const int sidx = i / 192, w = (i / 96) & 1, e = i % 96;
-      Rows[i] = sidx < nb ? (w == 0 ? a.ephase : a.gphase)[int64_t(a.reps[ib + sidx]) * 96 + e] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
+    const float2* Rows = RowsBuf + bp * PB * 192;  // this batch's rows (staged during the previous batch)
+    // the next batch's rows into the other buffer, last read before the previous batch's final barrier
+    if (ib + PB < i1) stage_rows(ib + PB, min(PB, i1 - ib - PB), bp ^ 1);
     for (int i = t; i < PB * 2 * 192; i += THREADS) row_factors(Rows + (i / 192) * 96, Fac + (i / 192) * 192, i % 192);
     __syncthreads();
     // ---- 1. f^ t- on the three point sets (0 elsewhere on the planes)
@@ -327,6 +344,7 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
         acc[it].y += cp * u.y + cm * um.y;
       }
     }
+    cp_async_wait_all();  // the next batch's rows have landed before the barrier
     __syncthreads();
   }
   float2* out = a.part + (cell * a.blocks + blk) * 3 * N2;

@@ -20,6 +20,14 @@ extern std::atomic<int64_t> g_launches;
 
 // Once per device: kernel attributes (cudaFuncSetAttribute) belong to the
 // current device, so a process with plans on several GPUs sets them on each.
+// 16-byte global -> shared copy that completes asynchronously (cp.async); the
+// issuing thread's cp_async_wait_all and a barrier make it visible to the CTA
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 struct PerDeviceOnce {
   std::atomic<uint64_t> mask{0};
   bool done() const {
