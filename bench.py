@@ -90,6 +90,8 @@ class ClockSampler:
                  "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
             return
         # nvidia-smi takes a few hundred ms to start: wait (at most 5 s) for its
         # first sample so that the record covers the whole timed region
