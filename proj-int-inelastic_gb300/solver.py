@@ -612,9 +612,11 @@ class BoltzmannSolver1D(BoltzmannSolver):
         super().__init__(kn, riemann_solver, collision_operator)
 
     def setup(self, solution):
-        for b in (self.bc_lower[0], self.bc_upper[0]):
+        """Checks the boundary conditions as the reference's ghost fill does
+        (src/solver.py:67-105: lower side first)."""
+        for b, side in ((self.bc_lower[0], "Lower"), (self.bc_upper[0], "Upper")):
             if b is None:
-                raise Exception("Lower boundary condition not specified.")
+                raise Exception(f"{side} boundary condition not specified.")
             if b not in (BC.extrap, BC.periodic):
                 raise NotImplementedError("Boundary condition %s not implemented" % b)
         super().setup(solution)

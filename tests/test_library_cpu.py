@@ -175,6 +175,28 @@ def test_solver_host_logic():
         s.evolve_to_time(_Sol(), 1.0)
 
 
+def test_solver_setup_and_config_errors_match_reference():
+    """Boundary-condition errors of the ghost fill (src/solver.py:67-105) and
+    the velocity-dimension check, raised before any GPU work."""
+    import proj_int_inelastic_gb300 as pkg
+
+    assert (pkg.BC.extrap, pkg.BC.periodic) == (1, 2)  # src/solver.py:5-7
+    s = pkg.BoltzmannSolver1D(1.0)
+    with pytest.raises(Exception, match="Lower boundary condition not specified."):
+        s.setup(None)
+    s.bc_lower = [pkg.BC.extrap]
+    with pytest.raises(Exception, match="Upper boundary condition not specified."):
+        s.setup(None)
+    s.bc_upper = [3]
+    with pytest.raises(NotImplementedError, match="Boundary condition 3 not implemented"):
+        s.setup(None)
+    s.bc_upper = [pkg.BC.periodic]
+    s.setup(None)
+    assert s._is_set_up
+    with pytest.raises(ValueError, match="Dimension must be 2 or 3."):
+        pkg.Solution({"dim_x": 1, "dim_v": 4, "xmin": 0.0, "xmax": 1.0, "l": 8.0, "nx": 4, "nv": 8})
+
+
 def test_mesh_2d_matches_oracle():
     """2D-velocity mesh: circle quadrature and radial nodes as the reference's
     SpectralMesh (src/collision/spectral_mesh.py:51-56,94-97)."""
