@@ -193,6 +193,21 @@ def test_solver_setup_and_config_errors_match_reference():
     s.bc_upper = [pkg.BC.periodic]
     s.setup(None)
     assert s._is_set_up
+    # step-time checks of src/boltzmann.py:46-80 (before any device work)
+    class _Sol:
+        t = 0.0
+        state = None
+
+    s.time_integrator = "CONSP"
+    with pytest.raises(ValueError, match="The penalty parameter is not given"):
+        s.step(_Sol(), False, 0.0, 1.0)
+    s.time_integrator, s.penalty = "CONSP_M", 1.0
+    with pytest.raises(ValueError, match="The penalty parameter, e or tau are not given"):
+        s.step(_Sol(), False, 0.0, 1.0)
+    with pytest.raises(NotImplementedError, match="No stepping routine has been defined!"):
+        pkg.Solver().step(_Sol(), False, 0.0, 1.0)
+    with pytest.raises(NotImplementedError, match="No stepping routine has been defined!"):
+        pkg.IterativeBoltzmannSolver().step(_Sol())
     with pytest.raises(ValueError, match="Dimension must be 2 or 3."):
         pkg.Solution({"dim_x": 1, "dim_v": 4, "xmin": 0.0, "xmax": 1.0, "l": 8.0, "nx": 4, "nv": 8})
 
