@@ -548,10 +548,11 @@ def main():
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, FP32 FMA lanes x clock
+    n_sms = int(torch.cuda.get_device_properties(local).multi_processor_count)
+    fp32_peak = n_sms * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, FP32 FMA lanes x clock
     roof = {"kernel": dom, "bound": "fp32", "unit": "TFLOP/s", "peak": fp32_peak,
-            "peak_source": f"152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz={sm_max:.0f} (MEASURED_PEAKS.json); "
-                           "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
+            "peak_source": f"{n_sms} SMs (device query) x 128 FP32 lanes x 2 flop x sm_max_mhz={sm_max:.0f} "
+                           "(MEASURED_PEAKS.json); MEASURED_PEAKS.json has no FP32 CUDA-core figure",
             "launches_per_step": stages[dom]["launches"], "avg_launch_ms": stages[dom]["ms"] / stages[dom]["launches"]}
     if flops_total:
         per_launch = flops_total / stages[dom]["launches"]

@@ -35,6 +35,7 @@ extern "C" {
 #define PII_ERR_CUDA (-2)     /* CUDA runtime error                        */
 #define PII_ERR_SIZE (-3)     /* batch / size beyond the plan's capacity   */
 #define PII_ERR_NONFINITE (-4) /* NaN/Inf guard tripped on FP64 moments   */
+#define PII_ERR_STALL (-5)    /* a tensor-core DFT launch of an earlier call on the plan gave up waiting */
 
 #define PII_PREC_FP32 0 /* FP32 FFTs and quadrature sums, FP64 state and islands */
 #define PII_PREC_FP64 1 /* everything in FP64 (the parity path)                  */
@@ -124,12 +125,23 @@ int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stre
  * src/collision/inelastic_collisions.py:212-214): 0 = in-register CUDA-core
  * FFT, 1 = 64-point DFT on the tensor cores (tcgen05.mma, column-scaled split-FP16
  * operands hi + lo, FP32 accumulation in tensor memory).  Path 1 exists for
- * n = 64, FP32, 3D plans only; the autotuner times both.  get: `stalled`
- * (may be NULL) receives 1 if a tensor-core CTA ever gave up waiting for its
- * MMAs (results of that call are incomplete); reading it synchronises.
+ * n = 64, FP32, 3D plans only; the autotuner times both.  Every wait of the
+ * tensor-core kernel is bounded: a CTA that gives up first waits (bounded)
+ * for its copies and MMAs in flight, then frees its tensor memory, and the
+ * launch writes a stall word in mapped host memory.  The next pii_collide /
+ * pii_step / pii_step_splitting / pii_state_check on the plan returns
+ * PII_ERR_STALL (RuntimeError in Python) and clears the word.  get: `stalled`
+ * (may be NULL) receives the word without clearing it (1: gave up, 2: and
+ * could not drain); reading it synchronises the device.
  */
 int pii_plan_set_dft_path(pii_plan* plan, int path);
 int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stalled);
+/* Test hooks of the tensor-core kernel's bounded waits (no reference
+ * counterpart): wait_limit = mbarrier polls before a role gives up (default
+ * 4194304); withhold = 1 makes the TMA thread issue no copies at all, so the
+ * other roles wait on barriers that nothing completes and give up, with no
+ * copy or MMA in flight.  Drops captured step graphs. */
+int pii_plan_dft_test_hooks(pii_plan* plan, uint32_t wait_limit, int withhold);
 int pii_plan_get_tuning(const pii_plan* plan, int* gain_path, int* items_per_cluster, int64_t* chunk_points);
 /* Restores choices read by pii_plan_get_tuning (e.g. saved from an earlier
  * autotune); drops captured step graphs.  items_per_cluster in [1, 64]. */
@@ -243,18 +255,23 @@ int pii_fast_sweep(pii_plan* plan, double* f, const double* q, int64_t nx, doubl
 int pii_axpby(double* f, const double* d, double a, double b, int64_t count, void* stream);
 
 /*
- * Q(f,f) without any allocation, for callers that cannot call cudaMalloc
- * (while recording a CUDA graph, or under a host framework that owns all
- * device memory).  No counterpart in the reference.  Same result as
- * pii_collide in PII_PREC_FP32 (heat_bath = 0, mass_fix = 0), but the tables
- * and workspace live in one static device array of 2.5 MiB that the library
- * image reserves on every GPU that loads it.  Limits: n in {8, 16},
- * cells <= 8, n_r <= 32, n_sigma <= 192, n_r * n_sigma <= 1024; larger
- * requests return PII_ERR_SIZE.  All calls on a device share the array:
- * calls whose GPU work overlaps race.  The first call on a device resolves
- * the array's device address (cudaGetSymbolAddress) and must come before any
- * stream capture.  f, q: device arrays of cells x n^3 FP64; r, w_r, sigma:
- * host arrays as for pii_plan_create.
+ * Q(f,f) without any allocation.  No counterpart in the reference.  For
+ * callers that may not call cudaMalloc where they need Q: a host framework
+ * that hands out device memory only through its own pool, a time loop with a
+ * fixed memory budget set at start-up, or code that must not stall the device
+ * (cudaMalloc / cudaFree may synchronise it); pii_plan_create allocates, so
+ * they cannot use it.  Same result as pii_collide in PII_PREC_FP32
+ * (heat_bath = 0, mass_fix = 0), but the tables and workspace live in one
+ * static device array of 2.5 MiB that the library image reserves on every
+ * GPU that loads it.  Limits: n in {8, 16}, cells <= 8, n_r <= 32,
+ * n_sigma <= 192, n_r * n_sigma <= 1024; larger requests return
+ * PII_ERR_SIZE.  All calls on a device share the array, which keeps the last
+ * call's contents: calls whose GPU work overlaps race.  The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress) with that
+ * device current; cudaDeviceReset between calls is not supported.  f, q:
+ * device arrays of cells x n^3 FP64; r, w_r, sigma: host arrays as for
+ * pii_plan_create, read during the call and passed to the GPU by value (no
+ * host-to-device copy).
  */
 int pii_collide_noalloc(const double* f, double* q, int64_t cells, int n, int n_r, int n_sigma, const double* r,
                         const double* w_r, const double* sigma, double w_sigma, double L, double R, double e,
@@ -273,6 +290,9 @@ int pii_collide_noalloc(const double* f, double* q, int64_t cells, int n, int n_
 /* stage order: fwd_plane, col_fwd, col_pstart, pair_plane, col_pend, reduce,
  * col_iprep, finish, df, axpy, massfix, gain_cluster, gain_parity, nyq_corr */
 int64_t pii_kernel_launches(void);
+/* instantiated macro-step graphs held by the plan (at most 8: pii_step and
+ * pii_step_splitting evict the least recently replayed one) */
+int64_t pii_plan_graph_count(const pii_plan* plan);
 int pii_plan_profile(pii_plan* plan, int enable);
 int pii_plan_profile_read(pii_plan* plan, double* ms, int64_t* launches);
 

@@ -14,6 +14,7 @@ PII_ERR_ARG = -1
 PII_ERR_CUDA = -2
 PII_ERR_SIZE = -3
 PII_ERR_NONFINITE = -4
+PII_ERR_STALL = -5
 
 PREC_FP32 = 0
 PREC_FP64 = 1
@@ -49,6 +50,7 @@ SIGNATURES = {
     "pii_plan_set_tuning": (_c_int, [_vp, _c_int, _c_int, _c_i64]),
     "pii_plan_set_dft_path": (_c_int, [_vp, _c_int]),
     "pii_plan_get_dft_path": (_c_int, [_vp, _pint, _pint]),
+    "pii_plan_dft_test_hooks": (_c_int, [_vp, ctypes.c_uint32, _c_int]),
     "pii_collide": (_c_int, [_vp, _vp, _vp, _c_i64, _c_int, _c_dbl, _c_int, _vp]),
     "pii_laplacian": (_c_int, [_vp, _vp, _vp, _c_i64, _vp]),
     "pii_transport_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _vp]),
@@ -65,6 +67,7 @@ SIGNATURES = {
     "pii_collide_noalloc": (_c_int, [_vp, _vp, _c_i64, _c_int, _c_int, _c_int, _pdbl, _pdbl, _pdbl, _c_dbl, _c_dbl,
                                      _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _vp]),
     "pii_kernel_launches": (_c_i64, []),
+    "pii_plan_graph_count": (_c_i64, [_vp]),
     "pii_plan_profile": (_c_int, [_vp, _c_int]),
     "pii_plan_profile_read": (_c_int, [_vp, _pdbl, ctypes.POINTER(ctypes.c_int64)]),
 }

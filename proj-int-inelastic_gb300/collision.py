@@ -199,7 +199,7 @@ class SpectralMesh:
 
 def _precision_of(config, precision):
     if precision is None:
-        precision = str(config.get("config", {}).get("precision", "mixed")).lower()
+        precision = str(config.get("config", {}).get("precision", "double")).lower()
     if precision in ("double", "fp64", "float64"):
         return _lib.PREC_FP64
     if precision in ("mixed", "single", "fp32", "float32"):
@@ -268,10 +268,24 @@ class Plan:
         _lib.check(self._lib.pii_plan_set_dft_path(self.handle, _code(DFT_PATHS, dft_path, "dft_path")),
                    "pii_plan_set_dft_path")
 
+    def dft_test_hooks(self, wait_limit=1 << 22, withhold=False):
+        """Test hooks of the tensor-core DFT's bounded waits
+        (``pii_plan_dft_test_hooks``): polls before a role gives up, and
+        whether its TMA thread withholds every copy (so the waits run out with
+        nothing in flight)."""
+        _lib.check(self._lib.pii_plan_dft_test_hooks(self.handle, int(wait_limit), int(bool(withhold))),
+                   "pii_plan_dft_test_hooks")
+
+    @property
+    def graph_count(self):
+        """Instantiated macro-step graphs held by the plan (bounded)."""
+        return int(self._lib.pii_plan_graph_count(self.handle))
+
     @property
     def dft_stalled(self):
-        """True if a tensor-core DFT CTA ever gave up waiting for its MMAs
-        (``pii_plan_get_dft_path``; synchronises)."""
+        """True if a tensor-core DFT launch gave up waiting and the stall has
+        not been reported by a later call yet (``pii_plan_get_dft_path``;
+        synchronises)."""
         path, stalled = _lib.ctypes.c_int(), _lib.ctypes.c_int()
         _lib.check(self._lib.pii_plan_get_dft_path(self.handle, _lib.ctypes.byref(path), _lib.ctypes.byref(stalled)),
                    "pii_plan_get_dft_path")
@@ -314,8 +328,10 @@ class FSInelasticVHSCollision:
     (src/collision/inelastic_collisions.py:116-230, src/collision/base.py:6-58).
     Extra keyword arguments (not in the reference):
 
-    * ``precision``  -- "mixed" (FP32 FFTs and quadrature sums, the default) or
-      "double" (all FP64); also read from ``config["config"]["precision"]``;
+    * ``precision``  -- "double" (all FP64, the reference's arithmetic and the
+      default) or "mixed" (FP32 FFTs and quadrature sums, FP64 state and
+      output: ~1e-6 relative to FP64, tens of times faster); also read from
+      ``config["config"]["precision"]``;
     * ``with_loss``  -- what ``__call__`` evaluates: the reference's ``__call__``
       never passes ``with_loss``, so it returns the gain term only (default
       False, kept); True returns Q+ - Q-;

@@ -98,11 +98,11 @@ constexpr int OFF_G = OFF_P + 2 * PROW;     // gain rows of the epilogue's two a
 constexpr int OFF_SC = OFF_G + 2 * GROW * 4;  // column scales [4 tiles][128 columns] (floats)
 constexpr int OFF_XB = OFF_SC + 4 * TN * 4;     // partial bounds [2 tiles][2 halves][128 columns]
 constexpr int OFF_BAR = OFF_XB + 2 * 2 * TN * 4;
-// rfull[2] rempty[2] xfull[2] xempty[2] tfull[2] tempty[2] fbar gfull[2] gempty[2] sready[2]
-constexpr int NBAR = 19;
+// rfull[2] rempty[2] xfull[2] xempty[2] tfull[2] tempty[2] fbar gfull[2] gempty[2] sready[2] dbar
+constexpr int NBAR = 20;
 constexpr int SMEM = OFF_BAR + NBAR * 8 + 16;
 constexpr uint32_t TMEM_COLS = 512;         // X buffers [0, 256), accumulators [256, 512)
-constexpr uint32_t WAIT_LIMIT = 1u << 22;   // mbarrier polls before a role gives up
+constexpr uint32_t WAIT_LIMIT = 1u << 22;   // default mbarrier polls before a role gives up
 static_assert(SMEM <= 232448, "shared memory per CTA");
 }  // namespace ctc
 
@@ -116,7 +116,9 @@ struct ColTcArgs {
   const float* colb;     // PSTART: [cells][N2] max over a of |f^(a, j)|_1 (k_col_bound)
   int ns;
   int64_t items, c0, p0, np;
-  int* err;             // set to 1 if a role gave up waiting
+  int* err;             // host-mapped word: 1 if a role gave up waiting, 2 if the drain also timed out
+  uint32_t wait_limit;  // mbarrier polls before a role gives up
+  int withhold;         // test hook: the TMA thread issues no copies, so the other roles' waits run out
 };
 
 __device__ __forceinline__ uint32_t h2_bits(__half2 v) { return *reinterpret_cast<uint32_t*>(&v); }
@@ -130,12 +132,13 @@ __device__ __forceinline__ void split_pair(float x0, float x1, uint32_t& hi, uin
 }
 
 // bounded wait that also ends when another role has raised the abort flag
-__device__ __forceinline__ bool mbar_wait_role(uint64_t* mbar, uint32_t parity, volatile int* abort) {
-  for (uint32_t i = 0; i < ctc::WAIT_LIMIT; ++i) {
+__device__ __forceinline__ bool mbar_wait_role(uint64_t* mbar, uint32_t parity, volatile int* abort,
+                                               uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (mbar_try_wait(mbar, parity)) return true;
     if (*abort) return false;
   }
-  *abort = 1;
+  atomicMax(const_cast<int*>(abort), 1);
   return false;
 }
 
@@ -169,6 +172,9 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
   uint64_t* gfull = bars + 13;
   uint64_t* gempty = bars + 15;
   uint64_t* sready = bars + 17;
+  uint64_t* dbar = bars + 19;  // the issuer's final commit: every MMA it issued has completed
+  const uint32_t lim = a.wait_limit;
+  bool drained = true;
   float* scl = reinterpret_cast<float*>(sm + OFF_SC);
   volatile int* abort = reinterpret_cast<volatile int*>(bars + NBAR);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + NBAR) + 1;
@@ -191,6 +197,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       mbar_init(sready + b, 1);
     }
     mbar_init(fbar, 1);
+    mbar_init(dbar, 1);
     *abort = 0;
   }
   tm_fence_before();
@@ -213,7 +220,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       if constexpr (MODE == COL_PSTART)
         cb = a.colb[(a.c0 + (tile / TILES_PER_ITEM) / a.np) * N2 + int(tile % TILES_PER_ITEM) * TN + n];
       // the raw tile is in and operand buffer b is free (MMAs of tile i - 2 done)
-      const bool ok = mbar_wait_role(rfull + b, u, abort) && mbar_wait_role(xempty + b, u ^ 1u, abort);
+      const bool ok = mbar_wait_role(rfull + b, u, abort, lim) && mbar_wait_role(xempty + b, u ^ 1u, abort, lim);
       const float2* raw = reinterpret_cast<const float2*>(sm + OFF_R + b * RAW);
       const float2* ep = reinterpret_cast<const float2*>(sm + OFF_P + b * PROW);
       float2 ebc = make_float2(1.f, 0.f);
@@ -308,9 +315,9 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       const float* gsl = reinterpret_cast<const float*>(sm + OFF_G) + d * GROW;
       const float2* gpS = reinterpret_cast<const float2*>(gsl + 2 * SLICE);
       const uint32_t u = uint32_t(i >> 1) & 1u;
-      if (!mbar_wait_role(tfull + d, u, abort)) break;
-      if (!mbar_wait_role(sready + d, u, abort)) break;
-      if (MODE == COL_PEND && !mbar_wait_role(gfull + d, u, abort)) break;
+      if (!mbar_wait_role(tfull + d, u, abort, lim)) break;
+      if (!mbar_wait_role(sready + d, u, abort, lim)) break;
+      if (MODE == COL_PEND && !mbar_wait_role(gfull + d, u, abort, lim)) break;
       tm_fence_after();
       const float up = scl[(i & 3) * TN + n];  // the column's scale (S and D alike)
       const uint32_t ta = tmem + (uint32_t(32 * qd) << 16) + uint32_t(256 + 128 * d + 64 * hh);
@@ -348,13 +355,14 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       // ---- issuer
       const uint32_t sf = smem_u32(sm + OFF_F);
       constexpr uint32_t idesc = umma_idesc_f16(TN, 64);
-      bool go = mbar_wait_role(fbar, 0, abort);
+      bool go = mbar_wait_role(fbar, 0, abort, lim);
+      bool issued = false;
       int i = 0;
       for (int64_t tile = blockIdx.x; go && tile < ntiles; tile += gridDim.x, ++i) {
         const int b = i & 1;
         const uint32_t u = uint32_t(i >> 1) & 1u;
-        if (!mbar_wait_role(xfull + b, u, abort)) break;
-        if (!mbar_wait_role(tempty + b, u ^ 1u, abort)) break;
+        if (!mbar_wait_role(xfull + b, u, abort, lim)) break;
+        if (!mbar_wait_role(tempty + b, u ^ 1u, abort, lim)) break;
         mbar_arrive(sready + b);  // the converters' scales of this tile are visible from here
         tm_fence_after();
         const uint32_t tx = tmem + uint32_t(128 * b), td = tmem + uint32_t(256 + 128 * b);
@@ -373,19 +381,32 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         }
         umma_commit(xempty + b);
         umma_commit(tfull + b);
+        issued = true;
+      }
+      // drain: wait (bounded, not cut short by the abort flag) until every MMA
+      // issued here has completed, so no MMA writes tensor memory after it is freed
+      if (issued) {
+        umma_commit(dbar);
+        drained = mbar_wait_bounded(dbar, 0, lim);
       }
     }
   } else if (warp == TMA_WARP) {
     if (lane == 0) {
       // ---- TMA: the F image, then each tile's rows (and the pair's phase rows)
-      mbar_arrive_tx(fbar, FIMG);
+      // rphases[b] / gphases[b]: copies issued into raw / gain buffer b (one
+      // barrier phase each; at most one in flight per buffer)
+      int rphases[2] = {0, 0}, gphases[2] = {0, 0};
+      const bool go = !a.withhold;
+      if (go) {
+        mbar_arrive_tx(fbar, FIMG);
 #pragma unroll 1
-      for (int c = 0; c < 4; ++c)
-        bulk_g2s(sm + OFF_F + c * FOP, reinterpret_cast<const char*>(a.fimg) + c * FOP, FOP, fbar);
+        for (int c = 0; c < 4; ++c)
+          bulk_g2s(sm + OFF_F + c * FOP, reinterpret_cast<const char*>(a.fimg) + c * FOP, FOP, fbar);
+      }
       int i = 0;
-      for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      for (int64_t tile = blockIdx.x; go && tile < ntiles; tile += gridDim.x, ++i) {
         const int b = i & 1;
-        if (!mbar_wait_role(rempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
+        if (!mbar_wait_role(rempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort, lim)) break;
         const int64_t item = tile / TILES_PER_ITEM;
         const int j0 = int(tile - item * TILES_PER_ITEM) * TN;
         const int64_t ci = item / a.np;
@@ -393,13 +414,15 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         // rows of 64 per grid: f^ of cell c0 + ci, or item `item` of the chunk buffer
         const int y = int(MODE == COL_PSTART ? (a.c0 + ci) * NV : item * NV);
         mbar_arrive_tx(rfull + b, RAW + (MODE == COL_PSTART ? PROW : 0));
+        ++rphases[b];
         tma_load_2d(sm + OFF_R + b * RAW, &tmap, 2 * j0, y, rfull + b);
         if constexpr (MODE == COL_PSTART) bulk_g2s(sm + OFF_P + b * PROW, a.ephase + pair * 3 * NV, PROW, rfull + b);
         if constexpr (MODE == COL_PEND) {
           // the pair's gain rows into gain buffer b once the epilogue of tile i - 2 is done with it
-          if (!mbar_wait_role(gempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort)) break;
+          if (!mbar_wait_role(gempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort, lim)) break;
           unsigned char* g = sm + OFF_G + b * GROW * 4;
           mbar_arrive_tx(gfull + b, 2 * SLICE * 4 + PROW);
+          ++gphases[b];
           const float* gr = a.gsk + int64_t(pair / a.ns) * KS * SLICE;
           for (int h = 0; h < 2; ++h) {  // columns j0 .. j0 + 127 span k_b rows j0 / 64 and j0 / 64 + 1
             const int kb = kval(j0 / NV + h, NV);
@@ -408,11 +431,21 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
           bulk_g2s(g + 2 * SLICE * 4, a.gphase + pair * 3 * NV, PROW, gfull + b);
         }
       }
+      // drain: wait (bounded, not cut short by the abort flag) for the last copy
+      // into every buffer, so none lands in shared memory after the CTA is gone
+      if (go) drained = mbar_wait_bounded(fbar, 0, lim);
+      for (int b = 0; b < 2; ++b) {
+        if (rphases[b] > 0) drained &= mbar_wait_bounded(rfull + b, uint32_t(rphases[b] - 1) & 1u, lim);
+        if (gphases[b] > 0) drained &= mbar_wait_bounded(gfull + b, uint32_t(gphases[b] - 1) & 1u, lim);
+      }
     }
   }
+  if (!drained) atomicMax(const_cast<int*>(abort), 2);  // only the issuer and TMA lanes can fail to drain
   __syncthreads();
-  if (*abort) {
-    if (t == 0) atomicExch(a.err, 1);
+  if (t == 0 && *abort) {
+    // report to the host-mapped word (read by the next call on the plan)
+    *reinterpret_cast<volatile int*>(a.err) = *abort == 2 ? 2 : 1;
+    __threadfence_system();
   }
   tm_fence_before();
   __syncthreads();
@@ -543,8 +576,11 @@ int col_tc_prepare(pii_plan* p) {
     build_dft_images(img);
     PII_CUDA(cudaMalloc(&p->dft_img, img.size() * 2));
     PII_CUDA(cudaMemcpy(p->dft_img, img.data(), img.size() * 2, cudaMemcpyHostToDevice));
-    PII_CUDA(cudaMalloc(&p->dft_err, sizeof(int)));
-    PII_CUDA(cudaMemset(p->dft_err, 0, sizeof(int)));
+    // the stall word lives in mapped host memory: the host reads it without a
+    // synchronisation at the start of every later call on the plan
+    PII_CUDA(cudaHostAlloc(&p->dft_err_host, sizeof(int), cudaHostAllocMapped));
+    *p->dft_err_host = 0;
+    PII_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&p->dft_err), p->dft_err_host, 0));
     p->bytes += int64_t(img.size() * 2 + sizeof(int));
   }
   if (!p->dft_gs) {  // gsinc[r][k_b^2 + k_c^2 + k_a^2] by (r, |k_b|, |k_c|, |k_a|) (bulk-copy sources)
@@ -566,6 +602,19 @@ int col_tc_prepare(pii_plan* p) {
   }
   PII_CUDA(cudaDeviceGetAttribute(&p->dft_ctas, cudaDevAttrMultiProcessorCount, p->device));
   return PII_OK;
+}
+
+int dft_stall_check(pii_plan* p) {
+  if (!p || !p->dft_err_host) return PII_OK;
+  volatile int* w = p->dft_err_host;
+  const int v = *w;
+  if (!v) return PII_OK;
+  *w = 0;
+  set_error(v == 2 ? "tensor-core DFT: a CTA gave up waiting and could not drain its copies; results of that "
+                     "launch are invalid"
+                   : "tensor-core DFT: a CTA gave up waiting (bounded mbarrier wait); results of that launch are "
+                     "invalid");
+  return PII_ERR_STALL;
 }
 
 int col_tc_bounds(pii_plan* p, int64_t cells, cudaStream_t s) {
@@ -599,6 +648,8 @@ int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int
   a.p0 = p0;
   a.np = np;
   a.err = p->dft_err;
+  a.wait_limit = p->dft_wait_limit;
+  a.withhold = p->dft_withhold;
   const int64_t tiles = items * TILES_PER_ITEM;
   const unsigned grid = unsigned(std::min<int64_t>(p->dft_ctas, tiles));
   CUtensorMap tm;

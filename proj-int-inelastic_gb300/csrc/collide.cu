@@ -116,6 +116,7 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
     set_error("pii_collide: f and q must not alias");
     return PII_ERR_ARG;
   }
+  PII_TRY(dft_stall_check(p));  // a stall of an earlier launch on this plan
   int st = PII_OK;
   if (p->dim == 2)
     st = p->precision == PII_PREC_FP32 ? collide2d_f32(p, f, q, cells, with_loss, hb, s)
@@ -211,11 +212,7 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
   plan->gc_items_per_cluster = st == PII_OK ? pick.items : saved_items;
   plan->chunk_points = st == PII_OK ? pick.points : saved_points;
   plan->dft_path = st == PII_OK ? pick.dft : saved_dft;
-  for (auto& kv : plan->graphs) {  // captured graphs baked the old choices in
-    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
-  }
-  plan->graphs.clear();
+  pii::graphs_clear(plan);  // captured graphs baked the old choices in
   if (best_ms) *best_ms = best;
   return st;
 }
@@ -241,11 +238,7 @@ extern "C" int pii_plan_set_tuning(pii_plan* plan, int gain_path, int items_per_
   if (st != PII_OK) return st;
   plan->gc_items_per_cluster = items_per_cluster;
   plan->chunk_points = chunk_points;
-  for (auto& kv : plan->graphs) {  // captured graphs baked the old choices in
-    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
-  }
-  plan->graphs.clear();
+  pii::graphs_clear(plan);  // captured graphs baked the old choices in
   return PII_OK;
 }
 
@@ -276,11 +269,7 @@ extern "C" int pii_plan_set_dft_path(pii_plan* plan, int path) {
     return PII_ERR_ARG;
   }
   plan->dft_path = path;
-  for (auto& kv : plan->graphs) {  // captured graphs baked the old choice in
-    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
-  }
-  plan->graphs.clear();
+  pii::graphs_clear(plan);  // captured graphs baked the old choice in
   return PII_OK;
 }
 
@@ -292,11 +281,23 @@ extern "C" int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stall
   *path = plan->dft_path;
   if (stalled) {
     *stalled = 0;
-    if (plan->dft_err) {
+    if (plan->dft_err_host) {
       PII_CUDA(cudaSetDevice(plan->device));
-      PII_CUDA(cudaMemcpy(stalled, plan->dft_err, sizeof(int), cudaMemcpyDeviceToHost));
+      PII_CUDA(cudaDeviceSynchronize());
+      *stalled = *reinterpret_cast<volatile int*>(plan->dft_err_host);
     }
   }
+  return PII_OK;
+}
+
+extern "C" int pii_plan_dft_test_hooks(pii_plan* plan, uint32_t wait_limit, int withhold) {
+  if (!plan || wait_limit < 1) {
+    pii::set_error("pii_plan_dft_test_hooks: wait_limit must be >= 1");
+    return PII_ERR_ARG;
+  }
+  plan->dft_wait_limit = wait_limit;
+  plan->dft_withhold = withhold ? 1 : 0;
+  pii::graphs_clear(plan);  // captured graphs baked the old arguments in
   return PII_OK;
 }
 

@@ -1,18 +1,21 @@
 // pii_collide_noalloc: Q(f,f) for small velocity grids without allocating.
 //
-// Who needs it: code that may not call cudaMalloc at the point where it wants
-// a collision evaluation -- for example a caller that is recording a CUDA
-// graph of its own time loop (an allocation inside stream capture is an
-// error), a host framework that hands out device memory only through its own
-// pool and forbids raw cudaMalloc, or an embedded driver loop with a fixed
-// memory budget decided at start-up.  pii_plan_create allocates its tables
-// and workspace with cudaMalloc, so those callers cannot use it.
+// Who needs it: callers that may not call cudaMalloc at the point where they
+// want a collision evaluation.  Examples: a host framework that hands out
+// device memory only through its own pool and forbids raw cudaMalloc (its
+// pool already holds the memory, so a raw allocation can fail or fragment
+// it); an embedded time loop with a fixed memory budget decided at start-up;
+// code that must not stall the device, since cudaMalloc and cudaFree may
+// synchronise it.  pii_plan_create allocates its tables and workspace with
+// cudaMalloc, so those callers cannot use it.
 //
 // What it does instead: the tables, spectra and the chunk buffer of the
 // operator live in one file-scope device array (g_noalloc_scratch below) that
 // is part of the library image.  Every GPU that loads the library reserves it
 // (PII_NOALLOC_SCRATCH_BYTES) until the process exits.  The caller passes f
-// and q; nothing else is allocated, on the device or on the host.
+// and q; nothing else is allocated, on the device or on the host.  The
+// quadrature (r, w_r, sigma) travels by value in the table kernel's launch
+// parameters, so a call makes no host-to-device copy either.
 //
 // Limits (checked, PII_ERR_SIZE otherwise): n in {8, 16}, cells <= 8,
 // n_r <= 32, n_sigma <= 192, n_r * n_sigma <= 1024.  FP32 arithmetic (the
@@ -28,7 +31,9 @@
 // Set-up: the first call on a device (with that device current) resolves the
 // device address of the array with cudaGetSymbolAddress; the host-side name of
 // a __device__ array is not a device address and must never be passed to a
-// kernel.  Make that first call before any stream capture begins.
+// kernel.  The address is kept per device ordinal for the life of the
+// process: cudaDeviceReset between calls is not supported (the module is
+// reloaded and the kept address may no longer be valid).
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -63,11 +68,22 @@ static int noalloc_scratch(void** out) {
   return PII_OK;
 }
 
+// The quadrature at its largest (n_r <= 32, n_sigma <= 192): 5 KB, passed by
+// value as a launch parameter (within the 32 KB parameter limit of sm_70+).
+struct NoallocQuad {
+  double r[32];
+  double wr[32];
+  double sigma[192 * 3];
+};
+
 // Tables of the plan (same definitions as pii_plan_create), evaluated in FP64
 // on the device and rounded to FP32.
-__global__ void k_noalloc_tables(const double* r, const double* wr, const double* sigma, int nr, int ns, int n,
-                                 double L, double R, double e, double e0, double gamma, double wsigma,
-                                 float2* eph, float2* gph, float* gs, float* lk, float* lp) {
+__global__ void k_noalloc_tables(const NoallocQuad quad, int nr, int ns, int n, double L, double R, double e,
+                                 double e0, double gamma, double wsigma, float2* eph, float2* gph, float* gs,
+                                 float* lk, float* lp) {
+  const double* r = quad.r;
+  const double* wr = quad.wr;
+  const double* sigma = quad.sigma;
   const double pi = 3.141592653589793238462643383279502884;
   const int M = 3 * (n / 2) * (n / 2);
   const int64_t nphase = int64_t(nr) * ns * 3 * n;
@@ -126,9 +142,6 @@ static int noalloc_run(unsigned char* base, const double* f, double* q, int64_t 
     off += (bytes + 255) & ~size_t(255);
     return p;
   };
-  double* d_r = reinterpret_cast<double*>(carve(size_t(nr) * 8));
-  double* d_wr = reinterpret_cast<double*>(carve(size_t(nr) * 8));
-  double* d_sig = reinterpret_cast<double*>(carve(size_t(ns) * 3 * 8));
   float2* eph = reinterpret_cast<float2*>(carve(size_t(Q) * 3 * NV * sizeof(float2)));
   float2* gph = reinterpret_cast<float2*>(carve(size_t(Q) * 3 * NV * sizeof(float2)));
   float* gs = reinterpret_cast<float*>(carve(size_t(nr) * (M + 1) * 4));
@@ -143,17 +156,17 @@ static int noalloc_run(unsigned char* base, const double* f, double* q, int64_t 
     return PII_ERR_SIZE;
   }
   const int64_t items = int64_t((PII_NOALLOC_SCRATCH_BYTES - off) / (size_t(N) * sizeof(float2)));
-  if (items < 2 * cells || items < cells) {
+  if (items < 2 * cells) {
     set_error("pii_collide_noalloc: scratch too small for %lld cells of n = %d", (long long)cells, NV);
     return PII_ERR_SIZE;
   }
   float2* buf = reinterpret_cast<float2*>(carve(0));
 
-  PII_CUDA(cudaMemcpyAsync(d_r, r, size_t(nr) * 8, cudaMemcpyHostToDevice, s));
-  PII_CUDA(cudaMemcpyAsync(d_wr, wr, size_t(nr) * 8, cudaMemcpyHostToDevice, s));
-  PII_CUDA(cudaMemcpyAsync(d_sig, sigma, size_t(ns) * 3 * 8, cudaMemcpyHostToDevice, s));
-  k_noalloc_tables<<<64, 256, 0, s>>>(d_r, d_wr, d_sig, nr, ns, NV, L, R, e, e0, gamma, wsigma, eph, gph, gs, lk,
-                                      lp);
+  NoallocQuad quad{};
+  std::copy(r, r + nr, quad.r);
+  std::copy(wr, wr + nr, quad.wr);
+  std::copy(sigma, sigma + size_t(ns) * 3, quad.sigma);
+  k_noalloc_tables<<<64, 256, 0, s>>>(quad, nr, ns, NV, L, R, e, e0, gamma, wsigma, eph, gph, gs, lk, lp);
   PII_CHECK_LAUNCH();
 
   // a plan view onto the scratch: no allocation, no ownership

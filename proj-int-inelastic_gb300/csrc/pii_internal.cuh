@@ -121,8 +121,14 @@ struct GraphKey {
 struct GraphEntry {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  int64_t kernels = 0;  // kernel launches captured into the graph
+  cudaEvent_t done = nullptr;  // recorded after each replay: eviction waits for the last one
+  int64_t kernels = 0;         // kernel launches captured into the graph
+  uint64_t last_use = 0;       // plan-local replay counter at the last replay (LRU eviction)
 };
+
+// instantiated macro-step graphs kept per plan; the least recently replayed
+// one is destroyed when a new key would exceed this
+constexpr size_t kMaxGraphs = 8;
 
 struct ProfEvent {
   int stage;
@@ -177,7 +183,10 @@ struct pii_plan {
   // FFT (k_col), 1 = tensor-core split-FP16 DFT (k_col_tc)
   int dft_path = 0;
   void* dft_img = nullptr;  // DFT matrix images (A_hi | A_lo) for DIR = +1 and -1
-  int* dft_err = nullptr;   // device word: 1 if a k_col_tc CTA gave up waiting for its MMAs
+  int* dft_err = nullptr;   // device address of dft_err_host
+  int* dft_err_host = nullptr;  // mapped host word: 1 if a k_col_tc CTA gave up waiting (2: and could not drain)
+  uint32_t dft_wait_limit = 1u << 22;  // mbarrier polls before a k_col_tc role gives up
+  int dft_withhold = 0;     // test hook: k_col_tc's TMA thread issues no copies
   int dft_ctas = 0;         // resident CTAs of k_col_tc (one per SM)
   void* dft_gs = nullptr;   // gsinc by (r, |k_b|, |k_c|, |k_a|) slices (TMA sources)
   void* dft_colb = nullptr; // [batch_max][n^2] column bounds max_a |f^|_1 (k_col_bound)
@@ -186,6 +195,8 @@ struct pii_plan {
   alignas(128) unsigned char dft_tmap[2][128] = {};
   int64_t bytes = 0;
   std::map<pii::GraphKey, pii::GraphEntry> graphs;
+  uint64_t graph_tick = 0;
+  std::vector<double> v1host;  // the first-axis velocities last uploaded to v1dev
   // per-stage CUDA-event profiling (pii_plan_profile)
   bool prof = false;
   std::vector<pii::ProfEvent> prof_events;
@@ -230,6 +241,10 @@ int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s);
 int col_tc_prepare(pii_plan* p);
 int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int64_t np, cudaStream_t s);
 int col_tc_bounds(pii_plan* p, int64_t cells, cudaStream_t s);
+// col_tc.cu: PII_ERR_STALL if a tensor-core DFT launch of an earlier call gave
+// up waiting (read from mapped host memory without a synchronisation; cleared
+// once reported)
+int dft_stall_check(pii_plan* p);
 // transport.cu
 int transport_impl(pii_plan* p, const double* f, const double* q, double* df, int64_t nx, double dt,
                    double dx, int bc_lo, int bc_hi, double qscale, cudaStream_t s);
@@ -237,6 +252,9 @@ int mass_fix_impl(pii_plan* p, double* q, int64_t cells, int64_t N, cudaStream_t
 int axpy3_impl(pii_plan* p, double* f, const double* d, double s0, double s1, double s2, int64_t count,
                cudaStream_t s);
 int upload_v1(pii_plan* p, const double* v1, cudaStream_t s);
+// plan.cu: the macro-step graph cache
+void graphs_clear(pii_plan* p);
+void graph_entry_destroy(GraphEntry& g);
 int consp_m_impl(pii_plan* p, double* f, const double* q, int64_t cells, double c, double c2, double dt, double kn,
                  double e, double tau, cudaStream_t s);
 int axpy3_impl(pii_plan* p, double* f, const double* d, double s0, double s1, double s2, int64_t count,

@@ -73,6 +73,21 @@ bool GraphKey::operator<(const GraphKey& o) const {
                   o.levels, o.K[0], o.K[1], o.K[2], o.h[0], o.h[1], o.h[2], o.stream);
 }
 
+void graph_entry_destroy(GraphEntry& g) {
+  if (g.done) {
+    cudaEventSynchronize(g.done);  // its last replay has finished
+    cudaEventDestroy(g.done);
+  }
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g = GraphEntry{};
+}
+
+void graphs_clear(pii_plan* p) {
+  for (auto& kv : p->graphs) graph_entry_destroy(kv.second);
+  p->graphs.clear();
+}
+
 static double sinc(double x) { return x == 0.0 ? 1.0 : std::sin(x) / x; }
 
 // J_0(x) = (1/pi) int_0^pi cos(x sin t) dt by the trapezoidal rule, which
@@ -213,16 +228,14 @@ static void free_plan(pii_plan* p) {
   if (!p) return;
   prof_resolve(p);
   for (cudaEvent_t e : p->prof_pool) cudaEventDestroy(e);
-  for (auto& kv : p->graphs) {
-    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
-  }
+  graphs_clear(p);
   void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsxc, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
                   p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag,
-                  p->dft_img,    p->dft_err,    p->dft_gs,    p->dft_colb};
+                  p->dft_img,    p->dft_gs,     p->dft_colb};
   for (void* q : ptrs)
     if (q) cudaFree(q);
+  if (p->dft_err_host) cudaFreeHost(p->dft_err_host);
   delete p;
 }
 

@@ -128,6 +128,55 @@ static int splitting_body(const StepCtx& c, int integrator, double dt, double pe
   return PII_OK;
 }
 
+// Replays the cached graph of `key`, capturing `body` into a new one first if
+// there is none.  At most kMaxGraphs graphs are kept per plan: a new key
+// evicts the least recently replayed graph (after its last replay finished),
+// so callers that vary dt or rotate state buffers do not accumulate graphs.
+template <typename Body>
+static int replay_cached(pii_plan* plan, const GraphKey& key, cudaStream_t s, Body body) {
+  auto it = plan->graphs.find(key);
+  if (it == plan->graphs.end()) {
+    while (plan->graphs.size() >= kMaxGraphs) {
+      auto lru = plan->graphs.begin();
+      for (auto j = plan->graphs.begin(); j != plan->graphs.end(); ++j)
+        if (j->second.last_use < lru->second.last_use) lru = j;
+      graph_entry_destroy(lru->second);
+      plan->graphs.erase(lru);
+    }
+    PII_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = g_launches.load();
+    int st = body();
+    const int64_t captured = g_launches.load() - before;
+    g_launches.fetch_sub(captured);  // captured, not executed
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (st != PII_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (e != cudaSuccess) {
+      set_error("graph capture: %s", cudaGetErrorString(e));
+      return PII_ERR_CUDA;
+    }
+    GraphEntry ge;
+    ge.graph = g;
+    ge.kernels = captured;
+    e = cudaGraphInstantiate(&ge.exec, g, 0);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ge.done, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      graph_entry_destroy(ge);
+      set_error("graph instantiate: %s", cudaGetErrorString(e));
+      return PII_ERR_CUDA;
+    }
+    it = plan->graphs.emplace(key, ge).first;
+  }
+  it->second.last_use = ++plan->graph_tick;
+  PII_CUDA(cudaGraphLaunch(it->second.exec, s));
+  PII_CUDA(cudaEventRecord(it->second.done, s));
+  g_launches.fetch_add(it->second.kernels);
+  return PII_OK;
+}
+
 }  // namespace pii
 
 extern "C" {
@@ -161,41 +210,12 @@ int pii_step_splitting(pii_plan* plan, int integrator, double* f, int64_t nx, do
   PII_TRY(pii::upload_v1(plan, v1, s));
   const double delta = v1[1] - v1[0];
   plan->delta3 = plan->dim == 3 ? delta * delta * delta : delta * delta;  // velocity cell volume
+  PII_TRY(pii::dft_stall_check(plan));  // a stall of an earlier launch on this plan
   pii::StepCtx c{plan, f, nx, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, s};
   if (!use_graph || s == nullptr || plan->prof) return pii::splitting_body(c, integrator, dt, penalty, e, tau);
   pii::GraphKey key{integrator, f, nx, dt, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, 0,
                     {0, 0, 0}, {penalty, e, tau}, stream};
-  auto it = plan->graphs.find(key);
-  if (it == plan->graphs.end()) {
-    PII_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    const int64_t before = pii::g_launches.load();
-    int st = pii::splitting_body(c, integrator, dt, penalty, e, tau);
-    const int64_t captured = pii::g_launches.load() - before;
-    pii::g_launches.fetch_sub(captured);
-    cudaGraph_t g = nullptr;
-    cudaError_t er = cudaStreamEndCapture(s, &g);
-    if (st != PII_OK) {
-      if (g) cudaGraphDestroy(g);
-      return st;
-    }
-    if (er != cudaSuccess) {
-      pii::set_error("graph capture: %s", cudaGetErrorString(er));
-      return PII_ERR_CUDA;
-    }
-    pii::GraphEntry ge;
-    ge.graph = g;
-    ge.kernels = captured;
-    er = cudaGraphInstantiate(&ge.exec, g, 0);
-    if (er != cudaSuccess) {
-      cudaGraphDestroy(g);
-      pii::set_error("graph instantiate: %s", cudaGetErrorString(er));
-      return PII_ERR_CUDA;
-    }
-    it = plan->graphs.emplace(key, ge).first;
-  }
-  PII_CUDA(cudaGraphLaunch(it->second.exec, s));
-  pii::g_launches.fetch_add(it->second.kernels);
-  return PII_OK;
+  return pii::replay_cached(plan, key, s, [&] { return pii::splitting_body(c, integrator, dt, penalty, e, tau); });
 }
 
 
@@ -242,41 +262,14 @@ int pii_step(pii_plan* plan, int integrator, double* f, int64_t nx, double dt, c
     K[l] = inner_steps[l];
     h[l] = inner_dt[l];
   }
+  PII_TRY(pii::dft_stall_check(plan));  // a stall of an earlier launch on this plan
   if (!use_graph || s == nullptr || plan->prof) return pii::step_body(c, integrator, dt, K, h);
 
   pii::GraphKey key{integrator, f, nx, dt, dx, kn, bc_lower, bc_upper, with_loss, mass_fix, need,
                     {K[0], K[1], K[2]}, {h[0], h[1], h[2]}, stream};
-  auto it = plan->graphs.find(key);
-  if (it == plan->graphs.end()) {
-    PII_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    const int64_t before = pii::g_launches.load();
-    int st = pii::step_body(c, integrator, dt, K, h);
-    const int64_t captured = pii::g_launches.load() - before;
-    pii::g_launches.fetch_sub(captured);  // captured, not executed
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(s, &g);
-    if (st != PII_OK) {
-      if (g) cudaGraphDestroy(g);
-      return st;
-    }
-    if (e != cudaSuccess) {
-      pii::set_error("graph capture: %s", cudaGetErrorString(e));
-      return PII_ERR_CUDA;
-    }
-    pii::GraphEntry ge;
-    ge.graph = g;
-    ge.kernels = captured;
-    e = cudaGraphInstantiate(&ge.exec, g, 0);
-    if (e != cudaSuccess) {
-      cudaGraphDestroy(g);
-      pii::set_error("graph instantiate: %s", cudaGetErrorString(e));
-      return PII_ERR_CUDA;
-    }
-    it = plan->graphs.emplace(key, ge).first;
-  }
-  PII_CUDA(cudaGraphLaunch(it->second.exec, s));
-  pii::g_launches.fetch_add(it->second.kernels);
-  return PII_OK;
+  return pii::replay_cached(plan, key, s, [&] { return pii::step_body(c, integrator, dt, K, h); });
 }
+
+int64_t pii_plan_graph_count(const pii_plan* plan) { return plan ? int64_t(plan->graphs.size()) : -1; }
 
 }  // extern "C"

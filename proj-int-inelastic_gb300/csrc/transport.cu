@@ -310,7 +310,10 @@ int upload_v1(pii_plan* p, const double* v1, cudaStream_t s) {
     set_error("v1 velocity array is NULL");
     return PII_ERR_ARG;
   }
+  // uploaded only when it changed (a solver passes the same grid every macro-step)
+  if (p->v1host.size() == size_t(p->n) && std::equal(v1, v1 + p->n, p->v1host.begin())) return PII_OK;
   PII_CUDA(cudaMemcpyAsync(p->v1dev, v1, size_t(p->n) * sizeof(double), cudaMemcpyHostToDevice, s));
+  p->v1host.assign(v1, v1 + p->n);
   return PII_OK;
 }
 
@@ -378,6 +381,7 @@ int pii_state_check(pii_plan* plan, const double* f, double* out, int64_t cells,
   int h = 0;
   PII_CUDA(cudaMemcpyAsync(&h, plan->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
   PII_CUDA(cudaStreamSynchronize(s));
+  PII_TRY(pii::dft_stall_check(plan));  // the state may come from a stalled launch
   if (h) {
     pii::set_error("pii_state_check: f holds NaN or Inf values");
     return PII_ERR_NONFINITE;

@@ -7,7 +7,10 @@ by point count (``src/collision/spherical_design/__init__.py:62-88``).  The
 quadrature points must be identical for operator parity, so this script reads
 those tables once and stores them as float64 arrays keyed ``m{npts:05d}``
 (with the design strength in ``qdeg_m{npts:05d}``).  Run it where the reference
-checkout is present; the package reads only the ``.npz``.
+checkout is present (``PII_REFERENCE_ROOT``, required); the package reads
+only the ``.npz``:
+
+    PII_REFERENCE_ROOT=<reference checkout> python tests/golden/make_designs.py
 """
 import os
 import re
@@ -15,13 +18,15 @@ import sys
 
 import numpy as np
 
-SRC = os.path.join(
-    os.environ.get("PII_REFERENCE_ROOT", "/root/reference"),
-    "src/collision/spherical_design/symmetric",
-)
+OUT = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                   "proj-int-inelastic_gb300", "data", "sphere_designs.npz")
 
 
-def main(out=os.path.join(os.path.dirname(os.path.abspath(__file__)), "sphere_designs.npz")):
+def main(out=OUT):
+    root = os.environ.get("PII_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("set PII_REFERENCE_ROOT to the reference checkout (the directory holding src/)")
+    SRC = os.path.join(root, "src/collision/spherical_design/symmetric")
     arrays = {}
     for name in sorted(os.listdir(SRC)):
         m = re.match(r"womersley-ss(\d+)-m(\d+)\.txt$", name)

@@ -26,8 +26,8 @@ vectors, so parity is pinned by executing its own code under the shims in
 Run from the repository root:  ``python tests/golden/make_golden.py [stem ...]``
 (all fixtures, or only the named ones; the full set reproduces the committed
 files, the transport fixture drawing from the same generator after op_small).
-Needs the reference checkout (``PII_REFERENCE_ROOT``, default
-/root/reference); GPU test runs never execute this script.
+Needs the reference checkout: set ``PII_REFERENCE_ROOT`` to it (required, no
+default); GPU test runs never execute this script.
 """
 import math
 import os

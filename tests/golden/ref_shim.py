@@ -28,7 +28,8 @@ import types
 import numpy as np
 import scipy.fft
 
-REF_ROOT = os.environ.get("PII_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: required, no default (only the fixture scripts need it)
+REF_ROOT = os.environ.get("PII_REFERENCE_ROOT", "")
 
 
 def _install_shims(workers=None):
@@ -83,8 +84,10 @@ def _install_shims(workers=None):
 
 def load_reference(workers=None):
     """Return a namespace with the reference modules used by the fixtures."""
+    if not REF_ROOT:
+        raise RuntimeError("set PII_REFERENCE_ROOT to the reference checkout (the directory holding src/)")
     if not os.path.isdir(os.path.join(REF_ROOT, "src")):
-        raise RuntimeError(f"reference checkout not found under {REF_ROOT}")
+        raise RuntimeError(f"reference checkout not found under PII_REFERENCE_ROOT={REF_ROOT}")
     _install_shims(workers)
     if REF_ROOT not in sys.path:
         sys.path.insert(0, REF_ROOT)

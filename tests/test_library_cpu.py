@@ -141,9 +141,10 @@ def test_config_errors():
     with pytest.raises(ValueError):
         pkg.FSInelasticVHSCollision(cfg, sm, precision="half")
     col = pkg.FSInelasticVHSCollision(cfg, sm)
-    assert col.precision == "mixed" and col.default_with_loss is False
-    cfg2 = dict(cfg, config={"precision": "double"})
-    assert pkg.FSInelasticVHSCollision(cfg2, sm).precision == "double"
+    # the drop-in default is the reference's FP64 arithmetic; mixed precision is opt-in
+    assert col.precision == "double" and col.default_with_loss is False
+    cfg2 = dict(cfg, config={"precision": "mixed"})
+    assert pkg.FSInelasticVHSCollision(cfg2, sm).precision == "mixed"
     # an empty batch gives an empty result without touching a GPU; wrong trailing axes raise
     for shape in ((0, 16, 16, 16), (3, 0, 16, 16, 16)):
         out = col(np.empty(shape))
