@@ -7,7 +7,8 @@
   FP64 comparison run stays short); the state error is reported against a
   documented bound (see the test), mass to 1e-10;
 * large grid: n = 64, L = 10, e = 0.7, 48 radial nodes x the 70-point design
-  (no 64-point symmetric design exists), 3-component mixtures.
+  (no 64-point symmetric design exists), 3-component mixtures; against the
+  oracle's fixture (tests/golden/c5_n64.npz) and the FP64 path.
 Tolerance: 1e-5 relative L-inf against the FP64 GPU path unless stated.
 """
 import math
@@ -108,6 +109,47 @@ def test_tpi3_stiff_periodic_mixed_vs_fp64():
     dT = float(np.abs(res["mixed"][3] / res["double"][3] - 1).max())
     print(f"TPI3 kn=1e-4: max relative temperature difference mixed vs FP64 = {dT:.3e}")
     assert dT < 1e-2
+
+
+def _mixture_from(v, w, u, T):
+    """The seeded mixture of tests/golden/make_oracle_fixtures.py, rebuilt from its parameters."""
+    V = np.meshgrid(v, v, v, indexing="ij")
+    f = 0.0
+    for wi, ui, Ti in zip(w, u, T):
+        d2 = (V[0] - ui[0]) ** 2 + (V[1] - ui[1]) ** 2 + (V[2] - ui[2]) ** 2
+        f = f + wi / (2 * math.pi * Ti) ** 1.5 * np.exp(-d2 / (2 * Ti))
+    return f / (f.sum() * (v[1] - v[0]) ** 3)
+
+
+def test_large_grid_n64_full_quadrature_vs_oracle_fixture(golden):
+    """The large-grid configuration at its full quadrature (n = 64, L = 10,
+    48 radial nodes x the 70-point design, e = e0 = 0.7, hard spheres) against
+    the oracle's Q on one seeded 3-Maxwellian cell: the FP64 path to 1e-12 and
+    the mixed path with both first-axis column transforms (CUDA-core FFT and
+    tensor-core split-FP16 DFT) to 1e-5."""
+    pkg = _pkg()
+    d = golden("c5_n64.npz")
+    n, s, nr, ns, e, e0, g = (float(x) for x in d["params"])
+    cfg = op_config(int(n), s, int(nr), int(ns), e, e0, g)
+    sm = pkg.SpectralMesh(cfg)
+    assert abs(sm.L - 10.0) < 1e-12
+    f = _mixture_from(sm.v_center, d["w"], d["u"], d["T"])
+    assert abs(f.sum() - float(d["f_sum"])) < 1e-12 * float(d["f_sum"])
+    assert abs(f.max() - float(d["f_max"])) < 1e-12 * float(d["f_max"])
+    ref = d["q"][None]
+    ft = torch.as_tensor(f[None], device="cuda:0")
+    qd = pkg.FSInelasticVHSCollision(cfg, sm, precision="double").collide(ft, with_loss=True)
+    err = rel_linf(qd.cpu().numpy(), ref)
+    print(f"n=64 full quadrature, FP64 path vs oracle: rel Linf {err:.3e}")
+    assert err < 1e-12
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed")
+    for path in ("fft", "tensor"):
+        col.plan.set_dft_path(path)
+        qm = col.collide(ft, with_loss=True)
+        err = rel_linf(qm.cpu().numpy(), ref)
+        print(f"n=64 full quadrature, mixed path ({path} columns) vs oracle: rel Linf {err:.3e}")
+        assert err < 1e-5, path
+    assert not col.plan.dft_stalled
 
 
 def test_large_grid_n64_full_quadrature():

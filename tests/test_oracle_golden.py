@@ -4,7 +4,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import maxwellian, rel_linf
+from conftest import GOLDEN, maxwellian, rel_linf
 from oracle import fs_inelastic as fo
 from oracle import integrators as it
 from oracle import transport as tr
@@ -170,3 +170,25 @@ def test_fast_sweep_2d(golden):
         err = it.fast_sweep_step(f, d["v"], float(d["dx"]), float(d["kn"]), op, m.delta, dim=2)
         assert rel_linf(f, d["f"][k]) < 1e-12, k
         assert abs(err - d["err"][k]) <= 1e-12 * abs(d["err"][k]), k
+
+
+def test_c5_fixture_is_the_seeded_mixture(golden):
+    """The oracle-made 64^3 fixture: its input rebuilds from the stored mixture
+    parameters (the GPU test rebuilds f the same way), the generator's seed
+    reproduces those parameters, and Q is finite with a small mass defect
+    relative to |Q| (the reference operator does not conserve mass exactly)."""
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    import make_oracle_fixtures as mk
+
+    d = golden("c5_n64.npz")
+    w, u, T = mk.mixture_params()
+    assert np.array_equal(w, d["w"]) and np.array_equal(u, d["u"]) and np.array_equal(T, d["T"])
+    mesh = fo.Mesh(64, float(d["params"][1]), 48, 70)
+    assert abs(mesh.L - 10.0) < 1e-12
+    f = mk.mixture(mesh.v, w, u, T)
+    assert abs(f.sum() - float(d["f_sum"])) < 1e-12 * float(d["f_sum"])
+    q = d["q"]
+    assert q.shape == (64, 64, 64) and np.isfinite(q).all()
+    assert abs(q.sum()) < 0.1 * np.abs(q).sum()
