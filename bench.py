@@ -277,6 +277,184 @@ def measure_n64(pkg, device, cells=256, cells_fp64=2):
 
 
 # ---------------------------------------------------------------------------
+# ensemble configuration: 64 independent homogeneous problems, n drawn from
+# {16, 24, 32, 48} (16 each), e = e0 ~ U[0.2, 1], n_r = n / 2 radial nodes x the
+# 32-point design, L = 8, hard spheres; each f a sum of 2-4 Maxwellians (means
+# in [-2, 2]^3, T in [0.5, 2]) of unit mass; PFE macro-steps (K = 2 inner
+# Euler steps of 0.005, macro-step 0.02, kn = 1), Q = gain - loss
+# ---------------------------------------------------------------------------
+C3_KW = dict(dt=0.02, kn=1.0, integrator="PFE", inner_steps=[2], inner_dt=[0.005], with_loss=True)
+
+
+def ensemble_problem(pkg, count=64, seed=2026):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sizes = [16, 24, 32, 48]
+    configs, f0s = [], []
+    for i in range(count):
+        n = sizes[i % 4]
+        e = float(rng.uniform(0.2, 1.0))
+        cfg = {"velocity-mesh": {"nv": n, "s": S_L8, "nr": n // 2},
+               "spherical-design-rule": {"ssrule": "womersley", "nsphr": 32},
+               "collision-model": {"dim": 3, "type": "vhs", "e": e, "e0": e, "gamma": 1.0}}
+        v = pkg.SpectralMesh(cfg).v_center
+        k = int(rng.integers(2, 5))
+        f = sum(maxwellian(v, rng.uniform(0.5, 1.5), rng.uniform(-2.0, 2.0, 3), rng.uniform(0.5, 2.0))
+                for _ in range(k))
+        configs.append(cfg)
+        f0s.append(f / (f.sum() * (v[1] - v[0]) ** 3))
+    return configs, f0s
+
+
+def measure_c3(pkg, device, steps=5):
+    """Aggregate instance-evaluations per second of the 64-problem ensemble
+    (one captured graph per macro-step), and the per-instance relative L-inf
+    error of the mixed path against the FP64 path: of Q on the initial states,
+    and of f after the timed macro-steps."""
+    import torch
+
+    configs, f0s = ensemble_problem(pkg)
+    ens = pkg.Ensemble(configs, f0s, precision="mixed", device=device.index, **C3_KW)
+    tuning = [t for _, t in ens.autotune()]  # kernel choices per size class, timed on the device
+    dbl = pkg.Ensemble(configs, f0s, precision="double", device=device.index, **C3_KW)
+    qm, qd = ens.collide(), dbl.collide()
+    q_err = [float((a - b).abs().max() / b.abs().max()) for a, b in zip(qm, qd)]
+    warm = 2
+    for _ in range(warm):
+        ens.step()  # the first call captures the graph
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        ens.step()
+    b.record()
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) / 1e3
+    evals = len(configs) * C3_KW["inner_steps"][0] * steps
+    for _ in range(warm + steps):
+        dbl.step(use_graph=False)
+    torch.cuda.synchronize()
+    f_err = [float((x - y).abs().max() / y.abs().max()) for x, y in zip(ens.f, dbl.f)]
+    sizes = sorted({c["velocity-mesh"]["nv"] for c in configs})
+    out = {"config": "64 homogeneous problems, n_v in {16,24,32,48}^3 (16 each) on [-8,8]^3, e=e0~U[0.2,1], "
+                     "n_r=n/2 GL radial x 32-point design, 2-4 Maxwellian mixtures; PFE K=2 dt0=0.005 dt=0.02 kn=1",
+           "instances": len(configs), "macro_steps": steps, "instance_evals_per_s": evals / sec,
+           "ms_per_macro_step": sec / steps * 1e3, "plans": ens.plan_count, "tuning": tuning,
+           "q_rel_linf_err_vs_fp64_max": max(q_err), "f_rel_linf_err_vs_fp64_max": max(f_err),
+           "f_err_after_macro_steps": warm + steps,
+           "q_rel_linf_err_by_n": {str(n): max(e for e, c in zip(q_err, configs) if c["velocity-mesh"]["nv"] == n)
+                                   for n in sizes}}
+    del ens, dbl
+    torch.cuda.empty_cache()
+    return out
+
+
+# ---------------------------------------------------------------------------
+# stiff telescopic configuration: TPI3 at kn = 1e-4 on n_x = 512 periodic
+# cells, rho = 1 + 0.2 sin(2 pi x), T = 1 + 0.1 cos(2 pi x), zero velocity,
+# local Maxwellians; 32^3 on [-8, 8]^3, 32 x 32 quadrature, e = e0 = 0.9,
+# hard spheres, mass-mode fix on.  Levels dt = (1e-5, 2.5e-5, 6.25e-5), K = 2
+# each, macro-step 2e-4 (M = 0.5, 0.5, 1.2; advection CFL 0.79; the inner
+# step keeps the collision term's explicit bound, nu dt0 / kn <= 0.62).
+# ---------------------------------------------------------------------------
+C4_NX, C4_KN, C4_E = 512, 1e-4, 0.9
+C4_K, C4_H, C4_DT, C4_TEND = [2, 2, 2], [1e-5, 2.5e-5, 6.25e-5], 2e-4, 0.05
+
+
+def c4_state(v, nx=C4_NX):
+    import numpy as np
+
+    x = (np.arange(nx) + 0.5) / nx
+    return np.stack([maxwellian(v, 1 + 0.2 * math.sin(2 * math.pi * xi), (0, 0, 0),
+                                1 + 0.1 * math.cos(2 * math.pi * xi)) for xi in x])
+
+
+def c4_solver(pkg, precision, device, f0):
+    import torch
+
+    cfg = {"velocity-mesh": {"nv": 32, "s": S_L8, "nr": 32},
+           "spherical-design-rule": {"ssrule": "womersley", "nsphr": 32},
+           "collision-model": {"dim": 3, "type": "vhs", "e": C4_E, "e0": C4_E, "gamma": 1.0}}
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, with_loss=True, mass_fix=True,
+                                      batch_max=C4_NX, device=device.index)
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": C4_NX, "nv": 32},
+                       device=device.index)
+    sol.state.f.copy_(torch.as_tensor(f0))
+    solver = pkg.BoltzmannSolver1D(C4_KN, collision_operator=col)
+    solver.all_bcs = pkg.BC.periodic
+    solver.time_integrator = "TPI3"
+    solver.inner_steps = list(C4_K)
+    solver.inner_dt = list(C4_H)
+    solver.dt = C4_DT
+    solver.setup(sol)
+    return col, sol, solver
+
+
+def measure_c4(pkg, device, macro_steps=10, fp64_steps=1):
+    """TPI3 macro-steps of the stiff periodic workload in mixed precision:
+    cell-evaluations per second (device time, graph replays), total mass and
+    energy after every macro-step relative to the start (FP64 moments), and
+    the relative L-inf state error against the FP64 path after each of the
+    first `fp64_steps` macro-steps."""
+    import numpy as np
+    import torch
+
+    v = (np.arange(32) + 0.5) * (16.0 / 32) - 8.0  # the 32^3 grid on [-8, 8]^3 (cell centres)
+    col, sol, solver = c4_solver(pkg, "mixed", device, c4_state(v))
+    f0 = sol.f.clone()
+    st = sol.state
+
+    def mass_energy():
+        rho, u, T = (np.asarray(x) for x in st.moments())
+        m = float(np.sum(rho))
+        e = float(np.sum(rho * (1.5 * T + 0.5 * np.sum(np.asarray(u) ** 2, axis=-1))))
+        return m, e, float(np.mean(T))
+
+    m0, e0, T0 = mass_energy()
+    stream = solver._get_stream(device)
+    solver.step(sol, False, 0.0, C4_DT)  # capture the macro-step graph (excluded from the record below)
+    sol.state.f.copy_(f0)
+    torch.cuda.synchronize()
+    keep = []
+    rec, ms = [], 0.0
+    for k in range(macro_steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            solver.step(sol, False, k * C4_DT, (k + 1) * C4_DT)
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms += a.elapsed_time(b)
+        m, e, T = mass_energy()
+        rec.append({"t": (k + 1) * C4_DT, "mass_rel": m / m0 - 1.0, "energy_rel": e / e0 - 1.0, "T_mean": T,
+                    "finite": bool(torch.isfinite(sol.f).all())})
+        if k < fp64_steps:
+            keep.append(sol.f.clone())
+    evals = 8 * C4_NX * macro_steps
+    out = {"config": f"TPI3 kn={C4_KN}, n_x={C4_NX} periodic, rho=1+0.2sin(2pi x), T=1+0.1cos(2pi x), 32^3 on "
+                     f"[-8,8]^3, 32x32, e=e0={C4_E}, hard spheres, mass fix; levels dt={C4_H}, K={C4_K}, "
+                     f"macro dt={C4_DT}", "cells": C4_NX, "macro_steps": macro_steps,
+           "cell_evals_per_s": evals / (ms / 1e3), "ms_per_macro_step": ms / macro_steps,
+           "mass_drift_max": max(abs(r["mass_rel"]) for r in rec), "energy_rel_end": rec[-1]["energy_rel"],
+           "T_mean_end": rec[-1]["T_mean"], "t_end": rec[-1]["t"], "all_finite": all(r["finite"] for r in rec),
+           "per_macro_step": rec if macro_steps <= 20 else rec[:: max(1, macro_steps // 20)] + [rec[-1]]}
+    del col, sol, solver
+    if fp64_steps:
+        colD, solD, solverD = c4_solver(pkg, "double", device, f0.cpu().numpy())
+        errs = []
+        for k in range(fp64_steps):
+            solverD.step(solD, False, k * C4_DT, (k + 1) * C4_DT)
+            torch.cuda.synchronize()
+            errs.append(float((keep[k] - solD.f).abs().max() / solD.f.abs().max()))
+        out["f_rel_linf_err_vs_fp64"] = errs
+        del colD, solD, solverD
+    torch.cuda.empty_cache()
+    return out
+
+
+# ---------------------------------------------------------------------------
 # CPU baseline (the oracle restatement of the reference operator, host cores)
 # ---------------------------------------------------------------------------
 def cpu_baseline(budget_s=15.0, max_cells=64):
@@ -418,6 +596,14 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's default kernel choices")
     ap.add_argument("--no-n64", action="store_true", help="skip the 64^3 configuration measurement")
+    ap.add_argument("--no-c3", action="store_true", help="skip the ensemble configuration measurement")
+    ap.add_argument("--no-c4", action="store_true", help="skip the stiff telescopic configuration measurement")
+    ap.add_argument("--c4-steps", type=int, default=10,
+                    help="TPI3 macro-steps of the stiff configuration (250 reach its end time t = 0.05)")
+    ap.add_argument("--c4-fp64-steps", type=int, default=1,
+                    help="macro-steps of the stiff configuration compared against the FP64 path")
+    ap.add_argument("--c4-only", action="store_true", help="measure only the stiff configuration and exit")
+    ap.add_argument("--c3-only", action="store_true", help="measure only the ensemble configuration and exit")
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: run 3 Q(f,f) evaluations on this many cells of the workload and exit")
     ap.add_argument("--ncu-case64", type=int, default=0,
@@ -431,6 +617,16 @@ def main():
         return ncu_case(args.ncu_case)
     if args.ncu_case64:
         return ncu_case64(args.ncu_case64, args.dft_path)
+    if args.c4_only or args.c3_only:
+        import torch
+
+        import proj_int_inelastic_gb300 as pkg
+
+        dev = torch.device("cuda:0")
+        out = {"c4": measure_c4(pkg, dev, args.c4_steps, args.c4_fp64_steps)} if args.c4_only else {
+            "c3": measure_c3(pkg, dev)}
+        print(json.dumps(out), flush=True)
+        return 0
     args.warmup = max(3, args.warmup)
 
     import numpy as np
@@ -640,6 +836,10 @@ def main():
             line["speedup_vs_fp64_gpu"] = collide_rate / torch64
     if rank == 0 and not args.no_n64:
         line["n64"] = measure_n64(pkg, device)
+    if rank == 0 and not args.no_c3:
+        line["c3"] = measure_c3(pkg, device)
+    if rank == 0 and not args.no_c4:
+        line["c4"] = measure_c4(pkg, device, args.c4_steps, args.c4_fp64_steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if rank == 0:

@@ -89,6 +89,18 @@ int pii_plan_create_nd(pii_plan** out, int dim, int n, int n_r, int n_sigma, con
                        int precision, int64_t batch_max, int device);
 int pii_plan_dim(const pii_plan* plan);
 
+/*
+ * Per-cell restitution (generalises the operator-wide e, e0 of
+ * load_parameters, src/collision/inelastic_collisions.py:30-52,77-80, to an
+ * ensemble of independent problems in one plan): cell c of every later call
+ * uses (e[c], e0[c]) for its gain tables, c < count <= batch_max; calls with
+ * more than `count` cells return PII_ERR_SIZE.  count = 0 restores the plan's
+ * own (e, e0) for every cell.  3D-velocity plans; the cluster gain kernel
+ * (gain path 1) is then unavailable.  Synchronises the device and drops
+ * captured step graphs.  e, e0: host arrays.
+ */
+int pii_plan_set_restitution(pii_plan* plan, const double* e, const double* e0, int64_t count);
+
 /* Free the plan, its tables and workspace (no reference counterpart: the
  * reference's numpy/cupy arrays are garbage collected). */
 int pii_plan_destroy(pii_plan* plan);

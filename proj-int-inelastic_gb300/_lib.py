@@ -42,6 +42,7 @@ SIGNATURES = {
     "pii_plan_create_nd": (_c_int, [ctypes.POINTER(_vp), _c_int, _c_int, _c_int, _c_int, _pdbl, _pdbl, _pdbl, _c_dbl,
                                     _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_i64, _c_int]),
     "pii_plan_dim": (_c_int, [_vp]),
+    "pii_plan_set_restitution": (_c_int, [_vp, _pdbl, _pdbl, _c_i64]),
     "pii_plan_destroy": (_c_int, [_vp]),
     "pii_plan_workspace_bytes": (_c_i64, [_vp]),
     "pii_plan_set_gain_path": (_c_int, [_vp, _c_int]),

@@ -268,6 +268,17 @@ class Plan:
         _lib.check(self._lib.pii_plan_set_dft_path(self.handle, _code(DFT_PATHS, dft_path, "dft_path")),
                    "pii_plan_set_dft_path")
 
+    def set_restitution(self, e, e0):
+        """Per-cell restitution: cell c of later calls uses (e[c], e0[c])
+        (``pii_plan_set_restitution``); empty sequences restore the plan's own."""
+        e = np.ascontiguousarray(e, np.float64)
+        e0 = np.ascontiguousarray(e0, np.float64)
+        if e.shape != e0.shape or e.ndim != 1:
+            raise ValueError("e and e0 must be 1D sequences of the same length")
+        _lib.check(self._lib.pii_plan_set_restitution(self.handle, _lib.dptr(e), _lib.dptr(e0), len(e)),
+                   "pii_plan_set_restitution")
+        self.restitution_sets = len(e)
+
     def dft_test_hooks(self, wait_limit=1 << 22, withhold=False):
         """Test hooks of the tensor-core DFT's bounded waits
         (``pii_plan_dft_test_hooks``): polls before a role gives up, and
@@ -391,6 +402,10 @@ class FSInelasticVHSCollision:
         return self._ensure_plan(self._batch_max)
 
     def _ensure_plan(self, cells):
+        sets = getattr(self._plan, "restitution_sets", 0)
+        if sets > 1 and cells > sets:
+            # a grown plan would drop the per-cell restitution: refuse like the C ABI does
+            raise ValueError(f"{cells} cells for a plan with {sets} per-cell restitution sets")
         if self._plan is None or self._plan.batch_max < cells:
             if self._plan is not None:
                 torch.cuda.synchronize(self._device)

@@ -112,7 +112,9 @@ struct ColTcArgs {
   const uint4* fimg;    // DFT matrix images of the direction (F_even hi, lo, F_odd hi, lo)
   const float2* ephase;  // [Q][3][64]
   const float2* gphase;  // [Q][3][64]
-  const float* gsk;      // [n_r][|k_b| < 33][SLICE]: gsinc[r][k_b^2 + k_c^2 + k_a^2]
+  const float* gsk;      // [sets][n_r][|k_b| < 33][SLICE]: gsinc[r][k_b^2 + k_c^2 + k_a^2]
+  int64_t gph_stride;    // complex elements of gphase per restitution set (0: one set)
+  int64_t gsk_stride;    // floats of gsk per restitution set (0: one set)
   const float* colb;     // PSTART: [cells][N2] max over a of |f^(a, j)|_1 (k_col_bound)
   int ns;
   int64_t items, c0, p0, np;
@@ -423,12 +425,13 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
           unsigned char* g = sm + OFF_G + b * GROW * 4;
           mbar_arrive_tx(gfull + b, 2 * SLICE * 4 + PROW);
           ++gphases[b];
-          const float* gr = a.gsk + int64_t(pair / a.ns) * KS * SLICE;
+          const int64_t cell = a.c0 + ci;  // its restitution set, when the plan has one per cell
+          const float* gr = a.gsk + cell * a.gsk_stride + int64_t(pair / a.ns) * KS * SLICE;
           for (int h = 0; h < 2; ++h) {  // columns j0 .. j0 + 127 span k_b rows j0 / 64 and j0 / 64 + 1
             const int kb = kval(j0 / NV + h, NV);
             bulk_g2s(g + h * SLICE * 4, gr + (kb < 0 ? -kb : kb) * SLICE, SLICE * 4, gfull + b);
           }
-          bulk_g2s(g + 2 * SLICE * 4, a.gphase + pair * 3 * NV, PROW, gfull + b);
+          bulk_g2s(g + 2 * SLICE * 4, a.gphase + cell * a.gph_stride + pair * 3 * NV, PROW, gfull + b);
         }
       }
       // drain: wait (bounded, not cut short by the abort flag) for the last copy
@@ -583,24 +586,41 @@ int col_tc_prepare(pii_plan* p) {
     PII_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&p->dft_err), p->dft_err_host, 0));
     p->bytes += int64_t(img.size() * 2 + sizeof(int));
   }
-  if (!p->dft_gs) {  // gsinc[r][k_b^2 + k_c^2 + k_a^2] by (r, |k_b|, |k_c|, |k_a|) (bulk-copy sources)
-    const int M1 = p->tab.M + 1;
-    std::vector<float> gs(size_t(p->nr) * M1), gk(size_t(p->nr) * KS * SLICE, 0.f);
-    PII_CUDA(cudaMemcpy(gs.data(), p->tab.gsinc, gs.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    for (int r = 0; r < p->nr; ++r)
-      for (int kb = 0; kb < KS; ++kb)
-        for (int kc = 0; kc < KS; ++kc)
-          for (int ka = 0; ka < KS; ++ka)
-            gk[(size_t(r) * KS + kb) * SLICE + kc * KA_PITCH + ka] = gs[size_t(r) * M1 + kb * kb + kc * kc + ka * ka];
-    PII_CUDA(cudaMalloc(&p->dft_gs, gk.size() * sizeof(float)));
-    PII_CUDA(cudaMemcpy(p->dft_gs, gk.data(), gk.size() * sizeof(float), cudaMemcpyHostToDevice));
-    p->bytes += int64_t(gk.size() * sizeof(float));
-  }
+  if (!p->dft_gs) PII_TRY(col_tc_gain_tables(p));
   if (!p->dft_colb) {
     PII_CUDA(cudaMalloc(&p->dft_colb, size_t(p->batch_max) * N2 * sizeof(float)));
     p->bytes += int64_t(p->batch_max) * N2 * sizeof(float);
   }
   PII_CUDA(cudaDeviceGetAttribute(&p->dft_ctas, cudaDevAttrMultiProcessorCount, p->device));
+  return PII_OK;
+}
+
+// gsinc[r][k_b^2 + k_c^2 + k_a^2] by (set, r, |k_b|, |k_c|, |k_a|): the bulk-copy
+// sources of the PEND epilogue's sinc slices, one block per restitution set
+int col_tc_gain_tables(pii_plan* p) {
+  using namespace ctc;
+  const int M1 = p->tab.M + 1;
+  const int64_t sets = p->tab.nsets;
+  const size_t per = size_t(p->nr) * KS * SLICE;
+  std::vector<float> gs(size_t(sets) * p->nr * M1), gk(size_t(sets) * per, 0.f);
+  PII_CUDA(cudaMemcpy(gs.data(), p->tab.gsinc, gs.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  for (int64_t st = 0; st < sets; ++st)
+    for (int r = 0; r < p->nr; ++r)
+      for (int kb = 0; kb < KS; ++kb)
+        for (int kc = 0; kc < KS; ++kc)
+          for (int ka = 0; ka < KS; ++ka)
+            gk[size_t(st) * per + (size_t(r) * KS + kb) * SLICE + kc * KA_PITCH + ka] =
+                gs[(size_t(st) * p->nr + r) * M1 + kb * kb + kc * kc + ka * ka];
+  if (p->dft_gs) {
+    cudaFree(p->dft_gs);
+    p->bytes -= p->dft_gs_bytes;
+    p->dft_gs = nullptr;
+  }
+  PII_CUDA(cudaMalloc(&p->dft_gs, gk.size() * sizeof(float)));
+  PII_CUDA(cudaMemcpy(p->dft_gs, gk.data(), gk.size() * sizeof(float), cudaMemcpyHostToDevice));
+  p->dft_gs_bytes = int64_t(gk.size() * sizeof(float));
+  p->bytes += p->dft_gs_bytes;
+  p->dft_gs_stride = sets > 1 ? int64_t(per) : 0;
   return PII_OK;
 }
 
@@ -641,6 +661,8 @@ int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int
   a.ephase = static_cast<const float2*>(p->tab.ephase);
   a.gphase = static_cast<const float2*>(p->tab.gphase);
   a.gsk = static_cast<const float*>(p->dft_gs);
+  a.gph_stride = p->tab.gph_stride;
+  a.gsk_stride = p->dft_gs_stride;
   a.colb = static_cast<const float*>(p->dft_colb);
   a.ns = p->ns;
   a.items = items;

@@ -116,6 +116,11 @@ int collide_impl(pii_plan* p, const double* f, double* q, int64_t cells, int wit
     set_error("pii_collide: f and q must not alias");
     return PII_ERR_ARG;
   }
+  if (p->tab.nsets > 1 && cells > p->tab.nsets) {
+    set_error("pii_collide: cells = %lld beyond the plan's %lld per-cell restitution sets", (long long)cells,
+              (long long)p->tab.nsets);
+    return PII_ERR_SIZE;
+  }
   PII_TRY(dft_stall_check(p));  // a stall of an earlier launch on this plan
   int st = PII_OK;
   if (p->dim == 2)
@@ -166,8 +171,10 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
   };
   std::vector<Cand> cands;
   const bool cluster_ok = plan->gc_clusters > 0;
+  const bool cluster_path_ok = cluster_ok && plan->tab.nsets == 1;  // the cluster kernel takes one table set
   if (cluster_ok) {
-    for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points, 0});
+    if (cluster_path_ok)
+      for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points, 0});
     cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points, 0});  // even split: no item knob
     if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points, 0});
   }
@@ -253,6 +260,10 @@ extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
   }
   if (path != 0 && (plan->gc_clusters <= 0 || plan->gp_ctas <= 0)) {
     pii::set_error("pii_plan_set_gain_path: the fused kernels exist for n = 32, FP32 plans only");
+    return PII_ERR_ARG;
+  }
+  if (path == 1 && plan->tab.nsets > 1) {
+    pii::set_error("pii_plan_set_gain_path: the cluster kernel takes one restitution set, not one per cell");
     return PII_ERR_ARG;
   }
   plan->gain_path = path;

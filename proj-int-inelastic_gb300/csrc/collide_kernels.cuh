@@ -96,8 +96,10 @@ __global__ void __launch_bounds__(128) k_col(ColArgs args) {
 #pragma unroll
     for (int a = 0; a < NV; ++a) x[a] = io[a * N2];
     fft_line<NV, -1>(x);
-    const V* gp = reinterpret_cast<const V*>(args.tab.gphase) + pair * 3 * NV;
-    const T* gs = reinterpret_cast<const T*>(args.tab.gsinc) + int64_t(ir) * (args.tab.M + 1);
+    const int64_t cell = args.c0 + ci;  // its restitution set, when the plan has one per cell
+    const V* gp = reinterpret_cast<const V*>(args.tab.gphase) + cell * args.tab.gph_stride + pair * 3 * NV;
+    const T* gs =
+        reinterpret_cast<const T*>(args.tab.gsinc) + cell * args.tab.gs_stride + int64_t(ir) * (args.tab.M + 1);
     const V gbc = cmul(gp[NV + jb], gp[2 * NV + jc]);
     const int mbc = kb * kb + kc * kc;
     static_for<0, NV>([&](auto ai) {

@@ -59,6 +59,9 @@ struct GainParityArgs {
   const float2* gpar;    // [Q][2][32]
   const float* gsx;      // [n_r][513][20]
   const float* gsxc;     // [n_r][153][17] (packed mode)
+  // elements per restitution set (0: one set for every cell) of gphase
+  // (complex), gpar (complex), gsx and gsxc
+  int64_t gph_stride, gpar_stride, gsx_stride, gsxc_stride;
   int ns, Q;
   int QP;                // passes per (cell, parity): Q, or the antipodal pairs when packed
   const int* reps;       // [QP] pair index of each packed pass (packed mode)
@@ -396,6 +399,12 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       }
     }
     const float2* fh = a.fhat + cell * N3;
+    // the cell's restitution set (the same tables for every cell when there is one)
+    const float2* gph_c = a.gphase + cell * a.gph_stride;
+    const float2* gpar_c = a.gpar + cell * a.gpar_stride;
+    const float* gsx_c = a.gsx + cell * a.gsx_stride;
+    const float* gsxc_c = a.gsxc + cell * a.gsxc_stride;
+    if (a.gsxc_stride) gsc_ir = -1;  // another cell's slab may be staged
     {
       // fS[m][c][b] = f[cell][2 m + par][b][c] (read before the first plane pass:
       // the stage-A barrier orders it)
@@ -422,7 +431,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
         const int ir = p / a.ns;
         if (ir != gsc_ir) {
           __syncthreads();
-          const float* src = a.gsxc + int64_t(ir) * GSC;
+          const float* src = gsxc_c + int64_t(ir) * GSC;
           for (int e = t; e < GSC; e += THREADS) gsc[e] = src[e];
           gsc_ir = ir;
         }
@@ -433,7 +442,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
         // already passed (a thread still in the previous stage C reads the other
         // gain buffer).
         if (t >= 48 && t < 96)
-          cp_async16(rows + 192 * (ip & 1) + 96 + 2 * (t - 48), a.gphase + int64_t(p) * 96 + 2 * (t - 48));
+          cp_async16(rows + 192 * (ip & 1) + 96 + 2 * (t - 48), gph_c + int64_t(p) * 96 + 2 * (t - 48));
         if (t < 48 && ip + 1 < p1)
           cp_async16(rows + 192 * ((ip + 1) & 1) + 2 * t, a.ephase + int64_t(a.reps[ip + 1]) * 96 + 2 * t);
       }
@@ -480,9 +489,9 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       __syncthreads();
       // ---- C: the thread's two columns (the previous pair's TMEM stores are complete first)
       {
-        const float2* gp = PACK ? rows + 192 * (ip & 1) + 96 : a.gphase + int64_t(p) * 96;
-        const float2* gpp = a.gpar + (int64_t(p) * 2 + par) * 32;
-        const float* gsr = a.gsx + int64_t(p / a.ns) * (513 * 20);
+        const float2* gp = PACK ? rows + 192 * (ip & 1) + 96 : gph_c + int64_t(p) * 96;
+        const float2* gpp = gpar_c + (int64_t(p) * 2 + par) * 32;
+        const float* gsr = gsx_c + int64_t(p / a.ns) * (513 * 20);
         const int4 uc = a.ucols[t];
         tm_wait_st();
         if constexpr (PACK) {
@@ -682,6 +691,10 @@ int gain_parity_run(pii_plan* p, int64_t cells, cudaStream_t s, bool packed) {
   a.gpar = static_cast<const float2*>(p->tab.gpar);
   a.gsx = static_cast<const float*>(p->tab.gsx);
   a.gsxc = static_cast<const float*>(p->tab.gsxc);
+  a.gph_stride = p->tab.gph_stride;
+  a.gpar_stride = p->tab.gpar_stride;
+  a.gsx_stride = p->tab.gsx_stride;
+  a.gsxc_stride = p->tab.gsxc_stride;
   a.ns = p->ns;
   a.Q = p->Q;
   a.QP = QP;

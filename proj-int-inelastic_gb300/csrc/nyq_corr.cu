@@ -56,6 +56,8 @@ struct NyqArgs {
   const float2* gphase;  // [Q][3][32]
   const float* gsinc;    // [n_r][M + 1]
   const int* reps;       // [QP] representative pair of each antipodal pass
+  int64_t gph_stride;    // complex elements of gphase per restitution set (0: one set)
+  int64_t gs_stride;     // floats of gsinc per restitution set (0: one set)
   int M, ns, QP;
   int64_t cells;
   int blocks;            // CTAs per cell
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
       const int sidx = i / 96, w = (i / 48) & 1, e = 2 * (i % 48);
       float2* d = dst + sidx * 192 + w * 96 + e;
       if (sidx < nbn) {
-        cp_async16(d, (w == 0 ? a.ephase : a.gphase) + int64_t(a.reps[jb + sidx]) * 96 + e);
+        cp_async16(d, (w == 0 ? a.ephase : a.gphase + cell * a.gph_stride) + int64_t(a.reps[jb + sidx]) * 96 + e);
       } else {
         d[0] = make_float2(0.f, 0.f);
         d[1] = make_float2(0.f, 0.f);
@@ -334,7 +336,7 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
       for (int s = 0; s < PB; ++s) {
         if (s >= nb) break;
         const int p = a.reps[ib + s];
-        const float gsv = a.gsinc[int64_t(p / a.ns) * (a.M + 1) + kk];
+        const float gsv = a.gsinc[cell * a.gs_stride + int64_t(p / a.ns) * (a.M + 1) + kk];
         const float2 gm = minus_from(Rows + s * 192 + 96, Fac + s * 384 + 192, plane, r, c);
         const float wx = gsv * gm.x, wy = gsv * gm.y;
         const float2 u = P[(s * 3 + plane) * PL + sw(r, c)];
@@ -390,6 +392,8 @@ int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.gphase = static_cast<const float2*>(p->tab.gphase);
   a.gsinc = static_cast<const float*>(p->tab.gsinc);
   a.reps = p->ap_reps;
+  a.gph_stride = p->tab.gph_stride;
+  a.gs_stride = p->tab.gs_stride;
   a.M = p->tab.M;
   a.ns = p->ns;
   a.QP = p->ap_count;

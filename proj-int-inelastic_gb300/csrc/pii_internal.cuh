@@ -104,6 +104,11 @@ struct Tables {
   void* lossk = nullptr;
   void* lapl = nullptr;
   int M = 0;
+  // restitution sets of the gain tables (gphase, gsinc, gpar, gsx, gsxc): with
+  // more than one, cell c of a call uses set c and each stride is the elements
+  // (complex ones for the phase rows) per set; with one, the strides are 0
+  int64_t nsets = 1;
+  int64_t gph_stride = 0, gs_stride = 0, gpar_stride = 0, gsx_stride = 0, gsxc_stride = 0;
 };
 
 struct GraphKey {
@@ -188,7 +193,8 @@ struct pii_plan {
   uint32_t dft_wait_limit = 1u << 22;  // mbarrier polls before a k_col_tc role gives up
   int dft_withhold = 0;     // test hook: k_col_tc's TMA thread issues no copies
   int dft_ctas = 0;         // resident CTAs of k_col_tc (one per SM)
-  void* dft_gs = nullptr;   // gsinc by (r, |k_b|, |k_c|, |k_a|) slices (TMA sources)
+  void* dft_gs = nullptr;   // gsinc by (set, r, |k_b|, |k_c|, |k_a|) slices (TMA sources)
+  int64_t dft_gs_bytes = 0, dft_gs_stride = 0;  // its size, and floats per restitution set (0: one set)
   void* dft_colb = nullptr; // [batch_max][n^2] column bounds max_a |f^|_1 (k_col_bound)
   // TMA tensor maps (CUtensorMap, 128 bytes each) of f^ and of the chunk buffer
   // as 2D FP32 arrays [rows of 64 (a) per grid][8192 floats per row]
@@ -241,6 +247,7 @@ int nyq_corr_run(pii_plan* p, int64_t cells, cudaStream_t s);
 int col_tc_prepare(pii_plan* p);
 int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int64_t np, cudaStream_t s);
 int col_tc_bounds(pii_plan* p, int64_t cells, cudaStream_t s);
+int col_tc_gain_tables(pii_plan* p);  // (re)builds the sinc slices of every restitution set
 // col_tc.cu: PII_ERR_STALL if a tensor-core DFT launch of an earlier call gave
 // up waiting (read from mapped host memory without a synchronisation; cleared
 // once reported)

@@ -13,6 +13,8 @@
 #include <cstring>
 #include <type_traits>
 
+#include <utility>
+
 #include "pii_internal.cuh"
 
 namespace pii {
@@ -104,15 +106,18 @@ static double bessel_j0(double x) {
   return s / nodes;
 }
 
+// Tables that do not depend on the restitution law: the phase rows of the
+// reference's exp table, the a-parity phase rows, the loss and Laplacian
+// factors (src/collision/inelastic_collisions.py:62-69,105-114)
 template <typename T>
-static int upload_tables(pii_plan* p) {
+static int upload_shared_tables(pii_plan* p) {
   const int n = p->n, nr = p->nr, ns = p->ns, Q = p->Q, dim = p->dim;
   const int M = dim * (n / 2) * (n / 2);
   p->tab.M = M;
   const double pi = 3.141592653589793238462643383279502884;
   // per-axis rows: always 3 per pair (the 2D operator leaves the third unused)
-  std::vector<T> eph(size_t(Q) * 3 * n * 2, T(0)), gph(size_t(Q) * 3 * n * 2, T(0));
-  std::vector<T> gs(size_t(nr) * (M + 1)), lk(M + 1), lp(M + 1);
+  std::vector<T> eph(size_t(Q) * 3 * n * 2, T(0));
+  std::vector<T> lk(M + 1), lp(M + 1);
   const double invN = 1.0 / double(p->N);
   // sphere (circle) constant 2 pi^{d/2} / Gamma(d/2): 4 pi in 3D, 2 pi in 2D (:50-52)
   const double sphr = dim == 3 ? 4.0 * pi : 2.0 * pi;
@@ -121,15 +126,8 @@ static int upload_tables(pii_plan* p) {
   std::vector<double> lk_d(M + 1, 0.0);
   for (int ir = 0; ir < nr; ++ir) {
     const double r = p->r[ir], wr = p->wr[ir];
-    // restitution law and exponential factor (inelastic_collisions.py:77-80)
-    const double er = 0.5 * (p->e0 - p->e) * std::tanh(r - 0.5 * p->R) + 0.5 * (p->e0 + p->e);
-    const double afac = 0.25 * pi * (1.0 + er) / p->L;
     const double rg = std::pow(r, p->gamma + dim - 1.0);  // pre_fac(r) / sphr  (:54-55)
-    for (int m = 0; m <= M; ++m) {
-      const double kn = std::sqrt(double(m));
-      gs[size_t(ir) * (M + 1) + m] = T(rg * wr * p->wsigma * kern(afac * r * kn));
-      lk_d[m] += sphr * rg * wr * kern(pi * r * kn / p->L);  // loss (:109-114)
-    }
+    for (int m = 0; m <= M; ++m) lk_d[m] += sphr * rg * wr * kern(pi * r * std::sqrt(double(m)) / p->L);  // loss
     for (int is = 0; is < ns; ++is) {
       const int pair = ir * ns + is;
       for (int d = 0; d < dim; ++d) {
@@ -137,25 +135,26 @@ static int upload_tables(pii_plan* p) {
         for (int i = 0; i < n; ++i) {
           const int k = i < n / 2 ? i : i - n;
           const double th_e = -pi * r * sd * double(k) / p->L;
-          const double th_g = afac * r * sd * double(k);
           const double sc = (d == 0) ? invN : 1.0;
           const size_t o = ((size_t(pair) * 3 + d) * n + i) * 2;
           eph[o] = T(sc * std::cos(th_e));
           eph[o + 1] = T(sc * std::sin(th_e));
-          gph[o] = T(std::cos(th_g));
-          gph[o + 1] = T(std::sin(th_g));
         }
       }
     }
   }
+  auto up = [&](void** dst, const void* src, size_t bytes) -> int {
+    PII_CUDA(cudaMalloc(dst, bytes));
+    PII_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+    p->bytes += int64_t(bytes);
+    return PII_OK;
+  };
   if (std::is_same<T, float>::value && n == 32 && dim == 3) {
-    // a-parity rows: the first-axis rows with the radix-2 twiddles of the
+    // a-parity phase rows: the first-axis rows with the radix-2 twiddles of the
     // parity split folded in, evaluated in FP64 (angles reduced exactly)
-    std::vector<T> ep2(size_t(Q) * 2 * 32 * 2), gp2(size_t(Q) * 2 * 32 * 2);
+    std::vector<T> ep2(size_t(Q) * 2 * 32 * 2);
     for (int ir = 0; ir < nr; ++ir) {
       const double r = p->r[ir];
-      const double er = 0.5 * (p->e0 - p->e) * std::tanh(r - 0.5 * p->R) + 0.5 * (p->e0 + p->e);
-      const double afac = 0.25 * pi * (1.0 + er) / p->L;
       for (int is = 0; is < ns; ++is) {
         const int pair = ir * ns + is;
         const double sd = p->sigma[size_t(is) * 3];
@@ -169,53 +168,136 @@ static int upload_tables(pii_plan* p) {
                                 (k >= 16 && par ? pi : 0.0);
             ep2[o] = T(invN * std::cos(th_e));
             ep2[o + 1] = T(invN * std::sin(th_e));
-            const double th_g = afac * r * sd * double(ks) - 2.0 * pi * double(par * k) / 32.0;
-            gp2[o] = T(std::cos(th_g));
-            gp2[o + 1] = T(std::sin(th_g));
           }
       }
     }
-    auto up2 = [&](void** dst, const std::vector<T>& v) -> int {
-      PII_CUDA(cudaMalloc(dst, v.size() * sizeof(T)));
-      PII_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
-      p->bytes += int64_t(v.size() * sizeof(T));
-      return PII_OK;
-    };
-    PII_TRY(up2(&p->tab.epar, ep2));
-    PII_TRY(up2(&p->tab.gpar, gp2));
-    // per-column rows of the radial sinc table: gsinc[r][m_bc + q^2], q = |k_a| <= 16
-    std::vector<T> gsx(size_t(nr) * 513 * 20, T(0));
-    for (int ir = 0; ir < nr; ++ir)
-      for (int mbc = 0; mbc <= 512; ++mbc)
-        for (int q = 0; q <= 16 && mbc + q * q <= M; ++q)
-          gsx[(size_t(ir) * 513 + mbc) * 20 + q] = gs[size_t(ir) * (M + 1) + mbc + q * q];
-    PII_TRY(up2(&p->tab.gsx, gsx));
-    // the same by (|k_b|, |k_c|) pair, u = min <= v = max (index v (v + 1) / 2 + u, 153
-    // pairs), 17 values q = 0..16: one radial node's slab is 10.4 KB (shared memory)
-    std::vector<T> gsxc(size_t(nr) * 153 * 17, T(0));
-    for (int ir = 0; ir < nr; ++ir)
-      for (int v = 0; v <= 16; ++v)
-        for (int u = 0; u <= v; ++u)
-          for (int q = 0; q <= 16; ++q)
-            gsxc[(size_t(ir) * 153 + v * (v + 1) / 2 + u) * 17 + q] = gs[size_t(ir) * (M + 1) + u * u + v * v + q * q];
-    PII_TRY(up2(&p->tab.gsxc, gsxc));
+    PII_TRY(up(&p->tab.epar, ep2.data(), ep2.size() * sizeof(T)));
   }
   for (int m = 0; m <= M; ++m) {
     lk[m] = T(lk_d[m]);
     lp[m] = T(-pi * pi / (p->L * p->L) * double(m));  // (:69)
   }
+  PII_TRY(up(&p->tab.ephase, eph.data(), eph.size() * sizeof(T)));
+  PII_TRY(up(&p->tab.lossk, lk.data(), lk.size() * sizeof(T)));
+  PII_TRY(up(&p->tab.lapl, lp.data(), lp.size() * sizeof(T)));
+  return PII_OK;
+}
+
+// Tables of the gain that depend on the restitution law through
+// a(r) = pi (1 + e(r)) / (4 L), e(r) = (e0 - e) tanh(r - R / 2) / 2 + (e0 + e) / 2
+// (src/collision/inelastic_collisions.py:77-103): the gain phase rows, the
+// radial sinc table and, for the fused n = 32 kernels, their derived forms.
+// One set per (e, e0) of `sets`, stored set after set; the strides are the
+// elements per set when there is more than one set (cell c then uses set c)
+// and 0 otherwise.
+template <typename T>
+static int upload_gain_tables(pii_plan* p, const std::vector<std::pair<double, double>>& sets) {
+  const int n = p->n, nr = p->nr, ns = p->ns, Q = p->Q, dim = p->dim;
+  const int M = dim * (n / 2) * (n / 2);
+  const size_t S = sets.size();
+  const double pi = 3.141592653589793238462643383279502884;
+  auto kern = [dim](double x) { return dim == 3 ? sinc(x) : bessel_j0(x); };
+  const size_t gph_set = size_t(Q) * 3 * n, gs_set = size_t(nr) * (M + 1);
+  std::vector<T> gph(S * gph_set * 2, T(0)), gs(S * gs_set);
+  const bool fused = std::is_same<T, float>::value && n == 32 && dim == 3;
+  const size_t gp2_set = size_t(Q) * 2 * 32, gsx_set = size_t(nr) * 513 * 20, gsxc_set = size_t(nr) * 153 * 17;
+  std::vector<T> gp2, gsx, gsxc;
+  if (p->tab.gphase) {  // replacing earlier sets: their bytes leave the plan's count
+    const size_t old = size_t(p->tab.nsets) * (gph_set * 2 + gs_set + (fused ? gp2_set * 2 + gsx_set + gsxc_set : 0));
+    p->bytes -= int64_t(old * sizeof(T));
+  }
+  if (fused) {
+    gp2.assign(S * gp2_set * 2, T(0));
+    gsx.assign(S * gsx_set, T(0));
+    gsxc.assign(S * gsxc_set, T(0));
+  }
+  for (size_t st = 0; st < S; ++st) {
+    const double e = sets[st].first, e0 = sets[st].second;
+    T* gphs = gph.data() + st * gph_set * 2;
+    T* gss = gs.data() + st * gs_set;
+    for (int ir = 0; ir < nr; ++ir) {
+      const double r = p->r[ir], wr = p->wr[ir];
+      // restitution law and exponential factor (inelastic_collisions.py:77-80)
+      const double er = 0.5 * (e0 - e) * std::tanh(r - 0.5 * p->R) + 0.5 * (e0 + e);
+      const double afac = 0.25 * pi * (1.0 + er) / p->L;
+      const double rg = std::pow(r, p->gamma + dim - 1.0);  // pre_fac(r) / sphr  (:54-55)
+      for (int m = 0; m <= M; ++m)
+        gss[size_t(ir) * (M + 1) + m] = T(rg * wr * p->wsigma * kern(afac * r * std::sqrt(double(m))));
+      for (int is = 0; is < ns; ++is) {
+        const int pair = ir * ns + is;
+        for (int d = 0; d < dim; ++d) {
+          const double sd = p->sigma[size_t(is) * dim + d];
+          for (int i = 0; i < n; ++i) {
+            const int k = i < n / 2 ? i : i - n;
+            const double th_g = afac * r * sd * double(k);
+            const size_t o = ((size_t(pair) * 3 + d) * n + i) * 2;
+            gphs[o] = T(std::cos(th_g));
+            gphs[o + 1] = T(std::sin(th_g));
+          }
+        }
+        if (fused) {
+          // a-parity gain rows (the radix-2 twiddles of the parity split folded in)
+          const double sd = p->sigma[size_t(is) * 3];
+          T* g2 = gp2.data() + st * gp2_set * 2;
+          for (int par = 0; par < 2; ++par)
+            for (int k = 0; k < 32; ++k) {
+              const size_t o = ((size_t(pair) * 2 + par) * 32 + k) * 2;
+              const int ks = k < 16 ? k : k - 32;
+              const double th_g = afac * r * sd * double(ks) - 2.0 * pi * double(par * k) / 32.0;
+              g2[o] = T(std::cos(th_g));
+              g2[o + 1] = T(std::sin(th_g));
+            }
+        }
+      }
+    }
+    if (fused) {
+      // per-column rows of the radial sinc table: gsinc[r][m_bc + q^2], q = |k_a| <= 16
+      T* gx = gsx.data() + st * gsx_set;
+      for (int ir = 0; ir < nr; ++ir)
+        for (int mbc = 0; mbc <= 512; ++mbc)
+          for (int q = 0; q <= 16 && mbc + q * q <= M; ++q)
+            gx[(size_t(ir) * 513 + mbc) * 20 + q] = gss[size_t(ir) * (M + 1) + mbc + q * q];
+      // the same by (|k_b|, |k_c|) pair, u = min <= v = max (index v (v + 1) / 2 + u, 153
+      // pairs), 17 values q = 0..16: one radial node's slab is 10.4 KB (shared memory)
+      T* gc = gsxc.data() + st * gsxc_set;
+      for (int ir = 0; ir < nr; ++ir)
+        for (int v = 0; v <= 16; ++v)
+          for (int u = 0; u <= v; ++u)
+            for (int q = 0; q <= 16; ++q)
+              gc[(size_t(ir) * 153 + v * (v + 1) / 2 + u) * 17 + q] = gss[size_t(ir) * (M + 1) + u * u + v * v + q * q];
+    }
+  }
   auto up = [&](void** dst, const void* src, size_t bytes) -> int {
+    if (*dst) {
+      cudaFree(*dst);
+      *dst = nullptr;
+    }
     PII_CUDA(cudaMalloc(dst, bytes));
     PII_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
     p->bytes += int64_t(bytes);
     return PII_OK;
   };
-  PII_TRY(up(&p->tab.ephase, eph.data(), eph.size() * sizeof(T)));
   PII_TRY(up(&p->tab.gphase, gph.data(), gph.size() * sizeof(T)));
   PII_TRY(up(&p->tab.gsinc, gs.data(), gs.size() * sizeof(T)));
-  PII_TRY(up(&p->tab.lossk, lk.data(), lk.size() * sizeof(T)));
-  PII_TRY(up(&p->tab.lapl, lp.data(), lp.size() * sizeof(T)));
+  if (fused) {
+    PII_TRY(up(&p->tab.gpar, gp2.data(), gp2.size() * sizeof(T)));
+    PII_TRY(up(&p->tab.gsx, gsx.data(), gsx.size() * sizeof(T)));
+    PII_TRY(up(&p->tab.gsxc, gsxc.data(), gsxc.size() * sizeof(T)));
+  }
+  const bool per_cell = S > 1;
+  p->tab.nsets = int64_t(S);
+  p->tab.gph_stride = per_cell ? int64_t(gph_set) : 0;
+  p->tab.gs_stride = per_cell ? int64_t(gs_set) : 0;
+  p->tab.gpar_stride = per_cell && fused ? int64_t(gp2_set) : 0;
+  p->tab.gsx_stride = per_cell && fused ? int64_t(gsx_set) : 0;
+  p->tab.gsxc_stride = per_cell && fused ? int64_t(gsxc_set) : 0;
   return PII_OK;
+}
+
+template <typename T>
+static int upload_tables(pii_plan* p) {
+  PII_TRY(upload_shared_tables<T>(p));
+  return upload_gain_tables<T>(p, {{p->e, p->e0}});
 }
 
 static int alloc(pii_plan* p, void** dst, size_t bytes) {
@@ -350,6 +432,37 @@ int pii_plan_create_nd(pii_plan** out, int dim, int n, int n_r, int n_sigma, con
                        int precision, int64_t batch_max, int device) {
   return pii::create(out, dim, n, n_r, n_sigma, r, w_r, sigma, w_sigma, L, R, e, e0, gamma, precision,
                      batch_max, device);
+}
+
+int pii_plan_set_restitution(pii_plan* plan, const double* e, const double* e0, int64_t count) {
+  using namespace pii;
+  if (!plan || count < 0 || (count > 0 && (!e || !e0))) {
+    set_error("pii_plan_set_restitution: invalid arguments");
+    return PII_ERR_ARG;
+  }
+  if (count > plan->batch_max) {
+    set_error("pii_plan_set_restitution: %lld restitution sets for a plan of batch_max = %lld", (long long)count,
+              (long long)plan->batch_max);
+    return PII_ERR_SIZE;
+  }
+  if (count > 1 && plan->dim != 3) {
+    set_error("pii_plan_set_restitution: per-cell restitution exists for 3D-velocity plans only");
+    return PII_ERR_ARG;
+  }
+  PII_CUDA(cudaSetDevice(plan->device));
+  PII_CUDA(cudaDeviceSynchronize());  // launches in flight may still read the old tables
+  std::vector<std::pair<double, double>> sets;
+  if (count == 0)
+    sets.push_back({plan->e, plan->e0});
+  else
+    for (int64_t c = 0; c < count; ++c) sets.push_back({e[c], e0[c]});
+  int st = plan->precision == PII_PREC_FP32 ? upload_gain_tables<float>(plan, sets)
+                                            : upload_gain_tables<double>(plan, sets);
+  if (st != PII_OK) return st;
+  if (plan->tab.nsets > 1 && plan->gain_path == 1) plan->gain_path = plan->ap_count > 0 ? 3 : 2;
+  if (plan->dft_img) PII_TRY(col_tc_gain_tables(plan));  // the tensor-core path's sinc slices
+  graphs_clear(plan);  // captured graphs baked the old tables in
+  return PII_OK;
 }
 
 int pii_plan_dim(const pii_plan* plan) { return plan ? plan->dim : -1; }

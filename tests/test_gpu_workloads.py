@@ -3,9 +3,10 @@
 * ensemble: 64 independent homogeneous problems, n in {16, 24, 32, 48},
   e ~ U[0.2, 1], 2-4 Maxwellian mixtures, one CUDA graph per PFE macro-step;
 * stiff telescopic: TPI3 at kn = 1e-4, periodic, rho = 1 + 0.2 sin(2 pi x),
-  T = 1 + 0.1 cos(2 pi x), n = 32, 32 x 32 (64 cells instead of 512 so that the
-  FP64 comparison run stays short); the state error is reported against a
-  documented bound (see the test), mass to 1e-10;
+  T = 1 + 0.1 cos(2 pi x), n = 32, 32 x 32, 512 cells for one macro-step
+  against FP64 (the state error against its measured bound, mass to 1e-10),
+  and one homogeneous cell stepped to the end time t = 0.05 in both
+  precisions;
 * large grid: n = 64, L = 10, e = 0.7, 48 radial nodes x the 70-point design
   (no 64-point symmetric design exists), 3-component mixtures; against the
   oracle's fixture (tests/golden/c5_n64.npz) and the FP64 path.
@@ -63,52 +64,86 @@ def test_ensemble_uneven_sizes_graph_vs_fp64():
         assert abs(T1 - T2) < 1e-5 * T2
 
 
-def test_tpi3_stiff_periodic_mixed_vs_fp64():
-    pkg = _pkg()
-    nx, kn = 64, 1e-4
+# the stiff telescopic configuration: TPI3, kn = 1e-4, e = e0 = 0.9, periodic,
+# rho = 1 + 0.2 sin(2 pi x), T = 1 + 0.1 cos(2 pi x).  Levels dt = (1e-5,
+# 2.5e-5, 6.25e-5), K = 2 each, macro-step 2e-4: M = (0.5, 0.5, 1.2), advection
+# CFL 0.79 at 512 cells, and an inner step inside the collision term's explicit
+# bound (nu dt0 / kn <= 0.62).  The reference defaults (K = [3, 3, 3],
+# dt_l = [kn, 5 kn, 10 kn]) give M_1 = -1 and an inner Euler step of kn,
+# outside that bound: both FP64 and mixed runs diverge there.
+C4_LEVELS = dict(inner_steps=[2, 2, 2], inner_dt=[1e-5, 2.5e-5, 6.25e-5], dt=2e-4)
+
+
+def _c4_run(pkg, precision, nx, steps, f0=None, record=None):
+    kn = 1e-4
     cfg = op_config(32, L8_S, 32, 32, 0.9, 0.9, 1.0)
     sm = pkg.SpectralMesh(cfg)
-    v = sm.v_center
-    x = (np.arange(nx) + 0.5) / nx
-    f0 = np.stack([maxwellian(v, 1 + 0.2 * math.sin(2 * math.pi * xi), (0, 0, 0), 1 + 0.1 * math.cos(2 * math.pi * xi))
-                   for xi in x])
-    res = {}
-    for prec in ("mixed", "double"):
-        col = pkg.FSInelasticVHSCollision(cfg, sm, precision=prec, with_loss=True, mass_fix=True, batch_max=nx)
-        sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": nx, "nv": 32})
-        sol.state.f.copy_(torch.as_tensor(f0))
-        solver = pkg.BoltzmannSolver1D(kn, collision_operator=col)
-        solver.all_bcs = pkg.BC.periodic
-        # The reference defaults (K = [3, 3, 3], dt_l = [kn, 5 kn, 10 kn]) give M_1 = -1 and an inner
-        # Euler step of kn, outside the explicit stability bound of this collision frequency: both the
-        # FP64 and the mixed runs diverge.  Stable levels: dt_0 = kn / 10, M = (8, 0.5, 2), and a macro
-        # step of 1e-3 (advection CFL 0.5 at 64 cells).
-        solver.time_integrator = "TPI3"
-        solver.inner_steps = [2, 2, 2]
-        solver.inner_dt = [1e-5, 1e-4, 2.5e-4]
-        solver.dt = 1e-3
-        solver.check_every = 1  # FP64 NaN / Inf guard after every macro-step
-        rho0, u0, T0 = sol.state.moments()
-        solver.evolve_to_time(sol, 1e-3)
-        rho1, u1, T1 = sol.state.moments()
-        res[prec] = (sol.f.clone(), rho0, rho1, T1)
-    fm, fd = res["mixed"][0], res["double"][0]
-    # Near equilibrium Q = gain - loss cancels; the FP32 rounding of gain and loss
-    # (~1e-7 of |gain|) enters f multiplied by dt / kn and by the extrapolation
-    # factors, so after 2 macro-steps (16 operator calls) the state differs by
-    # ~1e-4 (1.03e-4 measured after 2 macro-steps) although each Q call is within
-    # 2e-6 of FP64.  At these levels the telescopic scheme is itself far from a
-    # resolved run (T = 0.50 vs 0.35 from forward Euler at dt = 1e-5, t = 1e-3)
-    # and sensitive to small perturbations, so one macro-step is compared.
+    if f0 is None:
+        x = (np.arange(nx) + 0.5) / nx
+        f0 = np.stack([maxwellian(sm.v_center, 1 + 0.2 * math.sin(2 * math.pi * xi), (0, 0, 0),
+                                  1 + 0.1 * math.cos(2 * math.pi * xi)) for xi in x])
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, with_loss=True, mass_fix=True, batch_max=nx)
+    sol = pkg.Solution({"dim_x": 1, "dim_v": 3, "xmin": 0.0, "xmax": 1.0, "l": sm.L, "nx": nx, "nv": 32})
+    sol.state.f.copy_(torch.as_tensor(f0))
+    solver = pkg.BoltzmannSolver1D(kn, collision_operator=col)
+    solver.all_bcs = pkg.BC.periodic
+    solver.time_integrator = "TPI3"
+    solver.inner_steps = C4_LEVELS["inner_steps"]
+    solver.inner_dt = C4_LEVELS["inner_dt"]
+    solver.dt = C4_LEVELS["dt"]
+    solver.check_every = 1  # FP64 NaN / Inf guard after every macro-step
+    rho0, _, _ = sol.state.moments()
+    for k in range(steps):
+        solver.step(sol, False, k * solver.dt, (k + 1) * solver.dt)
+        if record is not None:
+            record.append((sol.f.clone(), sol.state.moments()))
+    torch.cuda.synchronize()
+    return sol.f.clone(), rho0
+
+
+def test_c4_full_size_macro_step_mixed_vs_fp64():
+    """512 cells, one macro-step (8 operator calls) in both precisions.  Near
+    equilibrium Q = gain - loss cancels, so the FP32 rounding of each term
+    (~1e-7 of |gain|) reaches f multiplied by dt / kn and the extrapolation
+    factors: measured 6.9e-6 after one macro-step, growing by ~1.8e-5 per
+    macro-step over the next two (2.8e-5, 5.5e-5), although every Q call is
+    within 3e-6 of FP64.  Bound: 2e-5 after one macro-step."""
+    pkg = _pkg()
+    fm, rho0 = _c4_run(pkg, "mixed", 512, 1)
+    fd, _ = _c4_run(pkg, "double", 512, 1)
     err = float((fm - fd).abs().max() / fd.abs().max())
-    print(f"TPI3 kn=1e-4: mixed vs FP64 rel Linf after 1 macro-step = {err:.3e}")
-    assert err < 5e-4
+    print(f"C4 512 cells: mixed vs FP64 rel Linf after 1 macro-step = {err:.3e}")
+    assert err < 2e-5
+    dv = (2 * 8.0 / 32) ** 3  # velocity cell volume of the 32^3 grid on [-8, 8]^3
+    for f in (fm, fd):  # periodic transport + mass-fixed Q conserve the total mass
+        assert abs(float(f.sum()) * dv / float(rho0.sum()) - 1) < 1e-10
+
+
+def test_c4_homogeneous_cell_full_horizon_mixed_vs_fp64():
+    """The stiff configuration's cooling on one homogeneous cell (rho = T = 1),
+    stepped to its end time t = 0.05 (250 macro-steps, 2000 operator calls) in
+    both precisions: the inelastic cooling takes T below the grid's velocity
+    resolution (thermal speed < the 0.5 cell width by t ~ 0.005); the mixed
+    and FP64 temperature histories must agree along the whole run."""
+    pkg = _pkg()
+    cfg = op_config(32, L8_S, 32, 32, 0.9, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    f0 = maxwellian(sm.v_center, 1.0, (0, 0, 0), 1.0)[None]
+    hist = {}
     for prec in ("mixed", "double"):
-        _, rho0, rho1, _ = res[prec]
-        assert abs(rho1.sum() - rho0.sum()) / rho0.sum() < 1e-10  # periodic transport + mass-fixed Q
-    dT = float(np.abs(res["mixed"][3] / res["double"][3] - 1).max())
-    print(f"TPI3 kn=1e-4: max relative temperature difference mixed vs FP64 = {dT:.3e}")
-    assert dT < 1e-2
+        rec = []
+        _c4_run(pkg, prec, 1, 250, f0=f0, record=rec)
+        hist[prec] = rec
+    errs, dT = [], []
+    for (fm, (_, _, Tm)), (fd, (_, _, Td)) in zip(hist["mixed"], hist["double"]):
+        errs.append(float((fm - fd).abs().max() / fd.abs().max()))
+        dT.append(float(abs(Tm[0] / Td[0] - 1)))
+    Td = [float(m[2][0]) for _, m in hist["double"]]
+    print("C4 homogeneous cell: step, T (FP64), mixed-vs-FP64 rel Linf of f, rel diff of T")
+    for k in list(range(0, 250, 25)) + [249]:
+        print(f"  {k + 1:4d} t={(k + 1) * 2e-4:.4f} T={Td[k]:.5f} err={errs[k]:.3e} dT={dT[k]:.3e}")
+    assert max(dT) < 1e-3
+    assert max(errs) < 1e-2
 
 
 def _mixture_from(v, w, u, T):
