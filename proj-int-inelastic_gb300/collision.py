@@ -349,12 +349,14 @@ class FSInelasticVHSCollision:
     * ``mass_fix``   -- subtract the per-cell mean of Q in FP64 (k = 0 mode);
     * ``batch_max``  -- initial cell capacity of the plan (grown on demand);
     * ``device``     -- CUDA device index;
-    * ``gain_path``  -- for n = 32 in mixed precision: "packed" (the fused
-      a-parity kernel on antipodal direction pairs plus the Nyquist-plane
-      correction, the default where the design is antipodally symmetric),
-      "parity" (fused a-parity kernel with a tensor-memory accumulator, the
-      default otherwise) or "cluster" (fused 2-CTA-cluster kernel); "pipeline"
-      (column / plane passes) in every case.  All evaluate the same operator.
+    * ``gain_path``  -- in mixed precision: "packed" (each antipodal direction
+      pair (sigma, -sigma) in one real-phase pass, plus the Nyquist-plane
+      correction; the default where the design is antipodally symmetric: the
+      fused a-parity kernel for n = 32, the column / plane pipeline otherwise),
+      for n = 32 also "parity" (fused a-parity kernel with a tensor-memory
+      accumulator, the default otherwise) or "cluster" (fused 2-CTA-cluster
+      kernel); "pipeline" (column / plane passes on every pair) in every case.
+      All evaluate the same operator.
     """
 
     collision_model = "vhs"

@@ -65,6 +65,7 @@
 #include <vector>
 
 #include "fft_reg.cuh"
+#include "pack.cuh"
 #include "pii_internal.cuh"
 #include "tmem.cuh"
 #include "umma.cuh"
@@ -118,6 +119,7 @@ struct ColTcArgs {
   const float* colb;     // PSTART: [cells][N2] max over a of |f^(a, j)|_1 (k_col_bound)
   int ns;
   int64_t items, c0, p0, np;
+  const int* reps;      // _PK modes: representative pair of each antipodal pass
   int* err;             // host-mapped word: 1 if a role gave up waiting, 2 if the drain also timed out
   uint32_t wait_limit;  // mbarrier polls before a role gives up
   int withhold;         // test hook: the TMA thread issues no copies, so the other roles' waits run out
@@ -162,6 +164,11 @@ __device__ __forceinline__ bool bar_any(bool pred) {
 template <int MODE>
 __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constant__ CUtensorMap tmap, ColTcArgs a) {
   using namespace ctc;
+  // START: the inverse transform of the first stage (PSTART, or PSTART_PK on an
+  // antipodal pass with the real phase t); !START: the forward transform of the
+  // last stage with the complex gain (PEND) or the real coefficient 2 s (PEND_PK)
+  constexpr bool START = MODE == COL_PSTART || MODE == COL_PSTART_PK;
+  constexpr bool PACK = MODE == COL_PSTART_PK || MODE == COL_PEND_PK;
   extern __shared__ __align__(1024) unsigned char sm[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + OFF_BAR);
   uint64_t* rfull = bars;
@@ -219,19 +226,29 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       const uint32_t u = uint32_t(i >> 1) & 1u;
       // PSTART: the cell's column bound, in flight during the waits below
       float cb = 0.f;
-      if constexpr (MODE == COL_PSTART)
+      if constexpr (START)
         cb = a.colb[(a.c0 + (tile / TILES_PER_ITEM) / a.np) * N2 + int(tile % TILES_PER_ITEM) * TN + n];
       // the raw tile is in and operand buffer b is free (MMAs of tile i - 2 done)
       const bool ok = mbar_wait_role(rfull + b, u, abort, lim) && mbar_wait_role(xempty + b, u ^ 1u, abort, lim);
       const float2* raw = reinterpret_cast<const float2*>(sm + OFF_R + b * RAW);
       const float2* ep = reinterpret_cast<const float2*>(sm + OFF_P + b * PROW);
       float2 ebc = make_float2(1.f, 0.f);
+      float tcp = 0.f, tcm = 0.f, tth = 0.f;  // PSTART_PK: the real phase's column constants
       if constexpr (MODE == COL_PSTART) {
         const int j = int(tile % TILES_PER_ITEM) * TN + n;
         if (ok) ebc = cmul(ep[NV + (j >> 6)], ep[2 * NV + (j & 63)]);
       }
+      if constexpr (MODE == COL_PSTART_PK) {
+        const int j = int(tile % TILES_PER_ITEM) * TN + n;
+        if (ok) pack_t_consts<float, float2, NV>(ep, j >> 6, j & 63, tcp, tcm, tth);
+      }
       float mx = 0.f;
-      if constexpr (MODE == COL_PSTART) {
+      if constexpr (MODE == COL_PSTART_PK) {
+        // |x0 t0 +- x1 t1| <= 2 max_a |f^(a, j)|_1 max_a |t|, |t| <= sqrt 2 |e_0| (|c| <= 1, and
+        // the a-row phases share the modulus |e_0|)
+        if (!ok) break;  // no barrier in this mode: threads may leave one by one
+        mx = 2.f * cb * (1.001f * 1.41422f * sqrtf(ep[0].x * ep[0].x + ep[0].y * ep[0].y));
+      } else if constexpr (MODE == COL_PSTART) {
         // the cell's column bound (k_col_bound): |x0 e0 +- x1 e1| <= 2 max_a |f^(a, j)|_1 |e_a| |e_bc|_1;
         // the a-row phases exp(i phi) / n^3 share one modulus, |e_0| (FP32 rounding of the table
         // can leave a bound a few ulp low: the scaled values then exceed 1 by as much, well
@@ -275,6 +292,12 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
             x1 = cmul(x1, cmul(ep[a0 + 1], ebc));
             y0 = cmul(y0, cmul(ep[a0 + 32], ebc));
             y1 = cmul(y1, cmul(ep[a0 + 33], ebc));
+          } else if constexpr (MODE == COL_PSTART_PK) {
+            auto tt = [&](int aa) { return aa == NV / 2 ? tth : fmaf(ep[aa].y, tcm, ep[aa].x * tcp); };
+            x0 = cscale(x0, tt(a0));
+            x1 = cscale(x1, tt(a0 + 1));
+            y0 = cscale(y0, tt(a0 + 32));
+            y1 = cscale(y1, tt(a0 + 33));
           }
           const float2 v[2][2] = {{cadd(x0, y0), cadd(x1, y1)}, {csub(x0, y0), csub(x1, y1)}};
 #pragma unroll
@@ -319,15 +342,19 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       const uint32_t u = uint32_t(i >> 1) & 1u;
       if (!mbar_wait_role(tfull + d, u, abort, lim)) break;
       if (!mbar_wait_role(sready + d, u, abort, lim)) break;
-      if (MODE == COL_PEND && !mbar_wait_role(gfull + d, u, abort, lim)) break;
+      if (!START && !mbar_wait_role(gfull + d, u, abort, lim)) break;
       tm_fence_after();
       const float up = scl[(i & 3) * TN + n];  // the column's scale (S and D alike)
       const uint32_t ta = tmem + (uint32_t(32 * qd) << 16) + uint32_t(256 + 128 * d + 64 * hh);
       float2 gbc = make_float2(1.f, 0.f);
+      float sdp = 0.f, sdm = 0.f, ssh = 0.f;  // PEND_PK: the real coefficient's column constants
       const float* grow = gsl;
-      if constexpr (MODE == COL_PEND) {
+      if constexpr (!START) {
         const int jb = j >> 6, jc = j & 63;
-        gbc = cmul(gpS[NV + jb], gpS[2 * NV + jc]);
+        if constexpr (PACK)
+          pack_s_consts<float, float2, NV>(gpS, jb, jc, sdp, sdm, ssh);
+        else
+          gbc = cmul(gpS[NV + jb], gpS[2 * NV + jc]);
         const int kc = kval(jc, NV);
         grow = gsl + (n >> 6) * SLICE + (kc < 0 ? -kc : kc) * KA_PITCH;  // slice of this column's k_b, row |k_c|
       }
@@ -343,6 +370,11 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
           if constexpr (MODE == COL_PEND) {
             const int ka = kval(k, NV);
             y = cmul(y, cscale(cmul(gpS[k], gbc), grow[ka < 0 ? -ka : ka]));
+          } else if constexpr (MODE == COL_PEND_PK) {
+            const int ka = kval(k, NV);
+            const float2 g = gpS[k];
+            const float sv = k == NV / 2 ? ssh : fmaf(-g.y, sdm, g.x * sdp);
+            y = cscale(y, 2.f * sv * grow[ka < 0 ? -ka : ka]);
           }
           out[int64_t(k) * N2] = y;
         }
@@ -350,7 +382,7 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
       // the accumulator has been read: the issuer may overwrite it
       tm_fence_before();
       mbar_arrive(tempty + d);
-      if constexpr (MODE == COL_PEND) mbar_arrive(gempty + d);  // and the gain rows
+      if constexpr (!START) mbar_arrive(gempty + d);  // and the gain rows
     }
   } else if (warp == ISSUER_WARP) {
     if (lane == 0) {
@@ -412,14 +444,14 @@ __global__ void __launch_bounds__(ctc::THREADS, 1) k_col_tc(const __grid_constan
         const int64_t item = tile / TILES_PER_ITEM;
         const int j0 = int(tile - item * TILES_PER_ITEM) * TN;
         const int64_t ci = item / a.np;
-        const int64_t pair = a.p0 + (item - ci * a.np);
+        const int64_t pair = PACK ? int64_t(a.reps[a.p0 + (item - ci * a.np)]) : a.p0 + (item - ci * a.np);
         // rows of 64 per grid: f^ of cell c0 + ci, or item `item` of the chunk buffer
-        const int y = int(MODE == COL_PSTART ? (a.c0 + ci) * NV : item * NV);
-        mbar_arrive_tx(rfull + b, RAW + (MODE == COL_PSTART ? PROW : 0));
+        const int y = int(START ? (a.c0 + ci) * NV : item * NV);
+        mbar_arrive_tx(rfull + b, RAW + (START ? PROW : 0));
         ++rphases[b];
         tma_load_2d(sm + OFF_R + b * RAW, &tmap, 2 * j0, y, rfull + b);
-        if constexpr (MODE == COL_PSTART) bulk_g2s(sm + OFF_P + b * PROW, a.ephase + pair * 3 * NV, PROW, rfull + b);
-        if constexpr (MODE == COL_PEND) {
+        if constexpr (START) bulk_g2s(sm + OFF_P + b * PROW, a.ephase + pair * 3 * NV, PROW, rfull + b);
+        if constexpr (!START) {
           // the pair's gain rows into gain buffer b once the epilogue of tile i - 2 is done with it
           if (!mbar_wait_role(gempty + b, (uint32_t(i >> 1) & 1u) ^ 1u, abort, lim)) break;
           unsigned char* g = sm + OFF_G + b * GROW * 4;
@@ -574,6 +606,8 @@ int col_tc_prepare(pii_plan* p) {
   PII_TRY(make_tmap(p->dft_tmap[1], p->buf, p->chunk_items));
   PII_CUDA(cudaFuncSetAttribute(k_col_tc<COL_PSTART>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
   PII_CUDA(cudaFuncSetAttribute(k_col_tc<COL_PEND>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+  PII_CUDA(cudaFuncSetAttribute(k_col_tc<COL_PSTART_PK>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+  PII_CUDA(cudaFuncSetAttribute(k_col_tc<COL_PEND_PK>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
   if (!p->dft_img) {
     std::vector<uint16_t> img;
     build_dft_images(img);
@@ -654,10 +688,21 @@ int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int
     set_error("col_tc_run: plan is not an n = 64 3D plan");
     return PII_ERR_ARG;
   }
+  const bool start = mode == COL_PSTART || mode == COL_PSTART_PK;
+  const bool pack = mode == COL_PSTART_PK || mode == COL_PEND_PK;
+  if (mode != COL_PSTART && mode != COL_PEND && !pack) {
+    set_error("col_tc_run: unknown column mode %d", mode);
+    return PII_ERR_ARG;
+  }
+  if (pack && !p->ap_reps) {
+    set_error("col_tc_run: antipodal passes need an antipodally symmetric design");
+    return PII_ERR_ARG;
+  }
   ColTcArgs a{};
-  a.src = static_cast<const float2*>(mode == COL_PSTART ? p->fhat : p->buf);
+  a.src = static_cast<const float2*>(start ? p->fhat : p->buf);
+  a.reps = p->ap_reps;
   a.dst = static_cast<float2*>(p->buf);
-  a.fimg = reinterpret_cast<const uint4*>(static_cast<const char*>(p->dft_img) + (mode == COL_PSTART ? 0 : FIMG));
+  a.fimg = reinterpret_cast<const uint4*>(static_cast<const char*>(p->dft_img) + (start ? 0 : FIMG));
   a.ephase = static_cast<const float2*>(p->tab.ephase);
   a.gphase = static_cast<const float2*>(p->tab.gphase);
   a.gsk = static_cast<const float*>(p->dft_gs);
@@ -675,13 +720,17 @@ int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int
   const int64_t tiles = items * TILES_PER_ITEM;
   const unsigned grid = unsigned(std::min<int64_t>(p->dft_ctas, tiles));
   CUtensorMap tm;
-  memcpy(&tm, p->dft_tmap[mode == COL_PSTART ? 0 : 1], sizeof(tm));
-  if (mode == COL_PSTART) {
-    StageTimer st(p, ST_COL_PSTART, s);
-    k_col_tc<COL_PSTART><<<grid, THREADS, SMEM, s>>>(tm, a);
-  } else {
-    StageTimer st(p, ST_COL_PEND, s);
-    k_col_tc<COL_PEND><<<grid, THREADS, SMEM, s>>>(tm, a);
+  memcpy(&tm, p->dft_tmap[start ? 0 : 1], sizeof(tm));
+  {
+    StageTimer st(p, start ? ST_COL_PSTART : ST_COL_PEND, s);
+    if (mode == COL_PSTART)
+      k_col_tc<COL_PSTART><<<grid, THREADS, SMEM, s>>>(tm, a);
+    else if (mode == COL_PEND)
+      k_col_tc<COL_PEND><<<grid, THREADS, SMEM, s>>>(tm, a);
+    else if (mode == COL_PSTART_PK)
+      k_col_tc<COL_PSTART_PK><<<grid, THREADS, SMEM, s>>>(tm, a);
+    else
+      k_col_tc<COL_PEND_PK><<<grid, THREADS, SMEM, s>>>(tm, a);
   }
   PII_CHECK_LAUNCH();
   return PII_OK;

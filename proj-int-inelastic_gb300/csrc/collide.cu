@@ -38,17 +38,22 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
   }
-  // items = (cell, pair); a chunk holds Cc cells x Pc pairs in the L2-resident buffer
+  // items = (cell, pair), or (cell, antipodal pass) on the packed pipeline; a
+  // chunk holds Cc cells x Pc of them in the L2-resident buffer
+  bool packed = false;
+  if constexpr (std::is_same<T, float>::value && NV != 32) packed = p->gain_path == 3 && p->ap_count > 0;
+  const int64_t QQ = packed ? p->ap_count : p->Q;
   int64_t Cc = std::max<int64_t>(1, (p->chunk_points + N - 1) / N);
   Cc = std::min<int64_t>(Cc, std::min<int64_t>(cells, p->chunk_items));
-  const int64_t Pc = std::max<int64_t>(1, std::min<int64_t>(p->Q, p->chunk_items / Cc));
+  const int64_t Pc = std::max<int64_t>(1, std::min<int64_t>(QQ, p->chunk_items / Cc));
   for (int64_t c0 = 0; c0 < cells; c0 += Cc) {
     const int64_t cc = std::min(Cc, cells - c0);
-    for (int64_t p0 = 0; p0 < p->Q; p0 += Pc) {
-      const int64_t np = std::min(Pc, p->Q - p0);
-      PII_TRY(K::pairs(p, c0, cc, p0, np, p0 == 0, s));
+    for (int64_t p0 = 0; p0 < QQ; p0 += Pc) {
+      const int64_t np = std::min(Pc, QQ - p0);
+      PII_TRY(K::pairs(p, c0, cc, p0, np, p0 == 0, s, packed));
     }
   }
+  if (packed) PII_TRY(nyq_gen_run(p, cells, s));  // what the packed passes leave out, on the Nyquist planes
   return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
 }
 
@@ -178,9 +183,14 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
     cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points, 0});  // even split: no item knob
     if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points, 0});
   }
-  for (int dft = 0; dft <= (plan->dft_img ? 1 : 0); ++dft)
-    for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
-      cands.push_back({0, plan->gc_items_per_cluster, pts, dft});
+  // the pipeline on (cell, pair) items, and on antipodal passes where it is packed (n != 32)
+  const bool pack_pipe = plan->n != 32 && plan->ap_count > 0 && plan->nq_part;
+  for (int path : {0, 3}) {
+    if (path == 3 && !pack_pipe) continue;
+    for (int dft = 0; dft <= (plan->dft_img ? 1 : 0); ++dft)
+      for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
+        cands.push_back({path, plan->gc_items_per_cluster, pts, dft});
+  }
   const int saved_path = plan->gain_path;
   const int saved_items = plan->gc_items_per_cluster;
   const int64_t saved_points = plan->chunk_points;
@@ -254,11 +264,11 @@ extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
     pii::set_error("pii_plan_set_gain_path: path must be 0 (pipeline), 1 (cluster), 2 (a-parity) or 3 (packed)");
     return PII_ERR_ARG;
   }
-  if (path == 3 && plan->ap_count == 0) {
-    pii::set_error("pii_plan_set_gain_path: the packed kernel needs an antipodally symmetric design");
+  if (path == 3 && (plan->ap_count == 0 || !plan->nq_part)) {
+    pii::set_error("pii_plan_set_gain_path: the packed path needs an FP32 3D plan on an antipodally symmetric design");
     return PII_ERR_ARG;
   }
-  if (path != 0 && (plan->gc_clusters <= 0 || plan->gp_ctas <= 0)) {
+  if ((path == 1 || path == 2) && (plan->gc_clusters <= 0 || plan->gp_ctas <= 0)) {
     pii::set_error("pii_plan_set_gain_path: the fused kernels exist for n = 32, FP32 plans only");
     return PII_ERR_ARG;
   }

@@ -23,6 +23,7 @@
 #pragma once
 #include <type_traits>
 #include "fft_reg.cuh"
+#include "pack.cuh"
 #include "pii_internal.cuh"
 
 namespace pii {
@@ -46,8 +47,11 @@ struct ColArgs {
   int64_t np;          // pairs per cell in the chunk
   int ns;              // n_sigma
   double hb;           // heat bath coefficient (IPREP)
+  const int* reps;     // _PK modes: representative pair of each antipodal pass
   Tables tab;
 };
+
+
 
 // ---------------------------------------------------------------------------
 // column pass along a
@@ -107,6 +111,49 @@ __global__ void __launch_bounds__(128) k_col(ColArgs args) {
       constexpr int ka = kval(a, NV);
       const V g = cscale(cmul(gp[a], gbc), gs[mbc + ka * ka]);
       io[a * N2] = cmul(x[pos(NV, a)], g);
+    });
+  } else if constexpr (MODE == COL_PSTART_PK) {
+    // the antipodal pass's input f^ t (real phase t), transformed along a
+    const int64_t ci = item / args.np;
+    const int pair = args.reps[args.p0 + (item - ci * args.np)];
+    const V* fh = reinterpret_cast<const V*>(args.src) + (args.c0 + ci) * N3 + j;
+    const V* ep = reinterpret_cast<const V*>(args.tab.ephase) + int64_t(pair) * 3 * NV;
+    T cp, cm, th;
+    pack_t_consts<T, V, NV>(ep, jb, jc, cp, cm, th);
+#pragma unroll
+    for (int a = 0; a < NV; ++a) {
+      const V e = ep[a];
+      const T t = a == NV / 2 ? th : e.x * cp + e.y * cm;
+      x[a] = cscale(fh[a * N2], t);
+    }
+    fft_line<NV, +1>(x);
+    V* out = reinterpret_cast<V*>(args.dst) + item * N3 + j;
+    static_for<0, NV>([&](auto ai) {
+      constexpr int a = decltype(ai)::value;
+      out[a * N2] = x[pos(NV, a)];
+    });
+  } else if constexpr (MODE == COL_PEND_PK) {
+    // forward transform along a, then the REAL coefficient 2 s(k) times the radial sinc
+    const int64_t ci = item / args.np;
+    const int pair = args.reps[args.p0 + (item - ci * args.np)];
+    const int ir = pair / args.ns;
+    V* io = reinterpret_cast<V*>(args.dst) + item * N3 + j;
+#pragma unroll
+    for (int a = 0; a < NV; ++a) x[a] = io[a * N2];
+    fft_line<NV, -1>(x);
+    const int64_t cell = args.c0 + ci;  // its restitution set, when the plan has one per cell
+    const V* gp = reinterpret_cast<const V*>(args.tab.gphase) + cell * args.tab.gph_stride + int64_t(pair) * 3 * NV;
+    const T* gs =
+        reinterpret_cast<const T*>(args.tab.gsinc) + cell * args.tab.gs_stride + int64_t(ir) * (args.tab.M + 1);
+    T dp, dm, sh;
+    pack_s_consts<T, V, NV>(gp, jb, jc, dp, dm, sh);
+    const int mbc = kb * kb + kc * kc;
+    static_for<0, NV>([&](auto ai) {
+      constexpr int a = decltype(ai)::value;
+      constexpr int ka = kval(a, NV);
+      const V g = gp[a];
+      const T sv = a == NV / 2 ? sh : g.x * dp - g.y * dm;
+      io[a * N2] = cscale(x[pos(NV, a)], T(2) * sv * gs[mbc + ka * ka]);
     });
   } else {  // COL_IPREP: item = cell in chunk; outputs Y1 -> dst[2 item], Y2 -> dst[2 item + 1]
     const int64_t cell = args.c0 + item;
@@ -405,7 +452,7 @@ int CollideKernels<T, NV>::fwd(pii_plan* p, const double* f, int64_t c0, int64_t
 
 template <typename T, int NV>
 int CollideKernels<T, NV>::pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t p0, int64_t np, bool first,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, bool packed) {
   using V = c2<T>;
   constexpr int N3 = Geo<NV>::N3, PPB = Geo<NV>::PPB, N2 = Geo<NV>::N2;
   const int smem = PPB * NV * Geo<NV>::LD * int(sizeof(V));
@@ -417,14 +464,18 @@ int CollideKernels<T, NV>::pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t
   a.c0 = c0;
   a.p0 = p0;
   a.np = np;
+  a.reps = p->ap_reps;
   const unsigned colblocks = unsigned((items * N2 + 127) / 128);
   bool tc = false;
   if constexpr (std::is_same<T, float>::value && NV == 64) tc = p->dft_path == 1;
   if (tc) {
-    PII_TRY(col_tc_run(p, COL_PSTART, items, c0, p0, np, s));
+    PII_TRY(col_tc_run(p, packed ? COL_PSTART_PK : COL_PSTART, items, c0, p0, np, s));
   } else {
     StageTimer st(p, ST_COL_PSTART, s);
-    k_col<T, NV, COL_PSTART><<<colblocks, 128, 0, s>>>(a);
+    if (packed)
+      k_col<T, NV, COL_PSTART_PK><<<colblocks, 128, 0, s>>>(a);
+    else
+      k_col<T, NV, COL_PSTART><<<colblocks, 128, 0, s>>>(a);
     PII_CHECK_LAUNCH();
   }
   const int64_t nplanes = items * NV;
@@ -435,10 +486,13 @@ int CollideKernels<T, NV>::pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t
   }
   PII_CHECK_LAUNCH();
   if (tc) {
-    PII_TRY(col_tc_run(p, COL_PEND, items, c0, p0, np, s));
+    PII_TRY(col_tc_run(p, packed ? COL_PEND_PK : COL_PEND, items, c0, p0, np, s));
   } else {
     StageTimer st(p, ST_COL_PEND, s);
-    k_col<T, NV, COL_PEND><<<colblocks, 128, 0, s>>>(a);
+    if (packed)
+      k_col<T, NV, COL_PEND_PK><<<colblocks, 128, 0, s>>>(a);
+    else
+      k_col<T, NV, COL_PEND><<<colblocks, 128, 0, s>>>(a);
     PII_CHECK_LAUNCH();
   }
   {

@@ -633,38 +633,14 @@ int gain_parity_prepare(pii_plan* p) {
   PII_CUDA(cudaMalloc(&p->gp_hpart, bytes));
   p->bytes += int64_t(bytes);
   p->gp_max_items = max_items;
-  // antipodal pairs of the design (the symmetric designs list every point and
-  // its negative): one representative per pair and radial node
-  const int ns = p->ns;
-  std::vector<int> mate(ns, -1);
-  bool sym = ns % 2 == 0;
-  for (int i = 0; i < ns && sym; ++i) {
-    for (int j = 0; j < ns; ++j) {
-      double d = 0;
-      for (int k = 0; k < 3; ++k) d = std::max(d, std::fabs(p->sigma[3 * i + k] + p->sigma[3 * j + k]));
-      if (d < 1e-12) {
-        mate[i] = j;
-        break;
-      }
-    }
-    sym = mate[i] >= 0 && mate[i] != i;
-  }
-  if (sym) {
-    std::vector<int> reps;
-    for (int ir = 0; ir < p->nr; ++ir)
-      for (int i = 0; i < ns; ++i)
-        if (i < mate[i]) reps.push_back(ir * ns + i);
-    if (int(reps.size()) * 2 == p->Q) {
-      PII_CUDA(cudaMalloc(&p->ap_reps, reps.size() * sizeof(int)));
-      PII_CUDA(cudaMemcpy(p->ap_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
-      p->bytes += int64_t(reps.size() * sizeof(int));
-      p->ap_count = int(reps.size());
-      // Nyquist-correction accumulators: cells x ceil(16 SMs / cells) <= 16 SMs + cells CTAs
-      const size_t nq = (size_t(16 * sms) + size_t(p->batch_max)) * 3 * N2 * sizeof(float2);
-      PII_CUDA(cudaMalloc(&p->nq_part, nq));
-      p->bytes += int64_t(nq);
-      PII_TRY(nyq_corr_prepare(p));
-    }
+  // the antipodal passes (representative pair of each (sigma, -sigma) per radial
+  // node) are set up with the plan; the packed kernel adds the Nyquist correction
+  if (p->ap_count > 0) {
+    // Nyquist-correction accumulators: cells x ceil(16 SMs / cells) <= 16 SMs + cells CTAs
+    const size_t nq = (size_t(16 * sms) + size_t(p->batch_max)) * 3 * N2 * sizeof(float2);
+    PII_CUDA(cudaMalloc(&p->nq_part, nq));
+    p->bytes += int64_t(nq);
+    PII_TRY(nyq_corr_prepare(p));
   }
   return PII_OK;
 }

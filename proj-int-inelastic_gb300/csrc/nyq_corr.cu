@@ -37,12 +37,18 @@ constexpr int PL = 32 * 33;  // plane footprint: rows padded to 33 (row and colu
 // shared memory: f of the cell [a][b][c ^ b] (float), f^ on the three Nyquist
 // planes [3][N2] (float2), P[PB][3] planes (float2), the phase / gain rows of
 // two batches [2][PB][2][96] (the next batch's copied by cp.async while this
-// one runs) and the batch's row factors [PB][2][6 x 32] (float2); the
+// one runs), the batch's row factors [PB][2][6 x 32] (float2) and the radial
+// sinc values of two batches [2][PB][GSN] (staged like the rows); the
 // correction accumulator lives in registers (each thread owns the same points
 // in every batch)
 constexpr size_t OFF_P = size_t(N3) * sizeof(float) + size_t(3 * N2) * sizeof(float2);
-constexpr size_t SMEM = OFF_P + size_t(3 * PB) * PL * sizeof(float2) + size_t(2 * PB) * 2 * 96 * sizeof(float2) +
-                        size_t(PB) * 2 * 6 * 32 * sizeof(float2);
+// radial sinc values gsinc[r][m] of a pair's radial node on the Nyquist planes:
+// m = |k|^2 in [256, 768], 513 of them (padded to 516)
+constexpr int GSN = 516;
+constexpr size_t OFF_GS = OFF_P + size_t(3 * PB) * PL * sizeof(float2) + size_t(2 * PB) * 2 * 96 * sizeof(float2) +
+                          size_t(PB) * 2 * 6 * 32 * sizeof(float2);
+constexpr size_t SMEM = OFF_GS + size_t(2 * PB) * GSN * sizeof(float);
+static_assert(SMEM <= 232448, "shared memory per CTA");
 static_assert((OFF_P + size_t(3 * PB) * PL * sizeof(float2)) % 16 == 0, "cp.async destinations are 16-byte aligned");
 constexpr int PTS = 3 * N2 / THREADS;  // Nyquist points per thread
 __device__ __forceinline__ int sw(int r, int c) { return r * 33 + c; }
@@ -192,6 +198,7 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
   float2* P = reinterpret_cast<float2*>(smem_raw + OFF_P);  // [PB][3] planes: P, then R, then U
   float2* RowsBuf = P + PB * 3 * PL;                         // [2][PB][2][96]: phase rows, gain rows
   float2* Fac = RowsBuf + 2 * PB * 2 * 96;                   // [PB][2][6 x 32] row factors
+  float* GsBuf = reinterpret_cast<float*>(smem_raw + OFF_GS);  // [2][PB][GSN] radial sinc values
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int64_t cell = blockIdx.x / a.blocks;
   const int blk = int(blockIdx.x - cell * a.blocks);
@@ -206,7 +213,8 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
     Fh[i] = fh[plane == 0 ? (16 * N2 + r * 32 + c) : plane == 1 ? (r * N2 + 16 * 32 + c) : (r * N2 + c * 32 + 16)];
   }
   // rows of the nbn pairs from jb into buffer b: 16-byte copies (a row is 48),
-  // zeros for absent pairs
+  // zeros for absent pairs; and their radial sinc values gsinc[r][256 ..] (4-byte copies)
+  const float* gsn = a.gsinc + cell * a.gs_stride;
   auto stage_rows = [&](int jb, int nbn, int b) {
     float2* dst = RowsBuf + b * PB * 192;
     for (int i = t; i < PB * 2 * 48; i += THREADS) {
@@ -219,6 +227,11 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
         d[1] = make_float2(0.f, 0.f);
       }
     }
+    float* gdst = GsBuf + b * PB * GSN;
+    for (int i = t; i < PB * 513; i += THREADS) {
+      const int sidx = i / 513, m = i - sidx * 513;
+      if (sidx < nbn) cp_async4(gdst + sidx * GSN + m, gsn + int64_t(a.reps[jb + sidx] / a.ns) * (a.M + 1) + 256 + m);
+    }
   };
   if (i0 < i1) stage_rows(i0, min(PB, i1 - i0), 0);
   cp_async_wait_all();
@@ -230,6 +243,7 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
   for (int ib = i0, bp = 0; ib < i1; ib += PB, bp ^= 1) {
     const int nb = min(PB, i1 - ib);
     const float2* Rows = RowsBuf + bp * PB * 192;  // this batch's rows (staged during the previous batch)
+    const float* Gs = GsBuf + bp * PB * GSN;       // and their radial sinc values
     // the next batch's rows into the other buffer, last read before the previous batch's final barrier
     if (ib + PB < i1) stage_rows(ib + PB, min(PB, i1 - ib - PB), bp ^ 1);
     for (int i = t; i < PB * 2 * 192; i += THREADS) row_factors(Rows + (i / 192) * 96, Fac + (i / 192) * 192, i % 192);
@@ -335,8 +349,7 @@ __global__ void __launch_bounds__(nq::THREADS, 1) k_nyq_corr(NyqArgs a) {
 #pragma unroll
       for (int s = 0; s < PB; ++s) {
         if (s >= nb) break;
-        const int p = a.reps[ib + s];
-        const float gsv = a.gsinc[cell * a.gs_stride + int64_t(p / a.ns) * (a.M + 1) + kk];
+        const float gsv = Gs[s * GSN + kk - 256];  // kk >= 256: one component is the Nyquist index
         const float2 gm = minus_from(Rows + s * 192 + 96, Fac + s * 384 + 192, plane, r, c);
         const float wx = gsv * gm.x, wy = gsv * gm.y;
         const float2 u = P[(s * 3 + plane) * PL + sw(r, c)];

@@ -26,6 +26,11 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+// the same for one 4-byte word (both addresses 4-byte aligned)
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 struct PerDeviceOnce {
@@ -41,7 +46,9 @@ struct PerDeviceOnce {
 };
 
 // modes of the first-axis column pass (collide_kernels.cuh, col_tc.cu)
-enum ColMode { COL_FWD = 0, COL_PSTART = 1, COL_PEND = 2, COL_IPREP = 3 };
+// column passes along the first velocity axis; the _PK modes take antipodal
+// passes (cell, antipodal pair) instead of (cell, pair) items
+enum ColMode { COL_FWD = 0, COL_PSTART = 1, COL_PEND = 2, COL_IPREP = 3, COL_PSTART_PK = 4, COL_PEND_PK = 5 };
 
 enum Stage {
   ST_FWD_PLANE = 0, ST_COL_FWD, ST_COL_PSTART, ST_PAIR_PLANE, ST_COL_PEND, ST_REDUCE,
@@ -168,7 +175,9 @@ struct pii_plan {
   double delta3 = 0;        // velocity cell volume of the last splitting step
   // gain kernel for n = 32, FP32: 0 = column/plane pipeline, 1 = fused
   // 2-CTA-cluster kernel, 2 = fused a-parity kernel (tensor-memory accumulator),
-  // 3 = a-parity kernel on antipodal pairs + Nyquist correction
+  // 3 = a-parity kernel on antipodal pairs + Nyquist correction; for other n
+  // (FP32, antipodally symmetric design): 0 = pipeline on (cell, pair) items,
+  // 3 = pipeline on antipodal passes + the general Nyquist correction
   int gain_path = 0;
   // tunables (pii_plan_autotune): work items per resident cluster, and the
   // points per chunk of the pipeline path (cells per chunk = this / n^3)
@@ -183,7 +192,8 @@ struct pii_plan {
   void* gp_hpart = nullptr;  // its per-item Hermitian slots
   int* ap_reps = nullptr;    // device: representative pair of each antipodal pair (0 if the design is not symmetric)
   int ap_count = 0;
-  void* nq_part = nullptr;   // Nyquist-correction accumulators [<= 16 SMs + batch_max CTAs][3][1024]
+  void* nq_part = nullptr;   // Nyquist-correction accumulators [CTAs][3][n^2]
+  int64_t nq_ctas = 0;       // their capacity in CTAs (the general kernel, n != 32)
   // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core
   // FFT (k_col), 1 = tensor-core split-FP16 DFT (k_col_tc)
   int dft_path = 0;
@@ -248,6 +258,9 @@ int col_tc_prepare(pii_plan* p);
 int col_tc_run(pii_plan* p, int mode, int64_t items, int64_t c0, int64_t p0, int64_t np, cudaStream_t s);
 int col_tc_bounds(pii_plan* p, int64_t cells, cudaStream_t s);
 int col_tc_gain_tables(pii_plan* p);  // (re)builds the sinc slices of every restitution set
+// nyq_gen.cu: Nyquist-plane correction of the packed pipeline (n != 32, FP32)
+int nyq_gen_prepare(pii_plan* p);
+int nyq_gen_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // col_tc.cu: PII_ERR_STALL if a tensor-core DFT launch of an earlier call gave
 // up waiting (read from mapped host memory without a synchronisation; cleared
 // once reported)
@@ -272,8 +285,9 @@ template <typename T, int NV>
 struct CollideKernels {
   static int prepare();
   static int fwd(pii_plan* p, const double* f, int64_t c0, int64_t cells, cudaStream_t s);
+  // items (cell, pair) for pairs [p0, p0 + np); packed: antipodal passes [p0, p0 + np) of p->ap_reps
   static int pairs(pii_plan* p, int64_t c0, int64_t cells, int64_t p0, int64_t np, bool first,
-                   cudaStream_t s);
+                   cudaStream_t s, bool packed = false);
   static int finish(pii_plan* p, const double* f, double* q, int64_t c0, int64_t cells, int with_loss,
                     double hb, cudaStream_t s);
 };

@@ -7,6 +7,7 @@
 //   exp(-i pi r k.sigma / L) = prod_d exp(-i pi r sigma_d k_d / L)   (per-axis rows)
 //   exp(+i a(r) r k.sigma)    = prod_d exp(+i a(r) r sigma_d k_d)    (per-axis rows)
 //   sinc(a(r) r |k|), sinc(pi r |k| / L) depend on |k|^2 = m only  (tables over m)
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -300,6 +301,39 @@ static int upload_tables(pii_plan* p) {
   return upload_gain_tables<T>(p, {{p->e, p->e0}});
 }
 
+// Antipodal passes: the symmetric designs list every direction with its
+// negative, whose phase and gain tables are the conjugates
+// (src/collision/inelastic_collisions.py:86-105: k . sigma changes sign).  One
+// representative pair (ir, i < mate(i)) per antipodal pair and radial node, in
+// radial-node order; none when the design is not antipodally symmetric.
+static int antipodal_setup(pii_plan* p) {
+  const int ns = p->ns;
+  std::vector<int> mate(ns, -1);
+  bool sym = p->dim == 3 && ns % 2 == 0;
+  for (int i = 0; i < ns && sym; ++i) {
+    for (int j = 0; j < ns; ++j) {
+      double d = 0;
+      for (int k = 0; k < 3; ++k) d = std::max(d, std::fabs(p->sigma[3 * i + k] + p->sigma[3 * j + k]));
+      if (d < 1e-12) {
+        mate[i] = j;
+        break;
+      }
+    }
+    sym = mate[i] >= 0 && mate[i] != i;
+  }
+  if (!sym) return PII_OK;
+  std::vector<int> reps;
+  for (int ir = 0; ir < p->nr; ++ir)
+    for (int i = 0; i < ns; ++i)
+      if (i < mate[i]) reps.push_back(ir * ns + i);
+  if (int(reps.size()) * 2 != p->Q) return PII_OK;
+  PII_CUDA(cudaMalloc(&p->ap_reps, reps.size() * sizeof(int)));
+  PII_CUDA(cudaMemcpy(p->ap_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
+  p->bytes += int64_t(reps.size() * sizeof(int));
+  p->ap_count = int(reps.size());
+  return PII_OK;
+}
+
 static int alloc(pii_plan* p, void** dst, size_t bytes) {
   PII_CUDA(cudaMalloc(dst, bytes));
   p->bytes += int64_t(bytes);
@@ -393,7 +427,7 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
     free_plan(p);
     return s2;
   }
-  if ((s2 = prepare_impl(p)) != PII_OK) {
+  if ((s2 = prepare_impl(p)) != PII_OK || (s2 = antipodal_setup(p)) != PII_OK) {
     free_plan(p);
     return s2;
   }
@@ -407,6 +441,14 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
   if (n == 64 && precision == PII_PREC_FP32 && dim == 3 && (s2 = col_tc_prepare(p)) != PII_OK) {
     free_plan(p);
     return s2;
+  }
+  if (n != 32 && precision == PII_PREC_FP32 && dim == 3 && p->ap_count > 0) {
+    // the packed pipeline: antipodal passes (half the items) plus the general Nyquist correction
+    if ((s2 = nyq_gen_prepare(p)) != PII_OK) {
+      free_plan(p);
+      return s2;
+    }
+    p->gain_path = 3;
   }
   *out = p;
   return PII_OK;

@@ -1,0 +1,68 @@
+"""The packed pipeline (antipodal passes + the general Nyquist correction) against the oracle.
+
+For every n other than 32 the FP32 plans of an antipodally symmetric design
+evaluate each direction pair (sigma, -sigma) in one pass of the column /
+plane pipeline with a real phase, and add what the pass leaves out on the
+three Nyquist planes (k_nyq_gen).  Checked against the oracle's Q
+(src/collision/inelastic_collisions.py:208-227) on smooth and on rough input
+(uniform random f: a full spectrum, where the Nyquist planes carry weight),
+next to the unpacked pipeline, with an r-dependent restitution (e != e0).
+"""
+import numpy as np
+import pytest
+
+from conftest import L8_S, maxwellian, op_config, rel_linf
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5  # mixed precision against FP64
+CASES = [(8, 4, 6), (16, 8, 12), (24, 4, 12), (48, 3, 6), (64, 2, 6)]
+
+
+@pytest.mark.parametrize("n,nr,ns", CASES)
+def test_packed_pipeline_matches_oracle(n, nr, ns):
+    import proj_int_inelastic_gb300 as pkg
+    from oracle import fs_inelastic as fo
+
+    cfg = op_config(n, L8_S, nr, ns, 0.6, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    v = sm.v_center
+    smooth = maxwellian(v, 1.0, (0.7, -0.4, 0.2), 1.1) + maxwellian(v, 0.6, (-1.2, 0.5, 0.3), 0.7)
+    rough = np.random.default_rng(n).uniform(0.1, 1.0, (n, n, n)) * 0.05
+    f = np.stack([smooth, rough])
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=2)
+    assert col.plan.tuning["gain_path"] == "packed"  # the default where the design is antipodally symmetric
+    ft = torch.as_tensor(f, device="cuda:0")
+    qp = col.collide(ft, with_loss=True).cpu().numpy()
+    gp = col.collide(ft, with_loss=False).cpu().numpy()
+    col.plan.set_tuning("pipeline", 6, 131072)
+    qu = col.collide(ft, with_loss=True).cpu().numpy()
+    op = fo.FSInelasticVHS(fo.Mesh(n, L8_S, nr, ns), 0.6, 0.9, 1.0)
+    for c in range(2):
+        ref = op.collide_cell(f[c], with_loss=True)
+        refg = op.collide_cell(f[c], with_loss=False)
+        ep, eu, eg = rel_linf(qp[c], ref), rel_linf(qu[c], ref), rel_linf(gp[c], refg)
+        print(f"n={n} cell {c}: packed {ep:.2e} (gain only {eg:.2e}), unpacked {eu:.2e}")
+        assert ep < TOL and eg < TOL and eu < TOL, c
+
+
+def test_packed_pipeline_per_cell_restitution_and_chunks():
+    """Three cells with their own restitution laws and chunks of one cell
+    (n = 16, 8 x 12 quadrature: 48 antipodal passes)."""
+    import proj_int_inelastic_gb300 as pkg
+    from oracle import fs_inelastic as fo
+
+    cfg = op_config(16, L8_S, 8, 12, 0.9, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    rng = np.random.default_rng(5)
+    f = rng.uniform(0.1, 1.0, (3, 16, 16, 16)) * 0.05
+    sets = [(0.3, 0.3), (0.8, 1.0), (1.0, 1.0)]
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=3)
+    col.plan.set_restitution([e for e, _ in sets], [e0 for _, e0 in sets])
+    col.plan.set_tuning("packed", 6, 4096)  # one cell per chunk
+    q = col.collide(torch.as_tensor(f, device="cuda:0"), with_loss=True).cpu().numpy()
+    mesh = fo.Mesh(16, L8_S, 8, 12)
+    for c, (e, e0) in enumerate(sets):
+        ref = fo.FSInelasticVHS(mesh, e, e0, 1.0).collide_cell(f[c], with_loss=True)
+        assert rel_linf(q[c], ref) < TOL, c
