@@ -413,6 +413,11 @@ def measure_c4(pkg, device, macro_steps=10, fp64_steps=1):
         return m, e, float(np.mean(T))
 
     m0, e0, T0 = mass_energy()
+    # time one macro-step advances under the reference's telescopic recurrence
+    # (src/boltzmann.py:142-158: level l adds M_l ... M_0 inner increments of dt0)
+    (K0, K1, K2), (h0, h1, h2) = C4_K, C4_H
+    M0, M1, M2 = h1 / h0 - K0, h2 / h1 - K1, C4_DT / h2 - K2
+    tau = K2 * (K1 * h1 + M1 * M0 * h0) + M2 * M1 * M0 * h0
     stream = solver._get_stream(device)
     solver.step(sol, False, 0.0, C4_DT)  # capture the macro-step graph (excluded from the record below)
     sol.state.f.copy_(f0)
@@ -428,7 +433,8 @@ def measure_c4(pkg, device, macro_steps=10, fp64_steps=1):
         torch.cuda.synchronize()
         ms += a.elapsed_time(b)
         m, e, T = mass_energy()
-        rec.append({"t": (k + 1) * C4_DT, "mass_rel": m / m0 - 1.0, "energy_rel": e / e0 - 1.0, "T_mean": T,
+        rec.append({"t": (k + 1) * C4_DT, "t_advanced": (k + 1) * tau, "mass_rel": m / m0 - 1.0,
+                    "energy_rel": e / e0 - 1.0, "T_mean": T, "f_min": float(sol.f.min()),
                     "finite": bool(torch.isfinite(sol.f).all())})
         if k < fp64_steps:
             keep.append(sol.f.clone())
@@ -437,6 +443,7 @@ def measure_c4(pkg, device, macro_steps=10, fp64_steps=1):
                      f"[-8,8]^3, 32x32, e=e0={C4_E}, hard spheres, mass fix; levels dt={C4_H}, K={C4_K}, "
                      f"macro dt={C4_DT}", "cells": C4_NX, "macro_steps": macro_steps,
            "cell_evals_per_s": evals / (ms / 1e3), "ms_per_macro_step": ms / macro_steps,
+           "time_advanced_per_macro_step": tau,
            "mass_drift_max": max(abs(r["mass_rel"]) for r in rec), "energy_rel_end": rec[-1]["energy_rel"],
            "T_mean_end": rec[-1]["T_mean"], "t_end": rec[-1]["t"], "all_finite": all(r["finite"] for r in rec),
            "per_macro_step": rec if macro_steps <= 20 else rec[:: max(1, macro_steps // 20)] + [rec[-1]]}

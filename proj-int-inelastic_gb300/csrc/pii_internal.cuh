@@ -32,6 +32,12 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// close the current group of cp.async copies; wait until at most N groups are pending
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 struct PerDeviceOnce {
   std::atomic<uint64_t> mask{0};
@@ -194,6 +200,8 @@ struct pii_plan {
   int ap_count = 0;
   void* nq_part = nullptr;   // Nyquist-correction accumulators [CTAs][3][n^2]
   int64_t nq_ctas = 0;       // their capacity in CTAs (the general kernel, n != 32)
+  void* nq_ft2 = nullptr;    // general kernel: f transposed within each a-plane [batch_max][n^3] (FP32)
+  void* nq_fhn = nullptr;    // general kernel: f^ at the Nyquist-plane points [batch_max][3 n^2]
   // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core
   // FFT (k_col), 1 = tensor-core split-FP16 DFT (k_col_tc)
   int dft_path = 0;

@@ -348,7 +348,7 @@ static void free_plan(pii_plan* p) {
   void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsxc, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
                   p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag,
-                  p->dft_img,    p->dft_gs,     p->dft_colb};
+                  p->dft_img,    p->dft_gs,     p->dft_colb,  p->nq_ft2,    p->nq_fhn};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (p->dft_err_host) cudaFreeHost(p->dft_err_host);
