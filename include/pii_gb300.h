@@ -148,6 +148,19 @@ int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stre
  */
 int pii_plan_set_dft_path(pii_plan* plan, int path);
 int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stalled);
+/*
+ * Nyquist-plane correction of the packed gain paths (no reference
+ * counterpart: the packing is this library's): 0 = the quadratic form
+ * C(k) = sum_q A(k, q) f^(q) f^(k - q) - B(k, q) conj f^(q) f^(k + q) with the
+ * kernels A, B (N x N real, N = 3 n^2 - 3 n + 1 Nyquist points) precomputed
+ * once per plan and restitution set, 1 = the direct per-pass kernels.  FP32
+ * 3D plans on an antipodally symmetric design; the default is 0 for n = 64
+ * (built at plan creation when A, B fit the memory budget) and 1 otherwise
+ * (path 0 then builds them on request).  set drops captured step graphs; get
+ * returns the path in use (-1 for NULL).
+ */
+int pii_plan_set_nyquist_path(pii_plan* plan, int path);
+int pii_plan_get_nyquist_path(const pii_plan* plan);
 /* Test hooks of the tensor-core kernel's bounded waits (no reference
  * counterpart): wait_limit = mbarrier polls before a role gives up (default
  * 4194304); withhold = 1 makes the TMA thread issue no copies at all, so the

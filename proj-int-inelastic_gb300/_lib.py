@@ -52,6 +52,8 @@ SIGNATURES = {
     "pii_plan_set_dft_path": (_c_int, [_vp, _c_int]),
     "pii_plan_get_dft_path": (_c_int, [_vp, _pint, _pint]),
     "pii_plan_dft_test_hooks": (_c_int, [_vp, ctypes.c_uint32, _c_int]),
+    "pii_plan_set_nyquist_path": (_c_int, [_vp, _c_int]),
+    "pii_plan_get_nyquist_path": (_c_int, [_vp]),
     "pii_collide": (_c_int, [_vp, _vp, _vp, _c_i64, _c_int, _c_dbl, _c_int, _vp]),
     "pii_laplacian": (_c_int, [_vp, _vp, _vp, _c_i64, _vp]),
     "pii_transport_df": (_c_int, [_vp, _vp, _vp, _c_i64, _c_dbl, _c_dbl, _pdbl, _c_int, _c_int, _vp]),

@@ -268,6 +268,20 @@ class Plan:
         _lib.check(self._lib.pii_plan_set_dft_path(self.handle, _code(DFT_PATHS, dft_path, "dft_path")),
                    "pii_plan_set_dft_path")
 
+    NYQUIST_PATHS = {"quadratic": 0, "direct": 1}
+
+    def set_nyquist_path(self, path):
+        """Nyquist-plane correction of the packed paths: "quadratic" (the
+        precomputed quadratic form in f^, the default for n = 64, built on
+        request otherwise) or "direct" (the per-pass kernels),
+        ``pii_plan_set_nyquist_path``."""
+        _lib.check(self._lib.pii_plan_set_nyquist_path(self.handle, _code(self.NYQUIST_PATHS, path, "nyquist_path")),
+                   "pii_plan_set_nyquist_path")
+
+    @property
+    def nyquist_path(self):
+        return {0: "quadratic", 1: "direct"}.get(int(self._lib.pii_plan_get_nyquist_path(self.handle)))
+
     def set_restitution(self, e, e0):
         """Per-cell restitution: cell c of later calls uses (e[c], e0[c])
         (``pii_plan_set_restitution``); empty sequences restore the plan's own."""

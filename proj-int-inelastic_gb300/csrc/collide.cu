@@ -33,7 +33,7 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
         PII_TRY(gain_cluster_run(p, cells, s));
       } else {
         PII_TRY(gain_parity_run(p, cells, s, p->gain_path == 3));
-        if (p->gain_path == 3) PII_TRY(nyq_corr_run(p, cells, s));
+        if (p->gain_path == 3) PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_corr_run(p, cells, s));
       }
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
@@ -53,7 +53,8 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
       PII_TRY(K::pairs(p, c0, cc, p0, np, p0 == 0, s, packed));
     }
   }
-  if (packed) PII_TRY(nyq_gen_run(p, cells, s));  // what the packed passes leave out, on the Nyquist planes
+  // what the packed passes leave out, on the Nyquist planes
+  if (packed) PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_gen_run(p, cells, s));
   return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
 }
 
@@ -320,6 +321,30 @@ extern "C" int pii_plan_dft_test_hooks(pii_plan* plan, uint32_t wait_limit, int 
   plan->dft_withhold = withhold ? 1 : 0;
   pii::graphs_clear(plan);  // captured graphs baked the old arguments in
   return PII_OK;
+}
+
+extern "C" int pii_plan_set_nyquist_path(pii_plan* plan, int path) {
+  if (!plan || path < 0 || path > 1) {
+    pii::set_error("pii_plan_set_nyquist_path: path must be 0 (quadratic form) or 1 (direct kernels)");
+    return PII_ERR_ARG;
+  }
+  if (path == 0 && !plan->nq_A) {
+    PII_CUDA(cudaSetDevice(plan->device));
+    PII_TRY(pii::nyq_quad_prepare(plan));  // built on request
+    if (!plan->nq_A) {
+      pii::set_error("pii_plan_set_nyquist_path: no quadratic-form kernels for this plan (not an FP32 3D plan on an "
+                     "antipodally symmetric design, or beyond the memory budget)");
+      return PII_ERR_ARG;
+    }
+  }
+  plan->nyq_path = path;
+  pii::graphs_clear(plan);  // captured graphs baked the old choice in
+  return PII_OK;
+}
+
+extern "C" int pii_plan_get_nyquist_path(const pii_plan* plan) {
+  if (!plan) return -1;
+  return pii::nyq_use_quad(plan) ? 0 : 1;
 }
 
 extern "C" int pii_laplacian(pii_plan* plan, const double* f, double* out, int64_t cells, void* stream) {

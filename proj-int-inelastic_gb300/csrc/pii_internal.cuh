@@ -200,6 +200,17 @@ struct pii_plan {
   int ap_count = 0;
   void* nq_part = nullptr;   // Nyquist-correction accumulators [CTAs][3][n^2]
   int64_t nq_ctas = 0;       // their capacity in CTAs (the general kernel, n != 32)
+  // quadratic-form Nyquist correction (nyq_quad.cu): kernels A, B [sets][Nq][Nq]
+  // ([q][k]), the Nyquist points, f^ transposed within each a-plane and f^ at
+  // the points; nyq_path 0 uses it where built, 1 the direct kernels
+  void* nq_A = nullptr;
+  void* nq_B = nullptr;
+  void* nq_pts = nullptr;
+  void* nq_fhT = nullptr;
+  void* nq_fhq = nullptr;
+  int nq_npts = 0;
+  int64_t nq_quad_bytes = 0;
+  int nyq_path = 0;
   void* nq_ft2 = nullptr;    // general kernel: f transposed within each a-plane [batch_max][n^3] (FP32)
   void* nq_fhn = nullptr;    // general kernel: f^ at the Nyquist-plane points [batch_max][3 n^2]
   // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core
@@ -269,6 +280,13 @@ int col_tc_gain_tables(pii_plan* p);  // (re)builds the sinc slices of every res
 // nyq_gen.cu: Nyquist-plane correction of the packed pipeline (n != 32, FP32)
 int nyq_gen_prepare(pii_plan* p);
 int nyq_gen_run(pii_plan* p, int64_t cells, cudaStream_t s);
+// nyq_quad.cu: the same correction as a quadratic form in f^ with precomputed kernels
+int nyq_quad_prepare(pii_plan* p);
+void nyq_quad_release(pii_plan* p);
+int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s);
+// the Nyquist correction of the packed paths: the quadratic form where it was
+// built and chosen, else the direct kernel of the plan's n
+inline bool nyq_use_quad(const pii_plan* p) { return p->nyq_path == 0 && p->nq_A != nullptr; }
 // col_tc.cu: PII_ERR_STALL if a tensor-core DFT launch of an earlier call gave
 // up waiting (read from mapped host memory without a synchronisation; cleared
 // once reported)

@@ -348,7 +348,8 @@ static void free_plan(pii_plan* p) {
   void* ptrs[] = {p->tab.ephase, p->tab.gphase, p->tab.epar, p->tab.gpar, p->tab.gsx, p->tab.gsxc, p->tab.gsinc, p->tab.lossk, p->tab.lapl, p->fhat, p->fT,
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
                   p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag,
-                  p->dft_img,    p->dft_gs,     p->dft_colb,  p->nq_ft2,    p->nq_fhn};
+                  p->dft_img,    p->dft_gs,     p->dft_colb,  p->nq_ft2,    p->nq_fhn,
+                  p->nq_A,       p->nq_B,       p->nq_pts,    p->nq_fhT,    p->nq_fhq};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (p->dft_err_host) cudaFreeHost(p->dft_err_host);
@@ -450,6 +451,17 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
     }
     p->gain_path = 3;
   }
+  // the Nyquist correction: the quadratic form by default for n = 64 (measured
+  // faster there, 17.1 vs 22.2 ms on 16 cells; at n <= 48 the direct kernels
+  // win), built on request for other n (pii_plan_set_nyquist_path)
+  p->nyq_path = 1;
+  if (precision == PII_PREC_FP32 && dim == 3 && p->ap_count > 0 && n >= 64) {
+    if ((s2 = nyq_quad_prepare(p)) != PII_OK) {
+      free_plan(p);
+      return s2;
+    }
+    if (p->nq_A) p->nyq_path = 0;
+  }
   *out = p;
   return PII_OK;
 }
@@ -503,6 +515,10 @@ int pii_plan_set_restitution(pii_plan* plan, const double* e, const double* e0, 
   if (st != PII_OK) return st;
   if (plan->tab.nsets > 1 && plan->gain_path == 1) plan->gain_path = plan->ap_count > 0 ? 3 : 2;
   if (plan->dft_img) PII_TRY(col_tc_gain_tables(plan));  // the tensor-core path's sinc slices
+  if (plan->nq_A) {  // A, B per set, rebuilt for the new sets (or dropped beyond the budget)
+    PII_TRY(nyq_quad_prepare(plan));
+    if (!plan->nq_A) plan->nyq_path = 1;
+  }
   graphs_clear(plan);  // captured graphs baked the old tables in
   return PII_OK;
 }

@@ -20,8 +20,9 @@ TOL = 1e-5  # mixed precision against FP64
 CASES = [(8, 4, 6), (16, 8, 12), (24, 4, 12), (48, 3, 6), (64, 2, 6)]
 
 
+@pytest.mark.parametrize("nyq", ["quadratic", "direct"])
 @pytest.mark.parametrize("n,nr,ns", CASES)
-def test_packed_pipeline_matches_oracle(n, nr, ns):
+def test_packed_pipeline_matches_oracle(n, nr, ns, nyq):
     import proj_int_inelastic_gb300 as pkg
     from oracle import fs_inelastic as fo
 
@@ -33,6 +34,10 @@ def test_packed_pipeline_matches_oracle(n, nr, ns):
     f = np.stack([smooth, rough])
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=2)
     assert col.plan.tuning["gain_path"] == "packed"  # the default where the design is antipodally symmetric
+    # the default correction: the quadratic form at n = 64, the direct kernels otherwise
+    assert col.plan.nyquist_path == ("quadratic" if n == 64 else "direct")
+    col.plan.set_nyquist_path(nyq)  # the other one is built on request
+    assert col.plan.nyquist_path == nyq
     ft = torch.as_tensor(f, device="cuda:0")
     qp = col.collide(ft, with_loss=True).cpu().numpy()
     gp = col.collide(ft, with_loss=False).cpu().numpy()
@@ -43,11 +48,12 @@ def test_packed_pipeline_matches_oracle(n, nr, ns):
         ref = op.collide_cell(f[c], with_loss=True)
         refg = op.collide_cell(f[c], with_loss=False)
         ep, eu, eg = rel_linf(qp[c], ref), rel_linf(qu[c], ref), rel_linf(gp[c], refg)
-        print(f"n={n} cell {c}: packed {ep:.2e} (gain only {eg:.2e}), unpacked {eu:.2e}")
+        print(f"n={n} {nyq} cell {c}: packed {ep:.2e} (gain only {eg:.2e}), unpacked {eu:.2e}")
         assert ep < TOL and eg < TOL and eu < TOL, c
 
 
-def test_packed_pipeline_per_cell_restitution_and_chunks():
+@pytest.mark.parametrize("nyq", ["quadratic", "direct"])
+def test_packed_pipeline_per_cell_restitution_and_chunks(nyq):
     """Three cells with their own restitution laws and chunks of one cell
     (n = 16, 8 x 12 quadrature: 48 antipodal passes)."""
     import proj_int_inelastic_gb300 as pkg
@@ -61,6 +67,7 @@ def test_packed_pipeline_per_cell_restitution_and_chunks():
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=3)
     col.plan.set_restitution([e for e, _ in sets], [e0 for _, e0 in sets])
     col.plan.set_tuning("packed", 6, 4096)  # one cell per chunk
+    col.plan.set_nyquist_path(nyq)
     q = col.collide(torch.as_tensor(f, device="cuda:0"), with_loss=True).cpu().numpy()
     mesh = fo.Mesh(16, L8_S, 8, 12)
     for c, (e, e0) in enumerate(sets):

@@ -132,3 +132,39 @@ def test_nyquist_planes_from_2d_transforms():
     assert np.abs(np.fft.fft2(ra) - u[h, :, :]).max() < 1e-13 * scale
     assert np.abs(np.fft.fft2(rb) - u[:, h, :]).max() < 1e-13 * scale
     assert np.abs(np.fft.fft2(rc) - u[:, :, h]).max() < 1e-13 * scale
+
+
+def test_nyquist_correction_as_quadratic_form():
+    """3. summed over the antipodal pairs, the correction is a quadratic form in
+    f^ with REAL kernels that depend on the tables only (what the default
+    correction, nyq_quad.cu, evaluates):
+      sum_p C_p(k) = sum_q A(k, q) f^(q) f^(k - q) - B(k, q) conj f^(q) f^(k + q),
+      A(k, q) = sum_p (w.x - w.y)_p(k) t-_p(q),  B(k, q) = sum_p (w.x + w.y)_p(k) t-_p(q),
+    with k, q over the Nyquist points (t-_p carries the inverse transform's 1/N)."""
+    n = 8
+    mesh = fo.Mesh(n, L8_S, 3, 6)
+    op = fo.FSInelasticVHS(mesh, 0.8, 0.8, 1.0)
+    f = np.random.default_rng(1).uniform(0.1, 1.0, (n, n, n))
+    fh = _fft3(f)
+    pts = np.argwhere(_nyquist_mask(n))
+    idx = tuple(pts.T)
+    ctot = np.zeros((n, n, n), complex)
+    A = np.zeros((len(pts), len(pts)))
+    B = np.zeros_like(A)
+    for ir in range(mesh.nr):
+        gain, expt = op.tables_r(ir)
+        for p, _ in _antipodes(mesh.sigma):
+            ep, gp = _herm(expt[p]), _herm(gain[p])
+            em, gm = expt[p] - ep, gain[p] - gp
+            tm = em.real + em.imag
+            u = _fft3(_ifft3(fh * tm) * f)
+            ctot += (gm.real - gm.imag) * u - (gm.real + gm.imag) * np.conj(_reflect(u))
+            tq = tm[idx] / n**3
+            A += np.outer((gm.real - gm.imag)[idx], tq)
+            B += np.outer((gm.real + gm.imag)[idx], tq)
+    km = (pts[:, None, :] - pts[None, :, :]) % n
+    kp = (pts[:, None, :] + pts[None, :, :]) % n
+    fq = fh[idx][None, :]
+    quad = (A * fq * fh[tuple(km.transpose(2, 0, 1))] - B * np.conj(fq) * fh[tuple(kp.transpose(2, 0, 1))]).sum(1)
+    ref = ctot[idx]
+    assert np.abs(quad - ref).max() < 1e-13 * np.abs(ref).max()
