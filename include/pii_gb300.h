@@ -154,10 +154,10 @@ int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stalled);
  * C(k) = sum_q A(k, q) f^(q) f^(k - q) - B(k, q) conj f^(q) f^(k + q) with the
  * kernels A, B (N x N real, N = 3 n^2 - 3 n + 1 Nyquist points) precomputed
  * once per plan and restitution set, 1 = the direct per-pass kernels.  FP32
- * 3D plans on an antipodally symmetric design; the default is 0 for n = 64
- * (built at plan creation when A, B fit the memory budget) and 1 otherwise
- * (path 0 then builds them on request).  set drops captured step graphs; get
- * returns the path in use (-1 for NULL).
+ * 3D plans on an antipodally symmetric design, n a multiple of 8 up to 64;
+ * the default is 0 where A, B (2 x 3 N n^2 floats per set) fit the memory
+ * budget, else 1.  set drops captured step graphs (path 0 builds A, B on
+ * request); get returns the path in use (-1 for NULL).
  */
 int pii_plan_set_nyquist_path(pii_plan* plan, int path);
 int pii_plan_get_nyquist_path(const pii_plan* plan);

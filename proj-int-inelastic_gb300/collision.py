@@ -272,8 +272,8 @@ class Plan:
 
     def set_nyquist_path(self, path):
         """Nyquist-plane correction of the packed paths: "quadratic" (the
-        precomputed quadratic form in f^, the default for n = 64, built on
-        request otherwise) or "direct" (the per-pass kernels),
+        precomputed quadratic form in f^, the default where its kernels fit
+        the memory budget) or "direct" (the per-pass kernels),
         ``pii_plan_set_nyquist_path``."""
         _lib.check(self._lib.pii_plan_set_nyquist_path(self.handle, _code(self.NYQUIST_PATHS, path, "nyquist_path")),
                    "pii_plan_set_nyquist_path")

@@ -1,6 +1,6 @@
 // Nyquist-plane correction of the packed gain paths as a quadratic form in f^
-// (FP32, every n; the default for n = 64, where it beats the direct kernels,
-// built on request for other n).
+// (FP32, n a multiple of 8 up to 64; the default wherever its kernels fit the
+// memory budget, the direct kernels of nyq_corr.cu / nyq_gen.cu otherwise).
 //
 // Per antipodal pass p the packed evaluation leaves out, on the Nyquist planes
 // only (nyq_corr.cu / nyq_gen.cu state it in full),
@@ -15,11 +15,26 @@
 // A and B (Nq x Nq, Nq = 3 n^2 - 3 n + 1 Nyquist points) are built once per
 // plan and restitution set: k_quad_coef evaluates t-, w.x - w.y and w.x + w.y
 // from the plan's FP32 rows (as the direct kernels do), k_quad_gemm contracts
-// them over the passes.  Per call k_quad_prep lays out f^ at the Nyquist
-// points and f^ transposed within each a-plane, and k_nyq_quad forms C(k) for
-// a tile of output points and a group of cells per CTA: A and B are read
-// coalesced ([q][k]) once per group, f^(k -+ q) gathered coalesced along each
-// output row (from the transposed copy for the plane k_c = n/2).
+// them over the passes, storing them in the order the correction kernel reads.
+//
+// Blocking.  The output points form three planes, one per orientation d
+// (k_a = h, k_b = h, k_c = h with h = n / 2; points of an earlier plane are
+// skipped), each indexed by its in-plane coordinates (k1, k2).  Seen from
+// orientation d, the input points q group into n slices by their coordinate
+// s along d: slice s != h is the row i1 = h plus the column i2 = h of the
+// plane at s, slice h the whole plane at h.  For k on the plane at h and q in
+// slice s, k - q lies in the plane at h - s and k + q in the plane at h + s
+// (the same plane, h - s = -(h + s) mod n), at in-plane offsets
+// (k1 -+ i1, k2 -+ i2).  k_nyq_quad stages those two planes of f^ for a group
+// of cells in shared memory once per slice (plane 0 and the input plane h for
+// s = h) and walks the slice's input points by segment (a row of n points,
+// or the column of n - 1); each thread owns R consecutive k2 of one k1, and
+// along a row it keeps the f^(k -+ q) it needs in a sliding window of
+// registers, one new value per step and plane.  A and B are laid out
+// [d][q in slice order][k2 / R][k1][k2 % R], so a warp reads them as one
+// coalesced 16-byte vector per lane and step, once per group of cells.  The
+// input points of an orientation are split into ranges across CTAs; each
+// range writes its partial sums and k_quad_add adds them into G.
 #include <algorithm>
 #include <vector>
 
@@ -29,8 +44,8 @@
 namespace pii {
 
 namespace nqq {
-constexpr int THREADS = 256;  // output points per CTA
-constexpr int GMAX = 8;       // cells per CTA when every cell shares the kernels
+constexpr int R = 4;             // consecutive k2 per thread (every supported n / 2 is a multiple)
+constexpr int SPLIT_MAX = 8;     // input-point ranges per orientation
 constexpr int TM = 64, TK = 16;  // GEMM tiles: 64 x 64 outputs, 16 passes per step
 }  // namespace nqq
 
@@ -74,8 +89,10 @@ __global__ void __launch_bounds__(256) k_quad_coef(const int* pts, int npts, int
   }
 }
 
-// C[q][k] = sum_p T[p][q] X[p][k]  (npts x npts, K = QP; both operands pass-major)
-__global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* X, float* C, int npts, int QP) {
+// C[j][kk] = sum_p T[p][qi[j]] X[p][ki[kk]]  (ki[kk] < 0: the output point is
+// skipped, its column zero); T and X rows have npts entries in point order
+__global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* X, const int* qi, const int* ki,
+                                                    float* C, int M, int Ncol, int QP, int npts) {
   using namespace nqq;
   __shared__ float ta[TK][TM], tb[TK][TM];
   const int q0 = blockIdx.y * TM, k0 = blockIdx.x * TM;
@@ -85,8 +102,9 @@ __global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* 
     for (int e = threadIdx.x; e < TK * TM; e += 256) {
       const int pp = e / TM, c = e - pp * TM;
       const bool okp = p0 + pp < QP;
-      ta[pp][c] = okp && q0 + c < npts ? T[int64_t(p0 + pp) * npts + q0 + c] : 0.f;
-      tb[pp][c] = okp && k0 + c < npts ? X[int64_t(p0 + pp) * npts + k0 + c] : 0.f;
+      const int kidx = okp && k0 + c < Ncol ? ki[k0 + c] : -1;
+      ta[pp][c] = okp && q0 + c < M ? T[int64_t(p0 + pp) * npts + qi[q0 + c]] : 0.f;
+      tb[pp][c] = kidx >= 0 ? X[int64_t(p0 + pp) * npts + kidx] : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -106,125 +124,269 @@ __global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* 
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int q = q0 + ty * 4 + i, k = k0 + tx * 4 + j;
-      if (q < npts && k < npts) C[int64_t(q) * npts + k] = acc[i][j];
+      if (q < M && k < Ncol) C[int64_t(q) * Ncol + k] = acc[i][j];
     }
 }
 
-// f^ at the Nyquist points, compact, and f^ transposed within each a-plane
-// (fhT[cell][a][c][b] = f^[cell][a][b][c], 32 x 32 tiles through shared memory)
-__global__ void __launch_bounds__(256) k_quad_prep(const float2* fhat, float2* fhn, float2* fhT, const int* pts,
-                                                    int npts, int n, int64_t cells) {
+// f^ transposed within each a-plane: fhT[cell][a][c][b] = f^[cell][a][b][c]
+// (32 x 32 tiles through shared memory)
+__global__ void __launch_bounds__(256) k_quad_prep(const float2* fhat, float2* fhT, int n, int64_t cells) {
   __shared__ float2 tile[32][33];
   const int tb_n = (n + 31) / 32;
-  const int64_t n2 = int64_t(n) * n, n3 = n2 * n;
+  const int64_t n2 = int64_t(n) * n;
   const int64_t bid = blockIdx.x;
-  const int64_t tiles = cells * n * tb_n * tb_n;
-  if (bid < tiles) {
-    const int64_t cp = bid / (tb_n * tb_n);  // (cell, a)
-    const int tt = int(bid - cp * tb_n * tb_n), tb = tt / tb_n, tc = tt - tb * tb_n;
-    const float2* src = fhat + cp * n2;
-    float2* dst = fhT + cp * n2;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-    for (int j = ty; j < 32; j += 8) {
-      const int b = tb * 32 + j, c = tc * 32 + tx;
-      if (b < n && c < n) tile[j][tx] = src[b * n + c];
-    }
-    __syncthreads();
-    for (int j = ty; j < 32; j += 8) {
-      const int c = tc * 32 + j, b = tb * 32 + tx;
-      if (b < n && c < n) dst[c * n + b] = tile[tx][j];
-    }
-  } else {
-    const int64_t gid = (bid - tiles) * 256 + threadIdx.x;
-    if (gid >= cells * npts) return;
-    const int64_t cell = gid / npts;
-    fhn[gid] = fhat[cell * n3 + pts[gid - cell * npts]];
+  const int64_t cp = bid / (tb_n * tb_n);  // (cell, a)
+  if (cp >= cells * n) return;
+  const int tt = int(bid - cp * tb_n * tb_n), tb = tt / tb_n, tc = tt - tb * tb_n;
+  const float2* src = fhat + cp * n2;
+  float2* dst = fhT + cp * n2;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int j = ty; j < 32; j += 8) {
+    const int b = tb * 32 + j, c = tc * 32 + tx;
+    if (b < n && c < n) tile[j][tx] = src[b * n + c];
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int c = tc * 32 + j, b = tb * 32 + tx;
+    if (b < n && c < n) dst[c * n + b] = tile[tx][j];
   }
 }
 
-// G[cell][k] += sum_q A(k, q) f^(q) f^(k - q) - B(k, q) conj f^(q) f^(k + q)
-// for the output points k of this CTA's tile and the NC cells of its group
-// (sets > 1: one cell per group, the cell's own kernels)
-template <int NC>
-__global__ void __launch_bounds__(nqq::THREADS) k_nyq_quad(const float* A, const float* B, const int* pts, int npts,
-                                                            int n, const float2* fhat, const float2* fhT,
-                                                            const float2* fhn, float2* G, int64_t cells,
-                                                            int64_t set_stride) {
-  using namespace nqq;
-  __shared__ int qs[THREADS];
-  __shared__ float2 fq[NC][THREADS];
-  const int K = blockIdx.x * THREADS + threadIdx.x;
-  const int64_t c0 = int64_t(blockIdx.y) * NC;
-  const bool on = K < npts;
-  const int n2 = n * n, h = n / 2;
+// segment g of an orientation's input points: slice s, kind (0: a row of n
+// points at i1, 1: the column i2 = h without i1 = h), first point index j0
+__device__ __forceinline__ void qq_segment(int g, int n, int& s, int& kind, int& i1, int& j0) {
+  const int h = n >> 1, L = 2 * n - 1;
+  if (g < 2 * h) {
+    s = g >> 1, kind = g & 1, i1 = h, j0 = s * L + kind * n;
+  } else if (g < 2 * h + n) {
+    s = h, kind = 0, i1 = g - 2 * h, j0 = h * L + i1 * n;
+  } else {
+    const int gg = g - 2 * h - n;
+    s = h + 1 + (gg >> 1), kind = gg & 1, i1 = h, j0 = h * L + n * n + (s - h - 1) * L + kind * n;
+  }
+}
+
+struct QuadArgs {
+  const float* A;
+  const float* B;
+  const float2* fhat;
+  const float2* fhT;
+  float2* part;        // [split][cells][3][n][n]
+  int64_t cells;
+  int64_t set_stride;  // floats between consecutive cells' kernels (0: one set for every cell)
+  int n, npts, W, split;
+};
+
+__device__ __forceinline__ void qq_term(float2& acc, float a, float b, float2 f0, float2 gm, float2 gp) {
+  // acc += a f0 gm - b conj(f0) gp
+  const float x1 = fmaf(a, gm.x, -b * gp.x), x2 = fmaf(a, gm.y, b * gp.y);
+  const float x3 = fmaf(a, gm.y, -b * gp.y), x4 = fmaf(a, gm.x, b * gp.x);
+  acc.x = fmaf(f0.x, x1, fmaf(-f0.y, x2, acc.x));
+  acc.y = fmaf(f0.x, x3, fmaf(f0.y, x4, acc.y));
+}
+
+// partial C over one range of one orientation's input points, for R output
+// points per thread and NC cells per CTA (NC = 1 when every cell has its own
+// kernels); grid (n / W, cell groups, 3 x split), n W / R threads
+template <int NC, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
+  constexpr int R = nqq::R;
+  extern __shared__ float2 qsm[];
+  const int n = a.n, h = n >> 1, n2 = n * n, LD = n + 1;
   const int64_t n3 = int64_t(n2) * n;
-  const int code = on ? pts[K] : 0;
-  const int ka = code / n2, kb = (code / n) % n, kc = code % n;
-  // the plane k_c = h (outside k_a = h, k_b = h) runs along k_b: gather from the transposed copy
-  const bool pl2 = kc == h && ka != h && kb != h;
+  const int d = blockIdx.z / a.split, range = blockIdx.z - d * a.split;
+  const int tid = threadIdx.x, rows_step = blockDim.x / n;
+  const int k1 = tid % n, kb = tid / n;
+  const int k20 = blockIdx.x * a.W + kb * R;
+  const int64_t c0 = int64_t(blockIdx.y) * NC;
+  const int per_cell = 2 * n * LD + 2 * n;  // P1 [n][LD], P2 [n][LD], QR [n], QC [n]
   const float2* src[NC];
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
-    const int64_t cell = min(c0 + c, cells - 1);
-    src[c] = (pl2 ? fhT : fhat) + cell * n3;
+    const int64_t cell = min(c0 + c, a.cells - 1);
+    src[c] = (d == 2 ? a.fhT : a.fhat) + cell * n3;
   }
-  const float* Ak = A + (set_stride ? c0 * set_stride : 0) + K;
-  const float* Bk = B + (set_stride ? c0 * set_stride : 0) + K;
-  float2 acc[NC];
+  // plane v of orientation d, element (i1, i2): off(v) + i1 * s1 + i2 (the
+  // plane k_c = v comes from the transposed copy)
+  const int s1 = d == 0 ? n : n2, vstride = d == 0 ? n2 : n;
+  const int64_t kset = a.set_stride ? c0 * a.set_stride : 0;
+  const int64_t kofs = kset + int64_t(d) * a.npts * n2 + (int64_t(k20 / R) * n + k1) * R;
+  const float* Ab = a.A + kofs;
+  const float* Bb = a.B + kofs;
+  float2 acc[NC][R];
 #pragma unroll
-  for (int c = 0; c < NC; ++c) acc[c] = make_float2(0.f, 0.f);
-  for (int j0 = 0; j0 < npts; j0 += THREADS) {
-    // a chunk of the input points and their f^ values into shared memory
-    __syncthreads();
-    const int jj = j0 + threadIdx.x;
-    qs[threadIdx.x] = jj < npts ? pts[jj] : 0;
+  for (int c = 0; c < NC; ++c)
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const int64_t cell = min(c0 + c, cells - 1);
-      fq[c][threadIdx.x] = jj < npts ? fhn[cell * npts + jj] : make_float2(0.f, 0.f);
+    for (int r = 0; r < R; ++r) acc[c][r] = make_float2(0.f, 0.f);
+
+  const int nseg = 3 * n - 2;
+  const int g0 = range * nseg / a.split, g1 = (range + 1) * nseg / a.split;
+  int cur = -1;
+  for (int g = g0; g < g1; ++g) {
+    int s, kind, i1f, j0;
+    qq_segment(g, n, s, kind, i1f, j0);
+    if (s != cur) {  // stage the slice's planes for the group's cells
+      __syncthreads();
+      const int vm = (h - s + n) % n, vp = (n - vm) % n, v2 = s == h ? h : vp;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        float2* P1 = qsm + c * per_cell;
+        float2* P2 = P1 + n * LD;
+        const float2* sm_ = src[c] + int64_t(vm) * vstride;
+        const float2* s2_ = src[c] + int64_t(v2) * vstride;
+        for (int i1 = kb; i1 < n; i1 += rows_step) {
+          cp_async8(P1 + i1 * LD + k1, sm_ + int64_t(i1) * s1 + k1);
+          cp_async8(P2 + i1 * LD + k1, s2_ + int64_t(i1) * s1 + k1);
+        }
+        if (s != h && kb < 2) {  // QR: row h of the plane at s; QC: its column h
+          const float2* ss = src[c] + int64_t(s) * vstride;
+          float2* Q = P2 + n * LD + kb * n;
+          cp_async8(Q + k1, kb == 0 ? ss + int64_t(h) * s1 + k1 : ss + int64_t(k1) * s1 + h);
+        }
+      }
+      cp_async_commit();
+      cp_async_wait_group<0>();
+      __syncthreads();
+      cur = s;
     }
-    __syncthreads();
-    const int jn = min(THREADS, npts - j0);
-    if (on) {
-#pragma unroll 2
-      for (int j = 0; j < jn; ++j) {
-        const int qc = qs[j];
-        const int qa = qc / n2, qb = (qc / n) % n, qq = qc % n;
-        int ma = ka - qa, mb = kb - qb, mc = kc - qq;
-        ma += ma < 0 ? n : 0, mb += mb < 0 ? n : 0, mc += mc < 0 ? n : 0;
-        int pa = ka + qa, pb = kb + qb, pc = kc + qq;
-        pa -= pa >= n ? n : 0, pb -= pb >= n ? n : 0, pc -= pc >= n ? n : 0;
-        const int im = pl2 ? ma * n2 + mc * n + mb : ma * n2 + mb * n + mc;
-        const int ip = pl2 ? pa * n2 + pc * n + pb : pa * n2 + pb * n + pc;
-        const float a = __ldg(Ak + int64_t(j0 + j) * npts), b = __ldg(Bk + int64_t(j0 + j) * npts);
+    if (kind == 0) {  // a row of input points: i1 = i1f, i2 = 0 .. n - 1
+      int rm = k1 - i1f, rp = k1 + i1f;
+      rm += rm < 0 ? n : 0;
+      rp -= rp >= n ? n : 0;
+      const float2* pm[NC];
+      const float2* pp[NC];
+      const float2* qrow[NC];
+      float2 wm[NC][R], wp[NC][R];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const float2* P1 = qsm + c * per_cell;
+        const float2* P2 = P1 + n * LD;
+        pm[c] = P1 + rm * LD;
+        pp[c] = (s == h ? P1 : P2) + rp * LD;
+        qrow[c] = s == h ? P2 + i1f * LD : P2 + n * LD;
+#pragma unroll
+        for (int r = 1; r < R; ++r) wm[c][r] = pm[c][k20 + r];
+#pragma unroll
+        for (int r = 0; r < R - 1; ++r) wp[c][r] = pp[c][k20 + r];
+      }
+      const float* Aj = Ab + int64_t(j0) * n2;
+      const float* Bj = Bb + int64_t(j0) * n2;
+      for (int i20 = 0; i20 < n; i20 += R) {
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+          const int i2 = i20 + t;
+          int um = k20 - i2, up = k20 + R - 1 + i2;
+          um += um < 0 ? n : 0;
+          up -= up >= n ? n : 0;
+          const float4 av = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(i2) * n2));
+          const float4 bv = __ldg(reinterpret_cast<const float4*>(Bj + int64_t(i2) * n2));
+          const float al[R] = {av.x, av.y, av.z, av.w}, be[R] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            wm[c][(R - t) % R] = pm[c][um];
+            wp[c][(R - 1 + t) % R] = pp[c][up];
+            const float2 f0 = qrow[c][i2];
+#pragma unroll
+            for (int r = 0; r < R; ++r) qq_term(acc[c][r], al[r], be[r], f0, wm[c][(r - t + R) % R], wp[c][(r + t) % R]);
+          }
+        }
+      }
+    } else {  // the column i2 = h of slice s != h, i1 over [0, n) without h
+      const int cm = (k20 + h) % n;  // k2 -+ h for the thread's first k2 (no wrap within the R)
+      for (int i1 = 0; i1 < n; ++i1) {
+        if (i1 == h) continue;
+        const int jj = j0 + (i1 < h ? i1 : i1 - 1);
+        int rm = k1 - i1, rp = k1 + i1;
+        rm += rm < 0 ? n : 0;
+        rp -= rp >= n ? n : 0;
+        const float4 av = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(jj) * n2));
+        const float4 bv = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(jj) * n2));
+        const float al[R] = {av.x, av.y, av.z, av.w}, be[R] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-          const float2 f0 = fq[c][j];
-          const float2 gm = __ldg(src[c] + im), gp = __ldg(src[c] + ip);
-          // a f0 gm - b conj(f0) gp
-          const float2 u = make_float2(f0.x * gm.x - f0.y * gm.y, f0.x * gm.y + f0.y * gm.x);
-          const float2 w = make_float2(f0.x * gp.x + f0.y * gp.y, f0.x * gp.y - f0.y * gp.x);
-          acc[c].x += a * u.x - b * w.x;
-          acc[c].y += a * u.y - b * w.y;
+          const float2* P1 = qsm + c * per_cell;
+          const float2* P2 = P1 + n * LD;
+          const float2* gmr = P1 + rm * LD + cm;
+          const float2* gpr = P2 + rp * LD + cm;
+          const float2 f0 = P2[n * LD + n + i1];
+#pragma unroll
+          for (int r = 0; r < R; ++r) qq_term(acc[c][r], al[r], be[r], f0, gmr[r], gpr[r]);
         }
       }
     }
   }
-  if (!on) return;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
-    if (c0 + c >= cells) break;
-    float2* g = G + (c0 + c) * n3 + code;
-    g->x += acc[c].x;
-    g->y += acc[c].y;
+    const int64_t cell = c0 + c;
+    if (cell >= a.cells) break;
+    float2* o = a.part + ((int64_t(range) * a.cells + cell) * 3 + d) * n2 + int64_t(k1) * n + k20;
+#pragma unroll
+    for (int r = 0; r < R; ++r) o[r] = acc[c][r];
   }
+}
+
+// G[cell][k] += the partial sums of every range, for the output points of the
+// three planes (points of an earlier plane skipped)
+__global__ void __launch_bounds__(256) k_quad_add(const float2* part, float2* G, int n, int64_t cells, int split) {
+  const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int n2 = n * n, h = n >> 1;
+  if (gid >= cells * 3 * n2) return;
+  const int64_t cd = gid / n2;  // (cell, d)
+  const int e = int(gid - cd * n2), k1 = e / n, k2 = e - k1 * n;
+  const int d = int(cd % 3);
+  if ((d == 1 && k1 == h) || (d == 2 && (k1 == h || k2 == h))) return;
+  const int64_t cell = cd / 3;
+  float2 sum = make_float2(0.f, 0.f);
+  for (int r = 0; r < split; ++r) {
+    const float2 v = part[(int64_t(r) * cells * 3 + cd) * n2 + e];
+    sum.x += v.x, sum.y += v.y;
+  }
+  const int code = d == 0 ? h * n2 + k1 * n + k2 : d == 1 ? k1 * n2 + h * n + k2 : k1 * n2 + k2 * n + h;
+  float2* g = G + cell * int64_t(n2) * n + code;
+  g->x += sum.x;
+  g->y += sum.y;
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+struct QuadCfg {
+  int nc, W, threads;
+  size_t smem;
+};
+
+static QuadCfg quad_cfg(int n, int nsets) {
+  QuadCfg c{};
+  c.nc = nsets > 1 ? 1 : (n <= 32 ? 4 : 2);
+  c.W = n == 32 || n == 48 ? 16 : n;
+  if (n == 64) c.W = c.nc == 1 ? 16 : 32;  // 256 or 512 threads
+  c.threads = n * c.W / nqq::R;
+  c.smem = size_t(c.nc) * size_t(2 * n * (n + 1) + 2 * n) * sizeof(float2);
+  return c;
+}
+
+template <int NC, int MAXT>
+static int quad_occupancy(const QuadCfg& c, int* per_sm) {
+  PII_CUDA(cudaFuncSetAttribute(k_nyq_quad<NC, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(c.smem)));
+  PII_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_nyq_quad<NC, MAXT>, c.threads, c.smem));
+  return PII_OK;
+}
+
+static int quad_kernel_setup(const QuadCfg& c, int* per_sm) {
+  if (c.nc == 4) return quad_occupancy<4, 256>(c, per_sm);
+  if (c.nc == 2) return quad_occupancy<2, 512>(c, per_sm);
+  return quad_occupancy<1, 256>(c, per_sm);
+}
+
+// input-point ranges per orientation for `cells` cells: about two waves of CTAs
+static int quad_split(const pii_plan* p, const QuadCfg& c, int64_t cells) {
+  const int64_t base = int64_t(p->n / c.W) * ((cells + c.nc - 1) / c.nc) * 3;
+  const int64_t want = (2 * int64_t(p->nq_slots) + base - 1) / base;
+  return int(std::max<int64_t>(1, std::min<int64_t>(want, std::min(nqq::SPLIT_MAX, 3 * p->n - 2))));
+}
+
 static void free_quad(pii_plan* p) {
-  for (void** q : {&p->nq_A, &p->nq_B, &p->nq_pts, &p->nq_fhT, &p->nq_fhq})
+  for (void** q : {&p->nq_A, &p->nq_B, &p->nq_fhT, &p->nq_qpart})
     if (*q) {
       cudaFree(*q);
       *q = nullptr;
@@ -232,6 +394,7 @@ static void free_quad(pii_plan* p) {
   p->bytes -= p->nq_quad_bytes;
   p->nq_quad_bytes = 0;
   p->nq_npts = 0;
+  p->nq_qpart_units = 0;
 }
 
 // (Re)builds A and B for the plan's restitution sets; leaves the plan without
@@ -241,6 +404,7 @@ int nyq_quad_prepare(pii_plan* p) {
   free_quad(p);
   if (p->ap_count <= 0 || p->precision != PII_PREC_FP32 || p->dim != 3) return PII_OK;
   const int n = p->n, h = n / 2, n2 = n * n;
+  if (n % 8 != 0 || n > 64) return PII_OK;  // R | h and the launch shapes below
   std::vector<int> pts;
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < n; ++c) pts.push_back(h * n2 + r * n + c);  // k_a = h
@@ -250,59 +414,106 @@ int nyq_quad_prepare(pii_plan* p) {
   for (int r = 0; r < n; ++r)
     for (int c = 0; c < n; ++c)
       if (r != h && c != h) pts.push_back(r * n2 + c * n + h);  // k_c = h, k_a, k_b != h
-  const int64_t npts = int64_t(pts.size()), sets = p->tab.nsets, QP = p->ap_count;
-  const size_t kern = size_t(npts) * npts * sizeof(float) * 2 * size_t(sets);
-  const size_t fh = size_t(p->batch_max) * (size_t(n2) * n + size_t(npts)) * sizeof(float2);
+  const int npts = int(pts.size());
+  std::vector<int> pidx(size_t(n2) * n, -1);
+  for (int i = 0; i < npts; ++i) pidx[pts[i]] = i;
+  auto code = [&](int d, int v, int i1, int i2) {
+    return d == 0 ? v * n2 + i1 * n + i2 : d == 1 ? i1 * n2 + v * n + i2 : i1 * n2 + i2 * n + v;
+  };
+  // input points of each orientation in slice order, output points in the kernels' layout
+  std::vector<int> qi, ki;
+  for (int d = 0; d < 3; ++d) {
+    for (int s = 0; s < n; ++s) {
+      if (s != h) {
+        for (int i2 = 0; i2 < n; ++i2) qi.push_back(pidx[code(d, s, h, i2)]);
+        for (int i1 = 0; i1 < n; ++i1)
+          if (i1 != h) qi.push_back(pidx[code(d, s, i1, h)]);
+      } else {
+        for (int i1 = 0; i1 < n; ++i1)
+          for (int i2 = 0; i2 < n; ++i2) qi.push_back(pidx[code(d, h, i1, i2)]);
+      }
+    }
+    for (int kbg = 0; kbg < n / R; ++kbg)
+      for (int k1 = 0; k1 < n; ++k1)
+        for (int r = 0; r < R; ++r) {
+          const int k2 = kbg * R + r;
+          const bool skip = (d == 1 && k1 == h) || (d == 2 && (k1 == h || k2 == h));
+          ki.push_back(skip ? -1 : pidx[code(d, h, k1, k2)]);
+        }
+  }
+  for (int v : qi)
+    if (v < 0) {
+      set_error("nyq_quad_prepare: internal error in the input-point order");
+      return PII_ERR_ARG;
+    }
+  const int64_t sets = p->tab.nsets, QP = p->ap_count;
+  const QuadCfg cfg = quad_cfg(n, int(sets));
+  int per_sm = 0, sms = 0;
+  PII_TRY(quad_kernel_setup(cfg, &per_sm));
+  PII_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  if (per_sm < 1) return PII_OK;  // the launch shape does not fit: the direct kernels stay in use
+  p->nq_slots = per_sm * sms;
+  int64_t units = 0;  // (range, cell) units of the partial sums at the largest use
+  for (int64_t c = 1; c <= p->batch_max; ++c) units = std::max(units, int64_t(quad_split(p, cfg, c)) * c);
+  const size_t kern = size_t(sets) * 3 * size_t(npts) * n2 * sizeof(float);  // each of A, B
+  const size_t fhT = size_t(p->batch_max) * size_t(n2) * n * sizeof(float2);
+  const size_t part = size_t(units) * 3 * n2 * sizeof(float2);
   size_t free_b = 0, total_b = 0;
   PII_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const size_t budget = std::min<size_t>(size_t(16) << 30, free_b / 4);
-  if (kern + fh > budget) return PII_OK;  // the direct kernels stay in use
+  if (2 * kern + fhT + part > budget) return PII_OK;  // the direct kernels stay in use
   float *T = nullptr, *Al = nullptr, *Be = nullptr;
+  int *dpts = nullptr, *dqi = nullptr, *dki = nullptr;
   const size_t coef = size_t(QP) * npts * sizeof(float);
   int st = PII_OK;
-  auto al = [&](void** d, size_t b) {
-    if (st == PII_OK && cudaMalloc(d, b) != cudaSuccess) {
+  auto al = [&](void** dst, size_t b) {
+    if (st == PII_OK && cudaMalloc(dst, b) != cudaSuccess) {
       set_error("nyq_quad_prepare: out of memory");
       st = PII_ERR_CUDA;
     }
   };
-  al(&p->nq_pts, pts.size() * sizeof(int));
-  al(&p->nq_A, kern / 2);
-  al(&p->nq_B, kern / 2);
-  al(&p->nq_fhT, size_t(p->batch_max) * n2 * n * sizeof(float2));
-  al(&p->nq_fhq, size_t(p->batch_max) * npts * sizeof(float2));
+  al(&p->nq_A, kern);
+  al(&p->nq_B, kern);
+  al(&p->nq_fhT, fhT);
+  al(&p->nq_qpart, part);
   al((void**)&T, coef);
   al((void**)&Al, coef * sets);
   al((void**)&Be, coef * sets);
+  al((void**)&dpts, pts.size() * sizeof(int));
+  al((void**)&dqi, qi.size() * sizeof(int));
+  al((void**)&dki, ki.size() * sizeof(int));
   if (st == PII_OK) {
-    PII_CUDA(cudaMemcpy(p->nq_pts, pts.data(), pts.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(dpts, pts.data(), pts.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(dqi, qi.data(), qi.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(dki, ki.data(), ki.size() * sizeof(int), cudaMemcpyHostToDevice));
     const int64_t work = QP * npts * (sets + 1);
     k_quad_coef<<<unsigned((work + 255) / 256), 256>>>(
-        static_cast<const int*>(p->nq_pts), int(npts), n, p->ap_reps, int(QP), p->ns, p->tab.M,
-        static_cast<const float2*>(p->tab.ephase), static_cast<const float2*>(p->tab.gphase),
-        static_cast<const float*>(p->tab.gsinc), p->tab.gph_stride, p->tab.gs_stride, int(sets), T, Al, Be);
-    const dim3 grid(unsigned((npts + TM - 1) / TM), unsigned((npts + TM - 1) / TM));
-    for (int64_t s = 0; s < sets; ++s) {
-      k_quad_gemm<<<grid, 256>>>(T, Al + s * QP * npts, static_cast<float*>(p->nq_A) + s * npts * npts, int(npts),
-                                 int(QP));
-      k_quad_gemm<<<grid, 256>>>(T, Be + s * QP * npts, static_cast<float*>(p->nq_B) + s * npts * npts, int(npts),
-                                 int(QP));
-    }
+        dpts, npts, n, p->ap_reps, int(QP), p->ns, p->tab.M, static_cast<const float2*>(p->tab.ephase),
+        static_cast<const float2*>(p->tab.gphase), static_cast<const float*>(p->tab.gsinc), p->tab.gph_stride,
+        p->tab.gs_stride, int(sets), T, Al, Be);
+    const dim3 grid(unsigned((n2 + TM - 1) / TM), unsigned((npts + TM - 1) / TM));
+    for (int64_t s = 0; s < sets; ++s)
+      for (int d = 0; d < 3; ++d) {
+        const int64_t o = (s * 3 + d) * int64_t(npts) * n2;
+        k_quad_gemm<<<grid, 256>>>(T, Al + s * QP * npts, dqi + d * npts, dki + d * n2,
+                                   static_cast<float*>(p->nq_A) + o, npts, n2, int(QP), npts);
+        k_quad_gemm<<<grid, 256>>>(T, Be + s * QP * npts, dqi + d * npts, dki + d * n2,
+                                   static_cast<float*>(p->nq_B) + o, npts, n2, int(QP), npts);
+      }
     const cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
       set_error("nyq_quad_prepare: %s", cudaGetErrorString(e));
       st = PII_ERR_CUDA;
     }
   }
-  cudaFree(T);
-  cudaFree(Al);
-  cudaFree(Be);
+  for (void* q : {(void*)T, (void*)Al, (void*)Be, (void*)dpts, (void*)dqi, (void*)dki}) cudaFree(q);
   if (st != PII_OK) {
     free_quad(p);
     return st;
   }
-  p->nq_npts = int(npts);
-  p->nq_quad_bytes = int64_t(kern + fh + pts.size() * sizeof(int));
+  p->nq_npts = npts;
+  p->nq_qpart_units = units;
+  p->nq_quad_bytes = int64_t(2 * kern + fhT + part);
   p->bytes += p->nq_quad_bytes;
   return PII_OK;
 }
@@ -315,35 +526,37 @@ int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s) {
     set_error("nyq_quad_run: the plan has no quadratic-form kernels");
     return PII_ERR_ARG;
   }
-  const int n = p->n, npts = p->nq_npts;
+  const int n = p->n, n2 = n * n;
+  const QuadCfg cfg = quad_cfg(n, int(p->tab.nsets));
+  int split = quad_split(p, cfg, cells);
+  split = int(std::min<int64_t>(split, p->nq_qpart_units / std::max<int64_t>(cells, 1)));
+  if (split < 1) {
+    set_error("nyq_quad_run: %lld cells exceed the partial-sum buffer", (long long)cells);
+    return PII_ERR_SIZE;
+  }
+  QuadArgs a{};
+  a.A = static_cast<const float*>(p->nq_A);
+  a.B = static_cast<const float*>(p->nq_B);
+  a.fhat = static_cast<const float2*>(p->fhat);
+  a.fhT = static_cast<const float2*>(p->nq_fhT);
+  a.part = static_cast<float2*>(p->nq_qpart);
+  a.cells = cells;
+  a.set_stride = p->tab.nsets > 1 ? int64_t(3) * p->nq_npts * n2 : 0;
+  a.n = n, a.npts = p->nq_npts, a.W = cfg.W, a.split = split;
+  StageTimer st(p, ST_NYQ, s);
   const int tb = (n + 31) / 32;
-  {
-    StageTimer st(p, ST_NYQ, s);
-    const int64_t tiles = cells * n * tb * tb, pb = (cells * npts + 255) / 256;
-    k_quad_prep<<<unsigned(tiles + pb), 256, 0, s>>>(static_cast<const float2*>(p->fhat),
-                                                      static_cast<float2*>(p->nq_fhq),
-                                                      static_cast<float2*>(p->nq_fhT),
-                                                      static_cast<const int*>(p->nq_pts), npts, n, cells);
-  }
+  k_quad_prep<<<unsigned(cells * n * tb * tb), 256, 0, s>>>(a.fhat, static_cast<float2*>(p->nq_fhT), n, cells);
   PII_CHECK_LAUNCH();
-  const unsigned kt = unsigned((npts + THREADS - 1) / THREADS);
-  const float* A = static_cast<const float*>(p->nq_A);
-  const float* B = static_cast<const float*>(p->nq_B);
-  const int* pts = static_cast<const int*>(p->nq_pts);
-  const float2* fh = static_cast<const float2*>(p->fhat);
-  const float2* fhT = static_cast<const float2*>(p->nq_fhT);
-  const float2* fhq = static_cast<const float2*>(p->nq_fhq);
-  float2* G = static_cast<float2*>(p->G);
-  {
-    StageTimer st(p, ST_NYQ, s);
-    if (p->tab.nsets > 1) {  // every cell its own kernels
-      const int64_t stride = int64_t(npts) * npts;
-      k_nyq_quad<1><<<dim3(kt, unsigned(cells)), THREADS, 0, s>>>(A, B, pts, npts, n, fh, fhT, fhq, G, cells, stride);
-    } else {
-      k_nyq_quad<GMAX><<<dim3(kt, unsigned((cells + GMAX - 1) / GMAX)), THREADS, 0, s>>>(A, B, pts, npts, n, fh, fhT,
-                                                                                       fhq, G, cells, 0);
-    }
-  }
+  const dim3 grid(unsigned(n / cfg.W), unsigned((cells + cfg.nc - 1) / cfg.nc), unsigned(3 * split));
+  if (cfg.nc == 4)
+    k_nyq_quad<4, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+  else if (cfg.nc == 2)
+    k_nyq_quad<2, 512><<<grid, cfg.threads, cfg.smem, s>>>(a);
+  else
+    k_nyq_quad<1, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+  PII_CHECK_LAUNCH();
+  const int64_t tot = cells * 3 * n2;
+  k_quad_add<<<unsigned((tot + 255) / 256), 256, 0, s>>>(a.part, static_cast<float2*>(p->G), n, cells, split);
   PII_CHECK_LAUNCH();
   return PII_OK;
 }

@@ -26,6 +26,11 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+// the same for 8 bytes (both addresses 8-byte aligned)
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 // the same for one 4-byte word (both addresses 4-byte aligned)
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
@@ -200,15 +205,17 @@ struct pii_plan {
   int ap_count = 0;
   void* nq_part = nullptr;   // Nyquist-correction accumulators [CTAs][3][n^2]
   int64_t nq_ctas = 0;       // their capacity in CTAs (the general kernel, n != 32)
-  // quadratic-form Nyquist correction (nyq_quad.cu): kernels A, B [sets][Nq][Nq]
-  // ([q][k]), the Nyquist points, f^ transposed within each a-plane and f^ at
-  // the points; nyq_path 0 uses it where built, 1 the direct kernels
+  // quadratic-form Nyquist correction (nyq_quad.cu): kernels A, B
+  // [sets][3 output planes][Nq input points][n^2 output points], f^ transposed
+  // within each a-plane, the partial sums of the input-point ranges;
+  // nyq_path 0 uses it where built, 1 the direct kernels
   void* nq_A = nullptr;
   void* nq_B = nullptr;
-  void* nq_pts = nullptr;
   void* nq_fhT = nullptr;
-  void* nq_fhq = nullptr;
+  void* nq_qpart = nullptr;
+  int64_t nq_qpart_units = 0;  // capacity of nq_qpart in (range, cell) units of 3 n^2 points
   int nq_npts = 0;
+  int nq_slots = 0;            // resident CTAs of the correction kernel on the device
   int64_t nq_quad_bytes = 0;
   int nyq_path = 0;
   void* nq_ft2 = nullptr;    // general kernel: f transposed within each a-plane [batch_max][n^3] (FP32)

@@ -349,7 +349,7 @@ static void free_plan(pii_plan* p) {
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
                   p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag,
                   p->dft_img,    p->dft_gs,     p->dft_colb,  p->nq_ft2,    p->nq_fhn,
-                  p->nq_A,       p->nq_B,       p->nq_pts,    p->nq_fhT,    p->nq_fhq};
+                  p->nq_A,       p->nq_B,       p->nq_fhT,    p->nq_qpart};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (p->dft_err_host) cudaFreeHost(p->dft_err_host);
@@ -451,11 +451,11 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
     }
     p->gain_path = 3;
   }
-  // the Nyquist correction: the quadratic form by default for n = 64 (measured
-  // faster there, 17.1 vs 22.2 ms on 16 cells; at n <= 48 the direct kernels
-  // win), built on request for other n (pii_plan_set_nyquist_path)
+  // the Nyquist correction: the quadratic form wherever its kernels fit the
+  // memory budget (3.4x to 9x faster than the direct kernels), else the direct
+  // kernels
   p->nyq_path = 1;
-  if (precision == PII_PREC_FP32 && dim == 3 && p->ap_count > 0 && n >= 64) {
+  if (precision == PII_PREC_FP32 && dim == 3 && p->ap_count > 0) {
     if ((s2 = nyq_quad_prepare(p)) != PII_OK) {
       free_plan(p);
       return s2;

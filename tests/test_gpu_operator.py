@@ -198,20 +198,20 @@ def test_fused_kernel_matches_pipeline_and_fp64(cells, path):
             assert rel_linf(qc[c].cpu().numpy(), qp[c].cpu().numpy()) < 1e-5, (wl, c)
 
 
-@pytest.mark.parametrize("path", ["cluster", "parity", "packed", "packed-quadratic"])
+@pytest.mark.parametrize("path", ["cluster", "parity", "packed", "packed-direct"])
 def test_fused_kernel_rough_input(path):
     """Uniform random f (spectrum up to the Nyquist planes, where exp_rs f^ is
     not Hermitian): fused kernels against the FP64 path, with and without loss,
     with heat bath, and with pair ranges of every length; the packed kernel
-    with both Nyquist corrections (the direct kernel, the default at n = 32,
-    and the quadratic form)."""
+    with both Nyquist corrections (the quadratic form, the default, and the
+    direct kernel)."""
     pkg = _pkg()
     cfg = op_config(32, L8_S, 3, 12, 0.5, 0.8, 1.0)
     sm = pkg.SpectralMesh(cfg)
     f = torch.as_tensor(np.random.default_rng(11).random((5, 32, 32, 32)), device="cuda:0")
     fused = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=5, gain_path=path.split("-")[0])
-    if path == "packed-quadratic":
-        fused.plan.set_nyquist_path("quadratic")
+    if path == "packed-direct":
+        fused.plan.set_nyquist_path("direct")
     dbl = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=5)
     for wl in (False, True):
         qf, qd = fused.collide(f, with_loss=wl), dbl.collide(f, with_loss=wl)

@@ -34,9 +34,8 @@ def test_packed_pipeline_matches_oracle(n, nr, ns, nyq):
     f = np.stack([smooth, rough])
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=2)
     assert col.plan.tuning["gain_path"] == "packed"  # the default where the design is antipodally symmetric
-    # the default correction: the quadratic form at n = 64, the direct kernels otherwise
-    assert col.plan.nyquist_path == ("quadratic" if n == 64 else "direct")
-    col.plan.set_nyquist_path(nyq)  # the other one is built on request
+    assert col.plan.nyquist_path == "quadratic"  # the default correction where its kernels fit
+    col.plan.set_nyquist_path(nyq)
     assert col.plan.nyquist_path == nyq
     ft = torch.as_tensor(f, device="cuda:0")
     qp = col.collide(ft, with_loss=True).cpu().numpy()
@@ -73,3 +72,28 @@ def test_packed_pipeline_per_cell_restitution_and_chunks(nyq):
     for c, (e, e0) in enumerate(sets):
         ref = fo.FSInelasticVHS(mesh, e, e0, 1.0).collide_cell(f[c], with_loss=True)
         assert rel_linf(q[c], ref) < TOL, c
+
+
+@pytest.mark.parametrize("n,nr,cells", [(32, 32, 37), (48, 6, 9)])
+def test_quadratic_correction_many_cells(n, nr, cells):
+    """Cell counts that split into several groups (the last one partial) and
+    several input-point ranges: both Nyquist corrections against the FP64 plan."""
+    import proj_int_inelastic_gb300 as pkg
+
+    cfg = op_config(n, L8_S, nr, 32, 0.8, 0.8, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    v = sm.v_center
+    rng = np.random.default_rng(cells)
+    f = np.stack([maxwellian(v, 1.0, tuple(rng.uniform(-1, 1, 3)), rng.uniform(0.6, 1.4)) *
+                  (1 + 0.05 * rng.random((n, n, n))) for _ in range(cells)])
+    ft = torch.as_tensor(f, device="cuda:0")
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=cells)
+    ref = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=cells).collide(ft, with_loss=True)
+    ref = ref.cpu().numpy()
+    out = {}
+    for nyq in ("direct", "quadratic"):
+        col.plan.set_nyquist_path(nyq)
+        out[nyq] = col.collide(ft, with_loss=True).cpu().numpy()
+        for c in range(cells):
+            assert rel_linf(out[nyq][c], ref[c]) < TOL, (nyq, c)
+    assert rel_linf(out["quadratic"], out["direct"]) < 2e-6
