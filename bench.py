@@ -235,13 +235,17 @@ def measure_n64(pkg, device, cells=256, cells_fp64=2):
     out = {"config": f"n_v={N64}^3 on [-10,10]^3, {NR64} GL radial x {NS64}-point symmetric design, "
                      f"hard spheres, e=e0={E64}, 3-Maxwellian mixtures", "cells": cells,
            "mixed": mixed, "unit": UNIT, "tuning": col.plan.tuning}
-    # the two first-axis column paths side by side (32 cells each): in-register
-    # CUDA-core FFT and the tensor-core split-FP16 DFT
+    # the gain paths side by side (32 cells each): the fused cluster kernel, and
+    # the packed pipeline with both first-axis column paths (in-register
+    # CUDA-core FFT, tensor-core split-FP16 DFT)
     tuned = col.plan.tuning
     paths, q_path = {}, {}
     nc = min(cells, 32)
-    for path in ("fft", "tensor"):
-        col.plan.set_dft_path(path)
+    for path in ("fused", "fft", "tensor"):
+        if path == "fused":
+            col.plan.set_tuning("fused", tuned["items_per_cluster"], tuned["chunk_points"])
+        else:
+            col.plan.set_tuning("packed", tuned["items_per_cluster"], tuned["chunk_points"], dft_path=path)
         col.collide(f[:nc], with_loss=True)
         torch.cuda.synchronize()
         a.record()
@@ -251,7 +255,7 @@ def measure_n64(pkg, device, cells=256, cells_fp64=2):
         paths[path] = nc / (a.elapsed_time(b) / 1e3)
         q_path[path] = col.collide(f[:cells_fp64], with_loss=True).clone()
     out["dft_paths"] = {"cells": nc, "unit": UNIT, **paths, "tensor_core_stalled": col.plan.dft_stalled}
-    col.plan.set_dft_path(tuned["dft_path"])
+    col.plan.set_tuning(**tuned)
     try:
         op = TorchFP64Operator(sm, device, e=E64, gamma=1.0)
         fc = f[:cells_fp64].to(torch.complex128)
@@ -592,6 +596,28 @@ def ncu_case64(cells, dft_path):
     return 0
 
 
+def ncu_case_class(n, cells):
+    """Small profiling case of one ensemble size class (n^3 on [-8, 8]^3,
+    n / 2 GL radial x 32-point design, e = e0 = 0.7, mixture states): two
+    mixed-precision Q(f,f) evaluations with the plan's default kernels."""
+    import torch
+
+    import proj_int_inelastic_gb300 as pkg
+
+    cfg = {"velocity-mesh": {"nv": n, "s": S_L8, "nr": n // 2},
+           "spherical-design-rule": {"ssrule": "womersley", "nsphr": 32},
+           "collision-model": {"dim": 3, "type": "vhs", "e": 0.7, "e0": 0.7, "gamma": 1.0}}
+    sm = pkg.SpectralMesh(cfg)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=cells)
+    f = torch.as_tensor(mixture_states(sm.v_center, cells, 64), device="cuda:0").contiguous()
+    for _ in range(2):
+        q = col.collide(f, with_loss=True)
+    torch.cuda.synchronize()
+    print(json.dumps({"ncu_case_class": n, "cells": cells, "q_abs_max": float(q.abs().max()),
+                      "tuning": col.plan.tuning}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -613,6 +639,9 @@ def main():
     ap.add_argument("--c3-only", action="store_true", help="measure only the ensemble configuration and exit")
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: run 3 Q(f,f) evaluations on this many cells of the workload and exit")
+    ap.add_argument("--ncu-class", type=int, default=0,
+                    help="profiling case: one ensemble size class n^3 (with --ncu-cells cells) and exit")
+    ap.add_argument("--ncu-cells", type=int, default=4)
     ap.add_argument("--ncu-case64", type=int, default=0,
                     help="profiling case: one 64^3 Q(f,f) evaluation on this many cells and exit")
     ap.add_argument("--dft-path", default="tensor", choices=["tensor", "fft"],
@@ -622,6 +651,8 @@ def main():
         return run_reference(args)
     if args.ncu_case:
         return ncu_case(args.ncu_case)
+    if args.ncu_class:
+        return ncu_case_class(args.ncu_class, args.ncu_cells)
     if args.ncu_case64:
         return ncu_case64(args.ncu_case64, args.dft_path)
     if args.c4_only or args.c3_only:

@@ -109,13 +109,18 @@ int pii_plan_destroy(pii_plan* plan);
 int64_t pii_plan_workspace_bytes(const pii_plan* plan);
 
 /*
- * Kernel choice for the gain term of n = 32 FP32 plans (tuning knob, no
- * reference counterpart): 3 = the fused a-parity kernel on antipodal direction
+ * Kernel choice for the gain term of FP32 3D plans (tuning knob, no reference
+ * counterpart).  n = 32: 3 = the fused a-parity kernel on antipodal direction
  * pairs (sigma, -sigma packed into one real-phase pass) plus the exact
  * Nyquist-plane correction (the default where the design is antipodally
  * symmetric), 2 = the fused a-parity kernel with its accumulator in tensor
- * memory, 1 = the fused 2-CTA-cluster kernel, 0 = the column / plane pass
- * pipeline used for every other size and for FP64.  All compute the same operator.
+ * memory, 1 = the fused 2-CTA-cluster kernel.  n = 16, 24, 48, 64: 4 = the
+ * fused kernel (one work item per CTA, or per cluster of 8 / 16 CTAs at
+ * n = 48 / 64, exchanging through distributed shared memory, the gain sum in
+ * tensor memory; packed with the Nyquist correction where the design is
+ * antipodally symmetric; the default at n = 16, 24, 48), 3 = the packed
+ * column / plane pipeline.  0 = the column / plane pipeline on (cell, pair)
+ * items, every size and FP64.  All compute the same operator.
  */
 int pii_plan_set_gain_path(pii_plan* plan, int path);
 
@@ -311,9 +316,10 @@ int pii_collide_noalloc(const double* f, double* q, int64_t cells, int n, int n_
  * pii_plan_profile_read fills ms[PII_NSTAGES] (summed device time) and
  * launches[PII_NSTAGES] after synchronising, and resets the counters.
  */
-#define PII_NSTAGES 14
+#define PII_NSTAGES 15
 /* stage order: fwd_plane, col_fwd, col_pstart, pair_plane, col_pend, reduce,
- * col_iprep, finish, df, axpy, massfix, gain_cluster, gain_parity, nyq_corr */
+ * col_iprep, finish, df, axpy, massfix, gain_cluster, gain_parity, nyq_corr,
+ * gain_fused */
 int64_t pii_kernel_launches(void);
 /* instantiated macro-step graphs held by the plan (at most 8: pii_step and
  * pii_step_splitting evict the least recently replayed one) */

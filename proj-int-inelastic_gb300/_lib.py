@@ -75,9 +75,9 @@ SIGNATURES = {
     "pii_plan_profile_read": (_c_int, [_vp, _pdbl, ctypes.POINTER(ctypes.c_int64)]),
 }
 
-NSTAGES = 14
+NSTAGES = 15
 STAGES = ["fwd_plane", "col_fwd", "col_pstart", "pair_plane", "col_pend", "reduce", "col_iprep", "finish", "df",
-          "axpy", "massfix", "gain_cluster", "gain_parity", "nyq_corr"]
+          "axpy", "massfix", "gain_cluster", "gain_parity", "nyq_corr", "gain_fused"]
 
 _lib = None
 

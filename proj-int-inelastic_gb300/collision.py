@@ -207,7 +207,7 @@ def _precision_of(config, precision):
     raise ValueError(f"precision must be 'mixed'/'fp32' or 'double'/'fp64', got {precision!r}")
 
 
-GAIN_PATHS = {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3}
+GAIN_PATHS = {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3, "fused": 4}
 # first-axis column transforms of the n = 64 FP32 pipeline
 DFT_PATHS = {"fft": 0, "tensor": 1}
 

@@ -38,6 +38,13 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
   }
+  if constexpr (std::is_same<T, float>::value && NV != 32) {
+    if (p->gain_path == 4) {  // the fused kernel: every item on chip, packed where the design allows
+      PII_TRY(gain_fused_run(p, cells, s));
+      if (p->ap_count > 0) PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_gen_run(p, cells, s));
+      return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
+    }
+  }
   // items = (cell, pair), or (cell, antipodal pass) on the packed pipeline; a
   // chunk holds Cc cells x Pc of them in the L2-resident buffer
   bool packed = false;
@@ -192,6 +199,7 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
       for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
         cands.push_back({path, plan->gc_items_per_cluster, pts, dft});
   }
+  if (plan->fz_clusters > 0) cands.push_back({4, plan->gc_items_per_cluster, plan->chunk_points, 0});
   const int saved_path = plan->gain_path;
   const int saved_items = plan->gc_items_per_cluster;
   const int64_t saved_points = plan->chunk_points;
@@ -261,8 +269,13 @@ extern "C" int pii_plan_set_tuning(pii_plan* plan, int gain_path, int items_per_
 }
 
 extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
-  if (!plan || path < 0 || path > 3) {
-    pii::set_error("pii_plan_set_gain_path: path must be 0 (pipeline), 1 (cluster), 2 (a-parity) or 3 (packed)");
+  if (!plan || path < 0 || path > 4) {
+    pii::set_error(
+        "pii_plan_set_gain_path: path must be 0 (pipeline), 1 (cluster), 2 (a-parity), 3 (packed) or 4 (fused)");
+    return PII_ERR_ARG;
+  }
+  if (path == 4 && plan->fz_clusters <= 0) {
+    pii::set_error("pii_plan_set_gain_path: the fused kernel exists for n = 16, 24, 48, 64, FP32 3D plans only");
     return PII_ERR_ARG;
   }
   if (path == 3 && (plan->ap_count == 0 || !plan->nq_part)) {

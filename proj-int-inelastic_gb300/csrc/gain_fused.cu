@@ -1,0 +1,468 @@
+// Fused gain term of Q(f,f) for the FP32 plans of n in {16, 24, 48, 64}: every
+// (cell, pass) work item stays on chip from the phase product to the gain sum.
+//
+// One work item is the n^3 complex grid of one quadrature pair (or antipodal
+// pass) of one cell (src/collision/inelastic_collisions.py:212-217):
+//   A  X = phase(k) f^(k), inverse transform along a          (column layout)
+//   B  inverse along b, inverse along c, * f, forward along c,
+//      forward along b                                         (plane layout)
+//   C  forward along a, * gain(k), summed over the cell's items (column layout)
+// A cluster of CS CTAs holds the item: CTA r owns the a-planes
+// [r NPL, (r + 1) NPL) in stage B and the columns (b, c) with b in the same
+// range in stages A and C (NPL = n / CS; n = 16, 24: CS = 1, the item fits one
+// CTA; n = 48: CS = 8; n = 64: CS = 16).  Between the layouts each thread
+// stores its line straight into the owning CTA's shared memory
+// (st.shared::cluster): a column's n values go to the n / NPL plane owners,
+// a plane column's n values to the column owners, 256 contiguous bytes per
+// warp store.  Cluster barriers (release / acquire, split arrive / wait)
+// order the exchanges; the arrive that frees a buffer is issued as soon as
+// its last read is done, so the transform that follows hides the wait.
+// The gain sum of the CTA's columns, n k_a values each (n = 64: 64 KB per
+// CTA ... 110 KB at n = 48), lives in tensor memory for all the items of a
+// cell; at the end of a cell's range the CTA writes it to a per-part slot,
+// and k_fused_expand adds the parts of each cell into G.  Antipodally
+// symmetric designs run the packed passes (real phase t, real coefficient
+// 2 s; pack.cuh), followed by the Nyquist correction.
+#include <algorithm>
+
+#include "fft_reg.cuh"
+#include "pack.cuh"
+#include "pii_internal.cuh"
+#include "tmem.cuh"
+
+namespace pii {
+
+namespace gfu {
+template <int NV>
+struct Cfg;
+template <>
+struct Cfg<16> {
+  static constexpr int CS = 1;
+};
+template <>
+struct Cfg<24> {
+  static constexpr int CS = 1;
+};
+template <>
+struct Cfg<48> {
+  static constexpr int CS = 8;
+};
+template <>
+struct Cfg<64> {
+  static constexpr int CS = 16;
+};
+
+template <int NV>
+struct Geo {
+  static constexpr int CS = Cfg<NV>::CS;
+  static constexpr int N2 = NV * NV, N3 = N2 * NV;
+  static constexpr int NPL = NV / CS;    // a-planes of a CTA
+  static constexpr int NCOL = N2 / CS;   // (b, c) columns of a CTA
+  static constexpr int THREADS = NCOL;   // = NPL * NV plane lines
+  static constexpr int LD = NV + 1;      // padded plane row (complex elements)
+  static constexpr int PLANE = NPL * NV * LD;
+  static constexpr int COLS = NV * NCOL;
+  static constexpr int BUF = PLANE > COLS ? PLANE : COLS;
+  static constexpr size_t F_OFF = size_t(BUF) * sizeof(float2);
+  // f of the CTA's planes, rows padded to LD floats (the row pass reads
+  // f[pl][b][c] for one c across lanes of consecutive b)
+  static constexpr size_t SMEM = F_OFF + size_t(NPL) * NV * LD * sizeof(float) + 16;
+  static constexpr int WARPS = THREADS / 32;
+  static constexpr int TCOLS_USED = ((WARPS + 3) / 4) * 2 * NV;
+  static constexpr int TCOLS = TCOLS_USED <= 32    ? 32
+                               : TCOLS_USED <= 64  ? 64
+                               : TCOLS_USED <= 128 ? 128
+                               : TCOLS_USED <= 256 ? 256
+                                                   : 512;
+  static constexpr int CHUNKS = 2 * NV / 16;  // 16-column tensor-memory chunks of a thread's sum
+  static_assert(THREADS % 32 == 0 && NV % CS == 0 && TCOLS_USED <= 512 && (2 * NV) % 16 == 0, "launch shape");
+  static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
+};
+}  // namespace gfu
+
+struct FusedArgs {
+  const float2* fhat;    // [cells][N3] spectra of f
+  const float* fT;       // [cells][N3] f in FP32
+  const float2* ephase;  // [Q][3][n]
+  const float2* gphase;  // [sets][Q][3][n]
+  const float* gsinc;    // [sets][n_r][M + 1]
+  int64_t gph_stride, gs_stride;
+  int M, ns, QP;
+  const int* reps;  // packed: the representative pair of each pass
+  int64_t cells;
+  float2* part;  // [clusters + cells][N3]: the gain sums of each (cluster, cell) segment
+};
+
+__device__ __forceinline__ uint32_t fz_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t fz_map(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void fz_st(uint32_t addr, float2 v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ void fz_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void fz_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+template <int NV, bool PACK>
+__global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedArgs a) {
+  using G = gfu::Geo<NV>;
+  constexpr int CS = G::CS, NPL = G::NPL, NCOL = G::NCOL, LD = G::LD, N2 = G::N2, N3 = G::N3, H = NV / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* buf = reinterpret_cast<float2*>(smem_raw);
+  float* fS = reinterpret_cast<float*>(smem_raw + G::F_OFF);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + G::SMEM - 16);
+  const int t = threadIdx.x, warp = t >> 5;
+  const int rank = CS > 1 ? int(fz_rank()) : 0;
+  const int cl = int(blockIdx.x) / CS, ncl = int(gridDim.x) / CS;
+  if (warp == 0) {
+    tm_alloc(tslot, G::TCOLS);
+    tm_relinquish();
+  }
+  tm_fence_before();
+  __syncthreads();
+  tm_fence_after();
+  const uint32_t tbase = *tslot;
+  const uint32_t treg = tbase + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 2 * NV);
+  // stages A and C: this thread's column (jb, jc), jb in the CTA's rows;
+  // stage B: plane pl = t / NV of the CTA, line l = t mod NV (the same numbers)
+  const int pl = t / NV, l = t - pl * NV;
+  const int jb = rank * NPL + pl, jc = l;
+  const int j = jb * NV + jc;
+  const int kb = kval(jb, NV), kc = kval(jc, NV);
+  const int mbc = kb * kb + kc * kc;
+  const uint32_t buf_s = static_cast<uint32_t>(__cvta_generic_to_shared(buf));
+  // the first wait (before the first exchange) also makes sure that every CTA
+  // of the cluster runs before any shared memory of another is written
+  if constexpr (CS > 1) fz_arrive();
+
+  const int64_t total = a.cells * a.QP;
+  const int64_t w0 = total * cl / ncl, w1 = total * (cl + 1) / ncl;
+  int64_t cur = -1;
+  auto flush = [&](int64_t cell) {  // the segment's sums -> part[cl + cell][a][j]
+    tm_wait_st();
+    float2* out = a.part + (int64_t(cl) + cell) * N3 + j;
+#pragma unroll
+    for (int c = 0; c < G::CHUNKS; ++c) {
+      uint32_t r[16];
+      tm_ld16(treg + 16 * c, r);
+      tm_wait_ld(r);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) out[int64_t(8 * c + i) * N2] = make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
+    }
+  };
+  for (int64_t w = w0; w < w1; ++w) {
+    const int64_t cell = w / a.QP;
+    const int ip = int(w - cell * a.QP);
+    if (cell != cur) {
+      if (cur >= 0) flush(cur);
+      uint32_t z[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) z[i] = 0u;
+#pragma unroll
+      for (int c = 0; c < G::CHUNKS; ++c) tm_st16(treg + 16 * c, z);
+      // f of the CTA's planes (read in stage B after the exchange barrier below)
+      const float* fc = a.fT + cell * N3 + int64_t(rank * NPL) * N2;
+      for (int e = t; e < NPL * N2; e += G::THREADS) {
+        const int p2 = e / N2, rem = e - p2 * N2, b = rem / NV, c = rem - b * NV;
+        fS[(p2 * NV + b) * LD + c] = fc[e];
+      }
+      cur = cell;
+    }
+    const int pair = PACK ? a.reps[ip] : ip;
+    float2 x[NV];
+    // ---- A: phase product and inverse transform along a of the column
+    {
+      const float2* fh = a.fhat + cell * N3 + j;
+      const float2* ep = a.ephase + int64_t(pair) * 3 * NV;
+      if constexpr (PACK) {
+        float cp, cm, th;
+        pack_t_consts<float, float2, NV>(ep, jb, jc, cp, cm, th);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+          const float2 e = ep[q];
+          x[q] = cscale(fh[q * N2], q == H ? th : fmaf(e.y, cm, e.x * cp));
+        }
+      } else {
+        const float2 ebc = cmul(ep[NV + jb], ep[2 * NV + jc]);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = cmul(fh[q * N2], cmul(ep[q], ebc));
+      }
+      fft_line<NV, +1>(x);
+    }
+    if constexpr (CS > 1) {
+      fz_wait();  // every buffer of the cluster has been read by the previous item's stage C
+      static_for<0, CS>([&](auto ri) {
+        constexpr int r = decltype(ri)::value;
+        const uint32_t base = fz_map(buf_s, uint32_t(r));
+        static_for<0, NPL>([&](auto mi) {
+          constexpr int m = decltype(mi)::value;
+          fz_st(base + uint32_t(((m * NV + jb) * LD + jc) * 8), x[pos(NV, r * NPL + m)]);
+        });
+      });
+      fz_arrive();
+      fz_wait();  // the planes of the CTA are complete
+    } else {
+      __syncthreads();  // the previous item's stage C has read the buffer
+      static_for<0, NV>([&](auto qi) {
+        constexpr int q = decltype(qi)::value;
+        buf[(q * NV + jb) * LD + jc] = x[pos(NV, q)];
+      });
+      __syncthreads();
+    }
+    // ---- B: inverse along b (column (pl, l))
+    {
+      float2* col = buf + pl * NV * LD + l;
+#pragma unroll
+      for (int b = 0; b < NV; ++b) x[b] = col[b * LD];
+      fft_line<NV, +1>(x);
+      static_for<0, NV>([&](auto bi) {
+        constexpr int b = decltype(bi)::value;
+        col[b * LD] = x[pos(NV, b)];
+      });
+    }
+    __syncthreads();
+    // inverse along c, * f, forward along c (row (pl, l))
+    {
+      float2* row = buf + (pl * NV + l) * LD;
+      const float* fr = fS + (pl * NV + l) * LD;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) x[c] = row[c];
+      fft_line<NV, +1>(x);
+      float2 y[NV];
+      static_for<0, NV>([&](auto ci) {
+        constexpr int c = decltype(ci)::value;
+        y[c] = cscale(x[pos(NV, c)], fr[c]);
+      });
+      fft_line<NV, -1>(y);
+      static_for<0, NV>([&](auto ci) {
+        constexpr int c = decltype(ci)::value;
+        row[c] = y[pos(NV, c)];
+      });
+    }
+    __syncthreads();
+    // forward along b (column (pl, l)), then to the column owners
+    {
+      float2* col = buf + pl * NV * LD + l;
+#pragma unroll
+      for (int b = 0; b < NV; ++b) x[b] = col[b * LD];
+      if constexpr (CS > 1) fz_arrive();  // this thread's reads of its planes are done
+      fft_line<NV, -1>(x);
+      if constexpr (CS > 1) {
+        const int ag = rank * NPL + pl;  // the plane's a
+        fz_wait();                       // every CTA has read its planes
+        static_for<0, CS>([&](auto ri) {
+          constexpr int r = decltype(ri)::value;
+          const uint32_t base = fz_map(buf_s, uint32_t(r));
+          static_for<0, NPL>([&](auto mi) {
+            constexpr int m = decltype(mi)::value;
+            fz_st(base + uint32_t((ag * NCOL + m * NV + l) * 8), x[pos(NV, r * NPL + m)]);
+          });
+        });
+        fz_arrive();
+        fz_wait();  // the columns of the CTA are complete
+      } else {
+        static_for<0, NV>([&](auto bi) {
+          constexpr int b = decltype(bi)::value;
+          col[b * LD] = x[pos(NV, b)];
+        });
+        __syncthreads();
+      }
+    }
+    // ---- C: forward along a of the column, * gain, summed in tensor memory
+    {
+      if constexpr (CS > 1) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = buf[q * NCOL + t];
+        fz_arrive();  // read: the next item may overwrite the buffer
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = buf[(q * NV + jb) * LD + jc];
+      }
+      fft_line<NV, -1>(x);
+      const float2* gp = a.gphase + cell * a.gph_stride + int64_t(pair) * 3 * NV;
+      const float* gs = a.gsinc + cell * a.gs_stride + int64_t(pair / a.ns) * (a.M + 1) + mbc;
+      float2 v[NV];
+      if constexpr (PACK) {
+        float dp, dm, sh;
+        pack_s_consts<float, float2, NV>(gp, jb, jc, dp, dm, sh);
+        static_for<0, NV>([&](auto qi) {
+          constexpr int q = decltype(qi)::value;
+          constexpr int kq = kval(q, NV);
+          const float2 g = gp[q];
+          const float sv = q == H ? sh : fmaf(-g.y, dm, g.x * dp);
+          v[q] = cscale(x[pos(NV, q)], 2.f * sv * gs[kq * kq]);
+        });
+      } else {
+        const float2 gbc = cmul(gp[NV + jb], gp[2 * NV + jc]);
+        static_for<0, NV>([&](auto qi) {
+          constexpr int q = decltype(qi)::value;
+          constexpr int kq = kval(q, NV);
+          v[q] = cmul(x[pos(NV, q)], cscale(cmul(gp[q], gbc), gs[kq * kq]));
+        });
+      }
+      tm_wait_st();
+      static_for<0, G::CHUNKS>([&](auto ci) {
+        constexpr int c = decltype(ci)::value;
+        uint32_t r[16];
+        tm_ld16(treg + 16 * c, r);
+        tm_wait_ld(r);
+        static_for<0, 8>([&](auto ii) {
+          constexpr int i = decltype(ii)::value;
+          r[2 * i] = __float_as_uint(__uint_as_float(r[2 * i]) + v[8 * c + i].x);
+          r[2 * i + 1] = __float_as_uint(__uint_as_float(r[2 * i + 1]) + v[8 * c + i].y);
+        });
+        tm_st16(treg + 16 * c, r);
+      });
+    }
+  }
+  if (cur >= 0) flush(cur);
+  if constexpr (CS > 1) fz_wait();  // matches the last arrive; no CTA leaves while others may still write to it
+  tm_wait_st();
+  tm_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tm_fence_after();
+    tm_dealloc(tbase, G::TCOLS);
+  }
+}
+
+// G[cell] = the sum of the parts of the clusters whose ranges meet the cell
+__global__ void __launch_bounds__(256) k_fused_expand(float2* G, const float2* part, int64_t cells, int QP, int ncl,
+                                                      int64_t N3) {
+  const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= cells * N3) return;
+  const int64_t cell = gid / N3, e = gid - cell * N3;
+  const int64_t total = cells * QP, lo = cell * QP, hi = lo + QP;
+  float2 s = make_float2(0.f, 0.f);
+  for (int64_t c = lo * ncl / total; c < ncl; ++c) {
+    const int64_t r0 = total * c / ncl, r1 = total * (c + 1) / ncl;
+    if (r0 >= hi) break;
+    if (r1 <= lo) continue;
+    const float2 v = part[(c + cell) * N3 + e];
+    s.x += v.x, s.y += v.y;
+  }
+  G[gid] = s;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <int NV, bool PACK>
+static int fused_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, int clusters, cudaStream_t s) {
+  using G = gfu::Geo<NV>;
+  cfg = {};
+  cfg.gridDim = dim3(unsigned(clusters * G::CS), 1, 1);
+  cfg.blockDim = dim3(G::THREADS, 1, 1);
+  cfg.dynamicSmemBytes = G::SMEM;
+  cfg.stream = s;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G::CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return PII_OK;
+}
+
+template <int NV, bool PACK>
+static int fused_setup(int* clusters) {
+  using G = gfu::Geo<NV>;
+  PII_CUDA(cudaFuncSetAttribute(k_gain_fused<NV, PACK>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(G::SMEM)));
+  if (G::CS > 8) PII_CUDA(cudaFuncSetAttribute(k_gain_fused<NV, PACK>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute attr[1];
+  fused_config<NV, PACK>(cfg, attr, 1, nullptr);
+  PII_CUDA(cudaOccupancyMaxActiveClusters(clusters, k_gain_fused<NV, PACK>, &cfg));
+  return PII_OK;
+}
+
+template <int NV>
+static int fused_prepare_t(pii_plan* p) {
+  int c1 = 0, c2 = 0;
+  PII_TRY((fused_setup<NV, true>(&c1)));
+  PII_TRY((fused_setup<NV, false>(&c2)));
+  const int clusters = std::min(c1, c2);
+  if (clusters < 1) return PII_OK;  // no cluster of this shape fits: the pipeline stays in use
+  const size_t bytes = size_t(clusters + p->batch_max) * size_t(gfu::Geo<NV>::N3) * sizeof(float2);
+  PII_CUDA(cudaMalloc(&p->fz_part, bytes));
+  p->bytes += int64_t(bytes);
+  p->fz_clusters = clusters;
+  return PII_OK;
+}
+
+int gain_fused_prepare(pii_plan* p) {
+  if (p->precision != PII_PREC_FP32 || p->dim != 3) return PII_OK;
+  switch (p->n) {
+    case 16: return fused_prepare_t<16>(p);
+    case 24: return fused_prepare_t<24>(p);
+    case 48: return fused_prepare_t<48>(p);
+    case 64: return fused_prepare_t<64>(p);
+    default: return PII_OK;
+  }
+}
+
+template <int NV>
+static int fused_run_t(pii_plan* p, int64_t cells, cudaStream_t s) {
+  using G = gfu::Geo<NV>;
+  const bool packed = p->ap_count > 0;
+  FusedArgs a{};
+  a.fhat = static_cast<const float2*>(p->fhat);
+  a.fT = static_cast<const float*>(p->fT);
+  a.ephase = static_cast<const float2*>(p->tab.ephase);
+  a.gphase = static_cast<const float2*>(p->tab.gphase);
+  a.gsinc = static_cast<const float*>(p->tab.gsinc);
+  a.gph_stride = p->tab.gph_stride;
+  a.gs_stride = p->tab.gs_stride;
+  a.M = p->tab.M;
+  a.ns = p->ns;
+  a.QP = packed ? p->ap_count : p->Q;
+  a.reps = p->ap_reps;
+  a.cells = cells;
+  a.part = static_cast<float2*>(p->fz_part);
+  const int clusters = int(std::min<int64_t>(p->fz_clusters, cells * a.QP));
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute attr[1];
+  {
+    StageTimer st(p, ST_GAIN_FUSED, s);
+    cudaError_t e;
+    if (packed) {
+      fused_config<NV, true>(cfg, attr, clusters, s);
+      e = cudaLaunchKernelEx(&cfg, k_gain_fused<NV, true>, a);
+    } else {
+      fused_config<NV, false>(cfg, attr, clusters, s);
+      e = cudaLaunchKernelEx(&cfg, k_gain_fused<NV, false>, a);
+    }
+    if (e != cudaSuccess) {
+      set_error("k_gain_fused launch: %s", cudaGetErrorString(e));
+      return PII_ERR_CUDA;
+    }
+    k_fused_expand<<<unsigned((cells * G::N3 + 255) / 256), 256, 0, s>>>(static_cast<float2*>(p->G), a.part, cells,
+                                                                        a.QP, clusters, G::N3);
+  }
+  PII_CHECK_LAUNCH();
+  return PII_OK;
+}
+
+int gain_fused_run(pii_plan* p, int64_t cells, cudaStream_t s) {
+  if (!p->fz_part || p->fz_clusters < 1) {
+    set_error("gain_fused_run: the plan has no fused gain kernel");
+    return PII_ERR_ARG;
+  }
+  switch (p->n) {
+    case 16: return fused_run_t<16>(p, cells, s);
+    case 24: return fused_run_t<24>(p, cells, s);
+    case 48: return fused_run_t<48>(p, cells, s);
+    case 64: return fused_run_t<64>(p, cells, s);
+    default:
+      set_error("gain_fused_run: no fused gain kernel for n = %d", p->n);
+      return PII_ERR_ARG;
+  }
+}
+
+}  // namespace pii

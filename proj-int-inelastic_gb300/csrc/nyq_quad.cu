@@ -271,15 +271,30 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
       }
       const float* Aj = Ab + int64_t(j0) * n2;
       const float* Bj = Bb + int64_t(j0) * n2;
+      float4 an[R], bn[R];  // the kernels of the next R input points, loaded one block ahead
+#pragma unroll
+      for (int t = 0; t < R; ++t) {
+        an[t] = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(t) * n2));
+        bn[t] = __ldg(reinterpret_cast<const float4*>(Bj + int64_t(t) * n2));
+      }
       for (int i20 = 0; i20 < n; i20 += R) {
+        float4 ac[R], bc[R];
+#pragma unroll
+        for (int t = 0; t < R; ++t) ac[t] = an[t], bc[t] = bn[t];
+        if (i20 + R < n) {
+#pragma unroll
+          for (int t = 0; t < R; ++t) {
+            an[t] = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(i20 + R + t) * n2));
+            bn[t] = __ldg(reinterpret_cast<const float4*>(Bj + int64_t(i20 + R + t) * n2));
+          }
+        }
 #pragma unroll
         for (int t = 0; t < R; ++t) {
           const int i2 = i20 + t;
           int um = k20 - i2, up = k20 + R - 1 + i2;
           um += um < 0 ? n : 0;
           up -= up >= n ? n : 0;
-          const float4 av = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(i2) * n2));
-          const float4 bv = __ldg(reinterpret_cast<const float4*>(Bj + int64_t(i2) * n2));
+          const float4 av = ac[t], bv = bc[t];
           const float al[R] = {av.x, av.y, av.z, av.w}, be[R] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
@@ -293,14 +308,19 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
       }
     } else {  // the column i2 = h of slice s != h, i1 over [0, n) without h
       const int cm = (k20 + h) % n;  // k2 -+ h for the thread's first k2 (no wrap within the R)
-      for (int i1 = 0; i1 < n; ++i1) {
-        if (i1 == h) continue;
-        const int jj = j0 + (i1 < h ? i1 : i1 - 1);
+      // the column's n - 1 input points are consecutive in the kernels: j0 + m, m < n - 1
+      float4 an = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(j0) * n2));
+      float4 bn = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(j0) * n2));
+      for (int m = 0; m < n - 1; ++m) {
+        const int i1 = m < h ? m : m + 1;
         int rm = k1 - i1, rp = k1 + i1;
         rm += rm < 0 ? n : 0;
         rp -= rp >= n ? n : 0;
-        const float4 av = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(jj) * n2));
-        const float4 bv = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(jj) * n2));
+        const float4 av = an, bv = bn;
+        if (m + 1 < n - 1) {
+          an = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(j0 + m + 1) * n2));
+          bn = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(j0 + m + 1) * n2));
+        }
         const float al[R] = {av.x, av.y, av.z, av.w}, be[R] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
         for (int c = 0; c < NC; ++c) {

@@ -63,7 +63,7 @@ enum ColMode { COL_FWD = 0, COL_PSTART = 1, COL_PEND = 2, COL_IPREP = 3, COL_PST
 
 enum Stage {
   ST_FWD_PLANE = 0, ST_COL_FWD, ST_COL_PSTART, ST_PAIR_PLANE, ST_COL_PEND, ST_REDUCE,
-  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_GAIN_PARITY, ST_NYQ, ST_COUNT
+  ST_COL_IPREP, ST_FINISH, ST_DF, ST_AXPY, ST_MASSFIX, ST_GAIN_CLUSTER, ST_GAIN_PARITY, ST_NYQ, ST_GAIN_FUSED, ST_COUNT
 };
 
 #define PII_CUDA(call)                                                                    \
@@ -218,6 +218,10 @@ struct pii_plan {
   int nq_slots = 0;            // resident CTAs of the correction kernel on the device
   int64_t nq_quad_bytes = 0;
   int nyq_path = 0;
+  // fused gain kernel (gain_fused.cu, n = 16, 24, 48, 64): per-(cluster, cell)
+  // segment sums [clusters + batch_max][n^3] and the clusters resident at once
+  void* fz_part = nullptr;
+  int fz_clusters = 0;
   void* nq_ft2 = nullptr;    // general kernel: f transposed within each a-plane [batch_max][n^3] (FP32)
   void* nq_fhn = nullptr;    // general kernel: f^ at the Nyquist-plane points [batch_max][3 n^2]
   // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core
@@ -289,6 +293,8 @@ int nyq_gen_prepare(pii_plan* p);
 int nyq_gen_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // nyq_quad.cu: the same correction as a quadratic form in f^ with precomputed kernels
 int nyq_quad_prepare(pii_plan* p);
+int gain_fused_prepare(pii_plan* p);
+int gain_fused_run(pii_plan* p, int64_t cells, cudaStream_t s);
 void nyq_quad_release(pii_plan* p);
 int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // the Nyquist correction of the packed paths: the quadratic form where it was

@@ -349,7 +349,7 @@ static void free_plan(pii_plan* p) {
                   p->G,          p->buf,        p->q,         p->d0,        p->d1,       p->d2,  p->v1dev,
                   p->gc_maps,    p->gc_hpart,   p->gp_hpart,  p->ap_reps,   p->nq_part,  p->mom,       p->flag,
                   p->dft_img,    p->dft_gs,     p->dft_colb,  p->nq_ft2,    p->nq_fhn,
-                  p->nq_A,       p->nq_B,       p->nq_fhT,    p->nq_qpart};
+                  p->nq_A,       p->nq_B,       p->nq_fhT,    p->nq_qpart,  p->fz_part};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (p->dft_err_host) cudaFreeHost(p->dft_err_host);
@@ -451,6 +451,12 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
     }
     p->gain_path = 3;
   }
+  // the fused gain kernel (one cluster of CTAs per work item) for n = 16, 24, 48, 64
+  if ((s2 = gain_fused_prepare(p)) != PII_OK) {
+    free_plan(p);
+    return s2;
+  }
+  if (p->fz_clusters > 0 && n != 64) p->gain_path = 4;  // at n = 64 the packed pipeline is faster
   // the Nyquist correction: the quadratic form wherever its kernels fit the
   // memory budget (3.4x to 9x faster than the direct kernels), else the direct
   // kernels

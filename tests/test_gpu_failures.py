@@ -32,7 +32,7 @@ def test_tensor_core_dft_stall_is_reported_and_recovers():
     sm = pkg.SpectralMesh(cfg)
     f = torch.as_tensor(maxwellian(sm.v_center, 1.0, (0.5, -0.3, 0.2), 1.3)[None], device="cuda:0")
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=1)
-    col.plan.set_dft_path("tensor")
+    col.plan.set_tuning("packed", 6, 131072, dft_path="tensor")
     good = col.collide(f, with_loss=True).clone()
     assert not col.plan.dft_stalled
     # every copy withheld: the roles give up after 1024 polls each

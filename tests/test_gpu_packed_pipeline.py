@@ -1,9 +1,9 @@
-"""The packed pipeline (antipodal passes + the general Nyquist correction) against the oracle.
+"""The packed passes (antipodal pairs + the Nyquist correction) against the oracle.
 
 For every n other than 32 the FP32 plans of an antipodally symmetric design
-evaluate each direction pair (sigma, -sigma) in one pass of the column /
-plane pipeline with a real phase, and add what the pass leaves out on the
-three Nyquist planes (k_nyq_gen).  Checked against the oracle's Q
+evaluate each direction pair (sigma, -sigma) in one pass with a real phase,
+in the fused cluster kernel (n = 16, 24, 48, 64) or the column / plane
+pipeline, and add what the pass leaves out on the three Nyquist planes.  Checked against the oracle's Q
 (src/collision/inelastic_collisions.py:208-227) on smooth and on rough input
 (uniform random f: a full spectrum, where the Nyquist planes carry weight),
 next to the unpacked pipeline, with an r-dependent restitution (e != e0).
@@ -20,9 +20,10 @@ TOL = 1e-5  # mixed precision against FP64
 CASES = [(8, 4, 6), (16, 8, 12), (24, 4, 12), (48, 3, 6), (64, 2, 6)]
 
 
+@pytest.mark.parametrize("gain", ["fused", "packed"])
 @pytest.mark.parametrize("nyq", ["quadratic", "direct"])
 @pytest.mark.parametrize("n,nr,ns", CASES)
-def test_packed_pipeline_matches_oracle(n, nr, ns, nyq):
+def test_packed_pipeline_matches_oracle(n, nr, ns, nyq, gain):
     import proj_int_inelastic_gb300 as pkg
     from oracle import fs_inelastic as fo
 
@@ -33,8 +34,12 @@ def test_packed_pipeline_matches_oracle(n, nr, ns, nyq):
     rough = np.random.default_rng(n).uniform(0.1, 1.0, (n, n, n)) * 0.05
     f = np.stack([smooth, rough])
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=2)
-    assert col.plan.tuning["gain_path"] == "packed"  # the default where the design is antipodally symmetric
+    # the defaults: the fused kernel at n = 16, 24, 48, else the packed pipeline
+    assert col.plan.tuning["gain_path"] == ("packed" if n in (8, 64) else "fused")
     assert col.plan.nyquist_path == "quadratic"  # the default correction where its kernels fit
+    if gain == "fused" and n == 8:
+        pytest.skip("no fused kernel at n = 8")
+    col.plan.set_tuning(gain, 6, 131072)
     col.plan.set_nyquist_path(nyq)
     assert col.plan.nyquist_path == nyq
     ft = torch.as_tensor(f, device="cuda:0")
@@ -47,7 +52,7 @@ def test_packed_pipeline_matches_oracle(n, nr, ns, nyq):
         ref = op.collide_cell(f[c], with_loss=True)
         refg = op.collide_cell(f[c], with_loss=False)
         ep, eu, eg = rel_linf(qp[c], ref), rel_linf(qu[c], ref), rel_linf(gp[c], refg)
-        print(f"n={n} {nyq} cell {c}: packed {ep:.2e} (gain only {eg:.2e}), unpacked {eu:.2e}")
+        print(f"n={n} {gain} {nyq} cell {c}: packed {ep:.2e} (gain only {eg:.2e}), unpacked {eu:.2e}")
         assert ep < TOL and eg < TOL and eu < TOL, c
 
 
@@ -97,3 +102,30 @@ def test_quadratic_correction_many_cells(n, nr, cells):
         for c in range(cells):
             assert rel_linf(out[nyq][c], ref[c]) < TOL, (nyq, c)
     assert rel_linf(out["quadratic"], out["direct"]) < 2e-6
+
+
+@pytest.mark.parametrize("n", [16, 24, 48])
+def test_fused_kernel_unpacked_design(n):
+    """A direction set without antipodal pairs: the fused kernel runs every
+    (r, sigma) pair unpacked, with no Nyquist correction; against the
+    pipeline and the FP64 plan."""
+    import proj_int_inelastic_gb300 as pkg
+
+    rng = np.random.default_rng(n)
+    pts = rng.standard_normal((7, 3))
+    pts /= np.linalg.norm(pts, axis=1, keepdims=True)
+    cfg = op_config(n, L8_S, 3, 7, 0.7, 0.9, 1.0)
+    cfg["spherical-design-rule"]["points"] = pts
+    sm = pkg.SpectralMesh(cfg)
+    v = sm.v_center
+    f = np.stack([maxwellian(v, 1.0, (0.5, -0.2, 0.1), 1.1), rng.uniform(0.1, 1.0, (n, n, n)) * 0.05])
+    ft = torch.as_tensor(f, device="cuda:0")
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=2)
+    assert col.plan.tuning["gain_path"] == "fused"
+    qf = col.collide(ft, with_loss=True).cpu().numpy()
+    col.plan.set_tuning("pipeline", 6, 131072)
+    qp = col.collide(ft, with_loss=True).cpu().numpy()
+    qd = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=2).collide(ft, with_loss=True)
+    qd = qd.cpu().numpy()
+    for c in range(2):
+        assert rel_linf(qf[c], qd[c]) < TOL and rel_linf(qp[c], qd[c]) < TOL, c

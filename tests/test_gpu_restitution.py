@@ -5,8 +5,9 @@ as one batched plan whose gain tables hold one set per cell
 (pii_plan_set_restitution).  Each cell's Q must equal the operator built for
 that cell's (e, e0) alone (src/collision/inelastic_collisions.py:30-52,77-103):
 checked against the oracle for the pipeline (FP64 and mixed), the fused n = 32
-packed kernel with its Nyquist correction, and the n = 64 tensor-core column
-path.
+packed kernel with its Nyquist correction, the fused cluster kernel of the
+other sizes (the mixed default at n = 16, 24, 48, 64) and the n = 64
+tensor-core column path.
 """
 import math
 
@@ -34,6 +35,9 @@ def _cells(v, k):
 CASES = [  # (n, s, n_r, n_sigma, precision, path, tolerance)
     (16, L8_S, 8, 12, "double", None, 1e-12),
     (16, L8_S, 8, 12, "mixed", None, 1e-5),
+    (16, L8_S, 8, 12, "mixed", "packed", 1e-5),
+    (48, L8_S, 3, 6, "mixed", "fused", 1e-5),
+    (64, 20.0 / (3.0 + math.sqrt(2.0)), 4, 6, "mixed", "fused", 1e-5),
     (32, L8_S, 8, 32, "mixed", "packed", 1e-5),
     (32, L8_S, 8, 32, "mixed", "parity", 1e-5),
     (64, 20.0 / (3.0 + math.sqrt(2.0)), 4, 6, "mixed", "tensor", 1e-5),
@@ -50,7 +54,7 @@ def test_per_cell_restitution_matches_oracle(n, s, nr, ns, precision, path, tol)
     f = _cells(sm.v_center, len(E_SETS))
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, batch_max=len(E_SETS))
     if path == "tensor":
-        col.plan.set_dft_path("tensor")
+        col.plan.set_tuning("packed", 6, 131072, dft_path="tensor")
     elif path is not None:
         col.plan.set_tuning(path, 6, 131072)
     col.plan.set_restitution([e for e, _ in E_SETS], [e0 for _, e0 in E_SETS])

@@ -216,12 +216,12 @@ def test_large_grid_n64_full_quadrature_vs_oracle_fixture(golden):
     print(f"n=64 full quadrature, FP64 path vs oracle: rel Linf {err:.3e}")
     assert err < 1e-12
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed")
-    for path in ("fft", "tensor"):
-        col.plan.set_dft_path(path)
+    for gain, path in (("fused", None), ("packed", "fft"), ("packed", "tensor")):
+        col.plan.set_tuning(gain, 6, 131072, dft_path=path)
         qm = col.collide(ft, with_loss=True)
         err = rel_linf(qm.cpu().numpy(), ref)
-        print(f"n=64 full quadrature, mixed path ({path} columns) vs oracle: rel Linf {err:.3e}")
-        assert err < 1e-5, path
+        print(f"n=64 full quadrature, mixed path ({gain}, {path} columns) vs oracle: rel Linf {err:.3e}")
+        assert err < 1e-5, (gain, path)
     assert not col.plan.dft_stalled
 
 
@@ -253,7 +253,7 @@ def test_large_grid_n64_tensor_core_dft():
     f = torch.as_tensor(f, device="cuda:0")
     qd = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=2).collide(f, with_loss=True)
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=2)
-    col.plan.set_dft_path("fft")
+    col.plan.set_tuning("packed", 6, 131072, dft_path="fft")
     qf = col.collide(f, with_loss=True)
     col.plan.set_dft_path("tensor")
     assert col.plan.tuning["dft_path"] == "tensor"

@@ -235,7 +235,7 @@ def test_python_tuning_maps():
     import proj_int_inelastic_gb300 as pkg
     from proj_int_inelastic_gb300 import collision
 
-    assert collision.GAIN_PATHS == {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3}
+    assert collision.GAIN_PATHS == {"pipeline": 0, "cluster": 1, "parity": 2, "packed": 3, "fused": 4}
     assert collision.DFT_PATHS == {"fft": 0, "tensor": 1}
     assert collision._code(collision.GAIN_PATHS, "packed", "gain_path") == 3
     with pytest.raises(ValueError, match="gain_path must be one of"):
