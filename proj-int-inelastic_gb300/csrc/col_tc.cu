@@ -664,10 +664,12 @@ int dft_stall_check(pii_plan* p) {
   const int v = *w;
   if (!v) return PII_OK;
   *w = 0;
-  set_error(v == 2 ? "tensor-core DFT: a CTA gave up waiting and could not drain its copies; results of that "
-                     "launch are invalid"
-                   : "tensor-core DFT: a CTA gave up waiting (bounded mbarrier wait); results of that launch are "
-                     "invalid");
+  set_error(v == 3   ? "fused gain kernel: a CTA gave up waiting for a cluster exchange (bounded mbarrier wait); "
+                       "results of that launch are invalid"
+            : v == 2 ? "tensor-core DFT: a CTA gave up waiting and could not drain its copies; results of that "
+                       "launch are invalid"
+                     : "tensor-core DFT: a CTA gave up waiting (bounded mbarrier wait); results of that launch are "
+                       "invalid");
   return PII_ERR_STALL;
 }
 

@@ -11,12 +11,16 @@
 // [r NPL, (r + 1) NPL) in stage B and the columns (b, c) with b in the same
 // range in stages A and C (NPL = n / CS; n = 16, 24: CS = 1, the item fits one
 // CTA; n = 48: CS = 8; n = 64: CS = 16).  Between the layouts each thread
-// stores its line straight into the owning CTA's shared memory
-// (st.shared::cluster): a column's n values go to the n / NPL plane owners,
-// a plane column's n values to the column owners, 256 contiguous bytes per
-// warp store.  Cluster barriers (release / acquire, split arrive / wait)
-// order the exchanges; the arrive that frees a buffer is issued as soon as
-// its last read is done, so the transform that follows hides the wait.
+// stores its line straight into the owning CTA's shared memory with st.async,
+// which counts the bytes on the receiver's mbarrier: a column's n values go to
+// the n / NPL plane owners, a plane column's n values to the column owners,
+// 256 contiguous bytes per warp store.  A CTA waits (bounded) for its
+// mbarrier to see all N3 / CS elements of an exchange; a cluster barrier
+// arrived on right after a buffer's last read (split arrive / wait, so the
+// transform that follows hides it) keeps the next exchange from overwriting
+// a buffer still being read.  The phase and gain rows of a pass and the sinc
+// row of its radial node are copied to shared memory by cp.async one stage
+// ahead of their use.
 // The gain sum of the CTA's columns, n k_a values each (n = 64: 64 KB per
 // CTA ... 110 KB at n = 48), lives in tensor memory for all the items of a
 // cell; at the end of a cell's range the CTA writes it to a per-part slot,
@@ -29,6 +33,7 @@
 #include "pack.cuh"
 #include "pii_internal.cuh"
 #include "tmem.cuh"
+#include "umma.cuh"
 
 namespace pii {
 
@@ -66,7 +71,12 @@ struct Geo {
   static constexpr size_t F_OFF = size_t(BUF) * sizeof(float2);
   // f of the CTA's planes, rows padded to LD floats (the row pass reads
   // f[pl][b][c] for one c across lanes of consecutive b)
-  static constexpr size_t SMEM = F_OFF + size_t(NPL) * NV * LD * sizeof(float) + 16;
+  static constexpr size_t ROW_OFF = F_OFF + size_t(NPL) * NV * LD * sizeof(float);
+  // the pass's phase row and gain row (3 n complex each), the radial node's sinc row
+  static constexpr int M1 = 3 * (NV / 2) * (NV / 2) + 1;
+  static constexpr size_t SLAB_OFF = ROW_OFF + size_t(6 * NV) * sizeof(float2);
+  static constexpr size_t BAR_OFF = (SLAB_OFF + size_t(M1) * sizeof(float) + 15) / 16 * 16;
+  static constexpr size_t SMEM = BAR_OFF + 16 + 16;  // two mbarriers, the tensor-memory slot
   static constexpr int WARPS = THREADS / 32;
   static constexpr int TCOLS_USED = ((WARPS + 3) / 4) * 2 * NV;
   static constexpr int TCOLS = TCOLS_USED <= 32    ? 32
@@ -91,6 +101,8 @@ struct FusedArgs {
   const int* reps;  // packed: the representative pair of each pass
   int64_t cells;
   float2* part;  // [clusters + cells][N3]: the gain sums of each (cluster, cell) segment
+  int* err;      // mapped stall word: 3 if an exchange wait gave up
+  uint32_t wait_limit;
 };
 
 __device__ __forceinline__ uint32_t fz_rank() {
@@ -103,8 +115,26 @@ __device__ __forceinline__ uint32_t fz_map(uint32_t addr, uint32_t rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void fz_st(uint32_t addr, float2 v) {
-  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
+__device__ __forceinline__ void fz_st_async(uint32_t addr, float2 v, uint32_t mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
+               "f"(v.x), "f"(v.y), "r"(mbar)
+               : "memory");
+}
+// waits (bounded) for phase `parity` of a barrier whose bytes other CTAs deliver
+__device__ __forceinline__ bool fz_wait_bar(uint64_t* mbar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(mbar));
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
 }
 __device__ __forceinline__ void fz_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void fz_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
@@ -116,13 +146,21 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* buf = reinterpret_cast<float2*>(smem_raw);
   float* fS = reinterpret_cast<float*>(smem_raw + G::F_OFF);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + G::SMEM - 16);
+  float2* erow = reinterpret_cast<float2*>(smem_raw + G::ROW_OFF);  // phase row of the current pass
+  float2* grow = erow + 3 * NV;                                      // gain row
+  float* slab = reinterpret_cast<float*>(smem_raw + G::SLAB_OFF);    // sinc row of the radial node
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + G::BAR_OFF);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem_raw + G::BAR_OFF + 16);
   const int t = threadIdx.x, warp = t >> 5;
   const int rank = CS > 1 ? int(fz_rank()) : 0;
   const int cl = int(blockIdx.x) / CS, ncl = int(gridDim.x) / CS;
   if (warp == 0) {
     tm_alloc(tslot, G::TCOLS);
     tm_relinquish();
+  }
+  if (CS > 1 && t == 0) {
+    mbar_init(&bars[0], 1);  // stage-A exchange: its thread 0 arrives with the expected bytes
+    mbar_init(&bars[1], 1);  // stage-B exchange
   }
   tm_fence_before();
   __syncthreads();
@@ -137,13 +175,23 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
   const int kb = kval(jb, NV), kc = kval(jc, NV);
   const int mbc = kb * kb + kc * kc;
   const uint32_t buf_s = static_cast<uint32_t>(__cvta_generic_to_shared(buf));
+  const uint32_t bar_s = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
+  constexpr uint32_t XBYTES = uint32_t(N3 / CS) * 8;  // bytes one CTA receives per exchange
+  uint32_t phase = 0;
+  bool gave_up = false;
   // the first wait (before the first exchange) also makes sure that every CTA
-  // of the cluster runs before any shared memory of another is written
+  // of the cluster runs, with its barriers initialised, before any shared
+  // memory of another is written
   if constexpr (CS > 1) fz_arrive();
 
   const int64_t total = a.cells * a.QP;
   const int64_t w0 = total * cl / ncl, w1 = total * (cl + 1) / ncl;
-  int64_t cur = -1;
+  int64_t cur = -1, slab_key = -1;
+  if (w0 < w1) {  // the first pass's phase row
+    const int p0 = PACK ? a.reps[int(w0 % a.QP)] : int(w0 % a.QP);
+    for (int e = t; e < 3 * NV; e += G::THREADS) erow[e] = a.ephase[int64_t(p0) * 3 * NV + e];
+    __syncthreads();
+  }
   auto flush = [&](int64_t cell) {  // the segment's sums -> part[cl + cell][a][j]
     tm_wait_st();
     float2* out = a.part + (int64_t(cl) + cell) * N3 + j;
@@ -179,7 +227,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     // ---- A: phase product and inverse transform along a of the column
     {
       const float2* fh = a.fhat + cell * N3 + j;
-      const float2* ep = a.ephase + int64_t(pair) * 3 * NV;
+      const float2* ep = erow;
       if constexpr (PACK) {
         float cp, cm, th;
         pack_t_consts<float, float2, NV>(ep, jb, jc, cp, cm, th);
@@ -197,16 +245,17 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     }
     if constexpr (CS > 1) {
       fz_wait();  // every buffer of the cluster has been read by the previous item's stage C
+      if (t == 0) mbar_arrive_tx(&bars[0], XBYTES);
       static_for<0, CS>([&](auto ri) {
         constexpr int r = decltype(ri)::value;
-        const uint32_t base = fz_map(buf_s, uint32_t(r));
+        const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s, uint32_t(r));
         static_for<0, NPL>([&](auto mi) {
           constexpr int m = decltype(mi)::value;
-          fz_st(base + uint32_t(((m * NV + jb) * LD + jc) * 8), x[pos(NV, r * NPL + m)]);
+          fz_st_async(base + uint32_t(((m * NV + jb) * LD + jc) * 8), x[pos(NV, r * NPL + m)], rb);
         });
       });
-      fz_arrive();
-      fz_wait();  // the planes of the CTA are complete
+      // the planes of the CTA are complete once every CTA's elements have landed
+      if (!fz_wait_bar(&bars[0], phase, a.wait_limit)) gave_up = true;
     } else {
       __syncthreads();  // the previous item's stage C has read the buffer
       static_for<0, NV>([&](auto qi) {
@@ -214,6 +263,27 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
         buf[(q * NV + jb) * LD + jc] = x[pos(NV, q)];
       });
       __syncthreads();
+    }
+    // every thread of the CTA is past this pass's stage A and the previous
+    // pass's stage C: copy this pass's gain row, the next pass's phase row and,
+    // on a change of radial node (or cell, with one restitution set per cell),
+    // the sinc row; complete before the barriers ahead of stages C and A
+    {
+      const float2* gsrc = a.gphase + cell * a.gph_stride + int64_t(pair) * 3 * NV;
+      for (int e = t; e < 3 * NV; e += G::THREADS) cp_async8(grow + e, gsrc + e);
+      if (w + 1 < w1) {
+        const int ipn = int((w + 1) % a.QP);
+        const int pn = PACK ? a.reps[ipn] : ipn;
+        for (int e = t; e < 3 * NV; e += G::THREADS) cp_async8(erow + e, a.ephase + int64_t(pn) * 3 * NV + e);
+      }
+      const int ir = pair / a.ns;
+      const int64_t key = a.gs_stride ? cell * 65536 + ir : ir;
+      if (key != slab_key) {
+        const float* src = a.gsinc + cell * a.gs_stride + int64_t(ir) * (a.M + 1);
+        for (int e = t; e < G::M1; e += G::THREADS) cp_async4(slab + e, src + e);
+        slab_key = key;
+      }
+      cp_async_commit();
     }
     // ---- B: inverse along b (column (pl, l))
     {
@@ -226,6 +296,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
         col[b * LD] = x[pos(NV, b)];
       });
     }
+    cp_async_wait_group<0>();  // the rows and the sinc row (read after the next barrier)
     __syncthreads();
     // inverse along c, * f, forward along c (row (pl, l))
     {
@@ -256,16 +327,17 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       if constexpr (CS > 1) {
         const int ag = rank * NPL + pl;  // the plane's a
         fz_wait();                       // every CTA has read its planes
+        if (t == 0) mbar_arrive_tx(&bars[1], XBYTES);
         static_for<0, CS>([&](auto ri) {
           constexpr int r = decltype(ri)::value;
-          const uint32_t base = fz_map(buf_s, uint32_t(r));
+          const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s + 8, uint32_t(r));
           static_for<0, NPL>([&](auto mi) {
             constexpr int m = decltype(mi)::value;
-            fz_st(base + uint32_t((ag * NCOL + m * NV + l) * 8), x[pos(NV, r * NPL + m)]);
+            fz_st_async(base + uint32_t((ag * NCOL + m * NV + l) * 8), x[pos(NV, r * NPL + m)], rb);
           });
         });
-        fz_arrive();
-        fz_wait();  // the columns of the CTA are complete
+        if (!fz_wait_bar(&bars[1], phase, a.wait_limit)) gave_up = true;  // the CTA's columns have landed
+        phase ^= 1;
       } else {
         static_for<0, NV>([&](auto bi) {
           constexpr int b = decltype(bi)::value;
@@ -285,8 +357,8 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
         for (int q = 0; q < NV; ++q) x[q] = buf[(q * NV + jb) * LD + jc];
       }
       fft_line<NV, -1>(x);
-      const float2* gp = a.gphase + cell * a.gph_stride + int64_t(pair) * 3 * NV;
-      const float* gs = a.gsinc + cell * a.gs_stride + int64_t(pair / a.ns) * (a.M + 1) + mbc;
+      const float2* gp = grow;
+      const float* gs = slab + mbc;
       float2 v[NV];
       if constexpr (PACK) {
         float dp, dm, sh;
@@ -323,6 +395,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
   }
   if (cur >= 0) flush(cur);
   if constexpr (CS > 1) fz_wait();  // matches the last arrive; no CTA leaves while others may still write to it
+  if (gave_up) atomicMax(a.err, 3);
   tm_wait_st();
   tm_fence_before();
   __syncthreads();
@@ -384,6 +457,7 @@ static int fused_setup(int* clusters) {
 
 template <int NV>
 static int fused_prepare_t(pii_plan* p) {
+  if (p->tab.M + 1 != gfu::Geo<NV>::M1) return PII_OK;  // the sinc row size the kernel stages
   int c1 = 0, c2 = 0;
   PII_TRY((fused_setup<NV, true>(&c1)));
   PII_TRY((fused_setup<NV, false>(&c2)));
@@ -393,6 +467,11 @@ static int fused_prepare_t(pii_plan* p) {
   PII_CUDA(cudaMalloc(&p->fz_part, bytes));
   p->bytes += int64_t(bytes);
   p->fz_clusters = clusters;
+  if (!p->dft_err_host) {  // the mapped stall word (shared with the tensor-core column passes)
+    PII_CUDA(cudaHostAlloc(&p->dft_err_host, sizeof(int), cudaHostAllocMapped));
+    *p->dft_err_host = 0;
+    PII_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&p->dft_err), p->dft_err_host, 0));
+  }
   return PII_OK;
 }
 
@@ -425,6 +504,8 @@ static int fused_run_t(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.reps = p->ap_reps;
   a.cells = cells;
   a.part = static_cast<float2*>(p->fz_part);
+  a.err = p->dft_err;
+  a.wait_limit = p->dft_wait_limit;
   const int clusters = int(std::min<int64_t>(p->fz_clusters, cells * a.QP));
   cudaLaunchConfig_t cfg;
   cudaLaunchAttribute attr[1];

@@ -229,7 +229,7 @@ struct pii_plan {
   int dft_path = 0;
   void* dft_img = nullptr;  // DFT matrix images (A_hi | A_lo) for DIR = +1 and -1
   int* dft_err = nullptr;   // device address of dft_err_host
-  int* dft_err_host = nullptr;  // mapped host word: 1 if a k_col_tc CTA gave up waiting (2: and could not drain)
+  int* dft_err_host = nullptr;  // mapped host word: 1 if a k_col_tc CTA gave up waiting (2: and could not drain; 3: a k_gain_fused exchange)
   uint32_t dft_wait_limit = 1u << 22;  // mbarrier polls before a k_col_tc role gives up
   int dft_withhold = 0;     // test hook: k_col_tc's TMA thread issues no copies
   int dft_ctas = 0;         // resident CTAs of k_col_tc (one per SM)
