@@ -448,6 +448,14 @@ static int fused_setup(int* clusters) {
   using G = gfu::Geo<NV>;
   PII_CUDA(cudaFuncSetAttribute(k_gain_fused<NV, PACK>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(G::SMEM)));
   if (G::CS > 8) PII_CUDA(cudaFuncSetAttribute(k_gain_fused<NV, PACK>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  if (G::CS == 1) {  // single-CTA items: every resident CTA of every SM
+    int per_sm = 0, sms = 0, dev = 0;
+    PII_CUDA(cudaGetDevice(&dev));
+    PII_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PII_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gain_fused<NV, PACK>, G::THREADS, G::SMEM));
+    *clusters = per_sm * sms;
+    return PII_OK;
+  }
   cudaLaunchConfig_t cfg;
   cudaLaunchAttribute attr[1];
   fused_config<NV, PACK>(cfg, attr, 1, nullptr);
