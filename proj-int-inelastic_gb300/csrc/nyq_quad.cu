@@ -35,6 +35,16 @@
 // coalesced 16-byte vector per lane and step, once per group of cells.  The
 // input points of an orientation are split into ranges across CTAs; each
 // range writes its partial sums and k_quad_add adds them into G.
+//
+// Pairing.  f is real, so f^(-q) = conj f^(q), and the terms of q and -q
+// (both Nyquist points) combine into one:
+//   A~(k, q) f^(q) f^(k - q) - B~(k, q) conj f^(q) f^(k + q),
+//   A~ = w (A(k, q) - B(k, -q)),  B~ = w (B(k, q) - A(k, -q)),
+// with w = 1/2 where q = -q.  The kernel walks one of each pair: slices
+// 1 .. h - 1 whole (their partners are slices n - 1 .. h + 1) and half of the
+// self-paired slices 0 and h (their rows i1 = 0, h up to i2 = h, padded to a
+// multiple of R with zero kernels, and slice 0's column up to i1 < h): the
+// same two planes per slice, about half the input points.
 #include <algorithm>
 #include <vector>
 
@@ -89,22 +99,31 @@ __global__ void __launch_bounds__(256) k_quad_coef(const int* pts, int npts, int
   }
 }
 
-// C[j][kk] = sum_p T[p][qi[j]] X[p][ki[kk]]  (ki[kk] < 0: the output point is
-// skipped, its column zero); T and X rows have npts entries in point order
-__global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* X, const int* qi, const int* ki,
-                                                    float* C, int M, int Ncol, int QP, int npts) {
+// C[j][kk] = w_j sum_p (T[p][q1_j] X1[p][ki[kk]] - T[p][q2_j] X2[p][ki[kk]]):
+// the paired kernel of slot j (q1 its input point, q2 = -q1; q1 < 0 marks a
+// padding slot, zero) at the output points ki (ki < 0: skipped, zero); T, X1
+// and X2 rows hold npts entries in point order
+__global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* X1, const float* X2, const int* q1,
+                                                    const int* q2, const float* w, const int* ki, float* C, int M,
+                                                    int Ncol, int QP, int npts) {
   using namespace nqq;
   __shared__ float ta[TK][TM], tb[TK][TM];
   const int q0 = blockIdx.y * TM, k0 = blockIdx.x * TM;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads, 4 x 4 outputs each
   float acc[4][4] = {};
-  for (int p0 = 0; p0 < QP; p0 += TK) {
+  for (int p0 = 0; p0 < 2 * QP; p0 += TK) {  // the passes twice: + T(q) X1, - T(-q) X2
     for (int e = threadIdx.x; e < TK * TM; e += 256) {
       const int pp = e / TM, c = e - pp * TM;
-      const bool okp = p0 + pp < QP;
+      const int pg = p0 + pp, second = pg >= QP ? 1 : 0, p = pg - second * QP;
+      const bool okp = pg < 2 * QP;
       const int kidx = okp && k0 + c < Ncol ? ki[k0 + c] : -1;
-      ta[pp][c] = okp && q0 + c < M ? T[int64_t(p0 + pp) * npts + qi[q0 + c]] : 0.f;
-      tb[pp][c] = kidx >= 0 ? X[int64_t(p0 + pp) * npts + kidx] : 0.f;
+      float tv = 0.f;
+      if (okp && q0 + c < M && q1[q0 + c] >= 0) {
+        const int qq = second ? q2[q0 + c] : q1[q0 + c];
+        tv = (second ? -w[q0 + c] : w[q0 + c]) * T[int64_t(p) * npts + qq];
+      }
+      ta[pp][c] = tv;
+      tb[pp][c] = kidx >= 0 ? (second ? X2 : X1)[int64_t(p) * npts + kidx] : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -152,29 +171,18 @@ __global__ void __launch_bounds__(256) k_quad_prep(const float2* fhat, float2* f
   }
 }
 
-// segment g of an orientation's input points: slice s, kind (0: a row of n
-// points at i1, 1: the column i2 = h without i1 = h), first point index j0
-__device__ __forceinline__ void qq_segment(int g, int n, int& s, int& kind, int& i1, int& j0) {
-  const int h = n >> 1, L = 2 * n - 1;
-  if (g < 2 * h) {
-    s = g >> 1, kind = g & 1, i1 = h, j0 = s * L + kind * n;
-  } else if (g < 2 * h + n) {
-    s = h, kind = 0, i1 = g - 2 * h, j0 = h * L + i1 * n;
-  } else {
-    const int gg = g - 2 * h - n;
-    s = h + 1 + (gg >> 1), kind = gg & 1, i1 = h, j0 = h * L + n * n + (s - h - 1) * L + kind * n;
-  }
-}
-
 struct QuadArgs {
   const float* A;
   const float* B;
   const float2* fhat;
   const float2* fhT;
   float2* part;        // [split][cells][3][n][n]
+  const int4* segs;    // segments of the kernel slots: (slice, 0 row / 1 column, row i1, steps)
+  const int* seg_j0;   // first kernel slot of each segment
+  int nseg;
   int64_t cells;
   int64_t set_stride;  // floats between consecutive cells' kernels (0: one set for every cell)
-  int n, npts, W, split;
+  int n, npts, W, split;  // npts: kernel slots per orientation
 };
 
 __device__ __forceinline__ void qq_term(float2& acc, float a, float b, float2 f0, float2 gm, float2 gp) {
@@ -219,12 +227,12 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[c][r] = make_float2(0.f, 0.f);
 
-  const int nseg = 3 * n - 2;
+  const int nseg = a.nseg;
   const int g0 = range * nseg / a.split, g1 = (range + 1) * nseg / a.split;
   int cur = -1;
   for (int g = g0; g < g1; ++g) {
-    int s, kind, i1f, j0;
-    qq_segment(g, n, s, kind, i1f, j0);
+    const int4 sg = __ldg(a.segs + g);
+    const int s = sg.x, kind = sg.y, i1f = sg.z, len = sg.w, j0 = __ldg(a.seg_j0 + g);
     if (s != cur) {  // stage the slice's planes for the group's cells
       __syncthreads();
       const int vm = (h - s + n) % n, vp = (n - vm) % n, v2 = s == h ? h : vp;
@@ -249,7 +257,7 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
       __syncthreads();
       cur = s;
     }
-    if (kind == 0) {  // a row of input points: i1 = i1f, i2 = 0 .. n - 1
+    if (kind == 0) {  // a row of input points: i1 = i1f, i2 = 0 .. len - 1 (len a multiple of R)
       int rm = k1 - i1f, rp = k1 + i1f;
       rm += rm < 0 ? n : 0;
       rp -= rp >= n ? n : 0;
@@ -277,11 +285,11 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
         an[t] = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(t) * n2));
         bn[t] = __ldg(reinterpret_cast<const float4*>(Bj + int64_t(t) * n2));
       }
-      for (int i20 = 0; i20 < n; i20 += R) {
+      for (int i20 = 0; i20 < len; i20 += R) {
         float4 ac[R], bc[R];
 #pragma unroll
         for (int t = 0; t < R; ++t) ac[t] = an[t], bc[t] = bn[t];
-        if (i20 + R < n) {
+        if (i20 + R < len) {
 #pragma unroll
           for (int t = 0; t < R; ++t) {
             an[t] = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(i20 + R + t) * n2));
@@ -306,18 +314,18 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
           }
         }
       }
-    } else {  // the column i2 = h of slice s != h, i1 over [0, n) without h
+    } else {  // the column i2 = h of slice s != h: i1 = m (m < h), m + 1 (m >= h), m < len
       const int cm = (k20 + h) % n;  // k2 -+ h for the thread's first k2 (no wrap within the R)
-      // the column's n - 1 input points are consecutive in the kernels: j0 + m, m < n - 1
+      // the column's input points are consecutive in the kernels: j0 + m
       float4 an = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(j0) * n2));
       float4 bn = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(j0) * n2));
-      for (int m = 0; m < n - 1; ++m) {
+      for (int m = 0; m < len; ++m) {
         const int i1 = m < h ? m : m + 1;
         int rm = k1 - i1, rp = k1 + i1;
         rm += rm < 0 ? n : 0;
         rp -= rp >= n ? n : 0;
         const float4 av = an, bv = bn;
-        if (m + 1 < n - 1) {
+        if (m + 1 < len) {
           an = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(j0 + m + 1) * n2));
           bn = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(j0 + m + 1) * n2));
         }
@@ -402,11 +410,11 @@ static int quad_kernel_setup(const QuadCfg& c, int* per_sm) {
 static int quad_split(const pii_plan* p, const QuadCfg& c, int64_t cells) {
   const int64_t base = int64_t(p->n / c.W) * ((cells + c.nc - 1) / c.nc) * 3;
   const int64_t want = (2 * int64_t(p->nq_slots) + base - 1) / base;
-  return int(std::max<int64_t>(1, std::min<int64_t>(want, std::min(nqq::SPLIT_MAX, 3 * p->n - 2))));
+  return int(std::max<int64_t>(1, std::min<int64_t>(want, std::min(nqq::SPLIT_MAX, std::max(1, p->nq_nseg)))));
 }
 
 static void free_quad(pii_plan* p) {
-  for (void** q : {&p->nq_A, &p->nq_B, &p->nq_fhT, &p->nq_qpart})
+  for (void** q : {&p->nq_A, &p->nq_B, &p->nq_fhT, &p->nq_qpart, &p->nq_segs})
     if (*q) {
       cudaFree(*q);
       *q = nullptr;
@@ -414,6 +422,7 @@ static void free_quad(pii_plan* p) {
   p->bytes -= p->nq_quad_bytes;
   p->nq_quad_bytes = 0;
   p->nq_npts = 0;
+  p->nq_nseg = 0;
   p->nq_qpart_units = 0;
 }
 
@@ -440,17 +449,58 @@ int nyq_quad_prepare(pii_plan* p) {
   auto code = [&](int d, int v, int i1, int i2) {
     return d == 0 ? v * n2 + i1 * n + i2 : d == 1 ? i1 * n2 + v * n + i2 : i1 * n2 + i2 * n + v;
   };
-  // input points of each orientation in slice order, output points in the kernels' layout
-  std::vector<int> qi, ki;
+  // the kernel slots: one input point of each pair {q, -q}, by segment (the
+  // same index pattern for every orientation); rows padded to a multiple of R
+  std::vector<int4> segs;
+  std::vector<int> seg_j0;
+  std::vector<char> seg_half;
+  int NJ = 0;
+  auto addseg = [&](int s, int kind, int i1, int len, bool half) {
+    segs.push_back(make_int4(s, kind, i1, len));
+    seg_j0.push_back(NJ);
+    seg_half.push_back(half ? 1 : 0);
+    NJ += len;
+  };
+  for (int s = 0; s <= h; ++s) {
+    if (s == 0) {
+      addseg(0, 0, h, h + R, true);  // the row of slice 0 up to i2 = h
+      addseg(0, 1, h, h, false);     // its column up to i1 < h
+    } else if (s < h) {
+      addseg(s, 0, h, n, false);
+      addseg(s, 1, h, n - 1, false);
+    } else {
+      for (int i1 = 0; i1 <= h; ++i1) addseg(h, 0, i1, i1 == 0 || i1 == h ? h + R : n, i1 == 0 || i1 == h);
+    }
+  }
+  const int nseg = int(segs.size());
+  auto negc = [&](int c) {
+    const int a = c / n2, b = (c / n) % n, cc = c % n;
+    return ((n - a) % n) * n2 + ((n - b) % n) * n + (n - cc) % n;
+  };
+  // per orientation and slot: the point q, its negative, the pair weight;
+  // output points in the kernels' layout
+  std::vector<int> q1, q2, ki;
+  std::vector<float> wq;
   for (int d = 0; d < 3; ++d) {
-    for (int s = 0; s < n; ++s) {
-      if (s != h) {
-        for (int i2 = 0; i2 < n; ++i2) qi.push_back(pidx[code(d, s, h, i2)]);
-        for (int i1 = 0; i1 < n; ++i1)
-          if (i1 != h) qi.push_back(pidx[code(d, s, i1, h)]);
-      } else {
-        for (int i1 = 0; i1 < n; ++i1)
-          for (int i2 = 0; i2 < n; ++i2) qi.push_back(pidx[code(d, h, i1, i2)]);
+    for (int g = 0; g < nseg; ++g) {
+      const int4 sg = segs[g];
+      for (int m = 0; m < sg.w; ++m) {
+        int c = -1;
+        if (sg.y == 0) {
+          if (!(seg_half[g] && m > h)) c = code(d, sg.x, sg.z, m);
+        } else {
+          c = code(d, sg.x, m < h ? m : m + 1, h);
+        }
+        if (c < 0) {
+          q1.push_back(-1), q2.push_back(0), wq.push_back(0.f);
+          continue;
+        }
+        const int cn = negc(c);
+        if (pidx[c] < 0 || pidx[cn] < 0) {
+          set_error("nyq_quad_prepare: internal error in the input-point order");
+          return PII_ERR_ARG;
+        }
+        q1.push_back(pidx[c]), q2.push_back(pidx[cn]), wq.push_back(c == cn ? 0.5f : 1.f);
       }
     }
     for (int kbg = 0; kbg < n / R; ++kbg)
@@ -461,11 +511,7 @@ int nyq_quad_prepare(pii_plan* p) {
           ki.push_back(skip ? -1 : pidx[code(d, h, k1, k2)]);
         }
   }
-  for (int v : qi)
-    if (v < 0) {
-      set_error("nyq_quad_prepare: internal error in the input-point order");
-      return PII_ERR_ARG;
-    }
+  p->nq_nseg = nseg;
   const int64_t sets = p->tab.nsets, QP = p->ap_count;
   const QuadCfg cfg = quad_cfg(n, int(sets));
   int per_sm = 0, sms = 0;
@@ -475,15 +521,19 @@ int nyq_quad_prepare(pii_plan* p) {
   p->nq_slots = per_sm * sms;
   int64_t units = 0;  // (range, cell) units of the partial sums at the largest use
   for (int64_t c = 1; c <= p->batch_max; ++c) units = std::max(units, int64_t(quad_split(p, cfg, c)) * c);
-  const size_t kern = size_t(sets) * 3 * size_t(npts) * n2 * sizeof(float);  // each of A, B
+  const size_t kern = size_t(sets) * 3 * size_t(NJ) * n2 * sizeof(float);  // each of A, B
   const size_t fhT = size_t(p->batch_max) * size_t(n2) * n * sizeof(float2);
   const size_t part = size_t(units) * 3 * n2 * sizeof(float2);
   size_t free_b = 0, total_b = 0;
   PII_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const size_t budget = std::min<size_t>(size_t(16) << 30, free_b / 4);
-  if (2 * kern + fhT + part > budget) return PII_OK;  // the direct kernels stay in use
-  float *T = nullptr, *Al = nullptr, *Be = nullptr;
-  int *dpts = nullptr, *dqi = nullptr, *dki = nullptr;
+  const size_t segb = size_t(nseg) * (sizeof(int4) + sizeof(int));
+  if (2 * kern + fhT + part + segb > budget) {  // the direct kernels stay in use
+    p->nq_nseg = 0;
+    return PII_OK;
+  }
+  float *T = nullptr, *Al = nullptr, *Be = nullptr, *dw = nullptr;
+  int *dpts = nullptr, *dq1 = nullptr, *dq2 = nullptr, *dki = nullptr;
   const size_t coef = size_t(QP) * npts * sizeof(float);
   int st = PII_OK;
   auto al = [&](void** dst, size_t b) {
@@ -496,29 +546,41 @@ int nyq_quad_prepare(pii_plan* p) {
   al(&p->nq_B, kern);
   al(&p->nq_fhT, fhT);
   al(&p->nq_qpart, part);
+  al(&p->nq_segs, segb);
   al((void**)&T, coef);
   al((void**)&Al, coef * sets);
   al((void**)&Be, coef * sets);
   al((void**)&dpts, pts.size() * sizeof(int));
-  al((void**)&dqi, qi.size() * sizeof(int));
+  al((void**)&dq1, q1.size() * sizeof(int));
+  al((void**)&dq2, q2.size() * sizeof(int));
+  al((void**)&dw, wq.size() * sizeof(float));
   al((void**)&dki, ki.size() * sizeof(int));
   if (st == PII_OK) {
     PII_CUDA(cudaMemcpy(dpts, pts.data(), pts.size() * sizeof(int), cudaMemcpyHostToDevice));
-    PII_CUDA(cudaMemcpy(dqi, qi.data(), qi.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(dq1, q1.data(), q1.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(dq2, q2.data(), q2.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(dw, wq.data(), wq.size() * sizeof(float), cudaMemcpyHostToDevice));
     PII_CUDA(cudaMemcpy(dki, ki.data(), ki.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(p->nq_segs, segs.data(), size_t(nseg) * sizeof(int4), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(static_cast<char*>(p->nq_segs) + size_t(nseg) * sizeof(int4), seg_j0.data(),
+                        size_t(nseg) * sizeof(int), cudaMemcpyHostToDevice));
     const int64_t work = QP * npts * (sets + 1);
     k_quad_coef<<<unsigned((work + 255) / 256), 256>>>(
         dpts, npts, n, p->ap_reps, int(QP), p->ns, p->tab.M, static_cast<const float2*>(p->tab.ephase),
         static_cast<const float2*>(p->tab.gphase), static_cast<const float*>(p->tab.gsinc), p->tab.gph_stride,
         p->tab.gs_stride, int(sets), T, Al, Be);
-    const dim3 grid(unsigned((n2 + TM - 1) / TM), unsigned((npts + TM - 1) / TM));
+    const dim3 grid(unsigned((n2 + TM - 1) / TM), unsigned((NJ + TM - 1) / TM));
     for (int64_t s = 0; s < sets; ++s)
       for (int d = 0; d < 3; ++d) {
-        const int64_t o = (s * 3 + d) * int64_t(npts) * n2;
-        k_quad_gemm<<<grid, 256>>>(T, Al + s * QP * npts, dqi + d * npts, dki + d * n2,
-                                   static_cast<float*>(p->nq_A) + o, npts, n2, int(QP), npts);
-        k_quad_gemm<<<grid, 256>>>(T, Be + s * QP * npts, dqi + d * npts, dki + d * n2,
-                                   static_cast<float*>(p->nq_B) + o, npts, n2, int(QP), npts);
+        const int64_t o = (s * 3 + d) * int64_t(NJ) * n2;
+        const float *al_s = Al + s * QP * npts, *be_s = Be + s * QP * npts;
+        const int *q1d = dq1 + d * NJ, *q2d = dq2 + d * NJ;
+        const float* wd = dw + d * NJ;
+        // A~ = w (A(k, q) - B(k, -q)),  B~ = w (B(k, q) - A(k, -q))
+        k_quad_gemm<<<grid, 256>>>(T, al_s, be_s, q1d, q2d, wd, dki + d * n2, static_cast<float*>(p->nq_A) + o, NJ,
+                                   n2, int(QP), npts);
+        k_quad_gemm<<<grid, 256>>>(T, be_s, al_s, q1d, q2d, wd, dki + d * n2, static_cast<float*>(p->nq_B) + o, NJ,
+                                   n2, int(QP), npts);
       }
     const cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -526,14 +588,15 @@ int nyq_quad_prepare(pii_plan* p) {
       st = PII_ERR_CUDA;
     }
   }
-  for (void* q : {(void*)T, (void*)Al, (void*)Be, (void*)dpts, (void*)dqi, (void*)dki}) cudaFree(q);
+  for (void* q : {(void*)T, (void*)Al, (void*)Be, (void*)dw, (void*)dpts, (void*)dq1, (void*)dq2, (void*)dki})
+    cudaFree(q);
   if (st != PII_OK) {
     free_quad(p);
     return st;
   }
-  p->nq_npts = npts;
+  p->nq_npts = NJ;
   p->nq_qpart_units = units;
-  p->nq_quad_bytes = int64_t(2 * kern + fhT + part);
+  p->nq_quad_bytes = int64_t(2 * kern + fhT + part + segb);
   p->bytes += p->nq_quad_bytes;
   return PII_OK;
 }
@@ -562,6 +625,9 @@ int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.part = static_cast<float2*>(p->nq_qpart);
   a.cells = cells;
   a.set_stride = p->tab.nsets > 1 ? int64_t(3) * p->nq_npts * n2 : 0;
+  a.segs = static_cast<const int4*>(p->nq_segs);
+  a.seg_j0 = reinterpret_cast<const int*>(static_cast<const char*>(p->nq_segs) + size_t(p->nq_nseg) * sizeof(int4));
+  a.nseg = p->nq_nseg;
   a.n = n, a.npts = p->nq_npts, a.W = cfg.W, a.split = split;
   StageTimer st(p, ST_NYQ, s);
   const int tb = (n + 31) / 32;

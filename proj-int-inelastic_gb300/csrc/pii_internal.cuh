@@ -205,8 +205,8 @@ struct pii_plan {
   int ap_count = 0;
   void* nq_part = nullptr;   // Nyquist-correction accumulators [CTAs][3][n^2]
   int64_t nq_ctas = 0;       // their capacity in CTAs (the general kernel, n != 32)
-  // quadratic-form Nyquist correction (nyq_quad.cu): kernels A, B
-  // [sets][3 output planes][Nq input points][n^2 output points], f^ transposed
+  // quadratic-form Nyquist correction (nyq_quad.cu): paired kernels A~, B~
+  // [sets][3 output planes][input-point slots][n^2 output points], f^ transposed
   // within each a-plane, the partial sums of the input-point ranges;
   // nyq_path 0 uses it where built, 1 the direct kernels
   void* nq_A = nullptr;
@@ -214,6 +214,8 @@ struct pii_plan {
   void* nq_fhT = nullptr;
   void* nq_qpart = nullptr;
   int64_t nq_qpart_units = 0;  // capacity of nq_qpart in (range, cell) units of 3 n^2 points
+  void* nq_segs = nullptr;     // segments of the kernel slots: int4 (slice, kind, i1, steps) [nseg], then int j0 [nseg]
+  int nq_nseg = 0;
   int nq_npts = 0;
   int nq_slots = 0;            // resident CTAs of the correction kernel on the device
   int64_t nq_quad_bytes = 0;
