@@ -166,11 +166,13 @@ int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stalled);
  */
 int pii_plan_set_nyquist_path(pii_plan* plan, int path);
 int pii_plan_get_nyquist_path(const pii_plan* plan);
-/* Test hooks of the tensor-core kernel's bounded waits (no reference
- * counterpart): wait_limit = mbarrier polls before a role gives up (default
- * 4194304); withhold = 1 makes the TMA thread issue no copies at all, so the
- * other roles wait on barriers that nothing completes and give up, with no
- * copy or MMA in flight.  Drops captured step graphs. */
+/* Test hooks of the bounded mbarrier waits of the tensor-core column kernel
+ * and the fused cluster kernel (no reference counterpart): wait_limit = polls
+ * before a wait gives up (default 4194304); withhold = 1 makes the
+ * tensor-core kernel's TMA thread issue no copies and the fused kernel's CTAs
+ * issue no exchange stores, so the waits run out on barriers that nothing
+ * completes, with no copy, MMA or remote store in flight.  Drops captured
+ * step graphs. */
 int pii_plan_dft_test_hooks(pii_plan* plan, uint32_t wait_limit, int withhold);
 int pii_plan_get_tuning(const pii_plan* plan, int* gain_path, int* items_per_cluster, int64_t* chunk_points);
 /* Restores choices read by pii_plan_get_tuning (e.g. saved from an earlier

@@ -294,10 +294,10 @@ class Plan:
         self.restitution_sets = len(e)
 
     def dft_test_hooks(self, wait_limit=1 << 22, withhold=False):
-        """Test hooks of the tensor-core DFT's bounded waits
-        (``pii_plan_dft_test_hooks``): polls before a role gives up, and
-        whether its TMA thread withholds every copy (so the waits run out with
-        nothing in flight)."""
+        """Test hooks of the bounded waits of the tensor-core DFT and the fused
+        cluster kernel (``pii_plan_dft_test_hooks``): polls before a wait gives
+        up, and whether the copies / exchange stores are withheld (so the waits
+        run out with nothing in flight)."""
         _lib.check(self._lib.pii_plan_dft_test_hooks(self.handle, int(wait_limit), int(bool(withhold))),
                    "pii_plan_dft_test_hooks")
 
@@ -308,9 +308,9 @@ class Plan:
 
     @property
     def dft_stalled(self):
-        """True if a tensor-core DFT launch gave up waiting and the stall has
-        not been reported by a later call yet (``pii_plan_get_dft_path``;
-        synchronises)."""
+        """True if a tensor-core DFT or fused-kernel launch gave up waiting and
+        the stall has not been reported by a later call yet
+        (``pii_plan_get_dft_path``; synchronises)."""
         path, stalled = _lib.ctypes.c_int(), _lib.ctypes.c_int()
         _lib.check(self._lib.pii_plan_get_dft_path(self.handle, _lib.ctypes.byref(path), _lib.ctypes.byref(stalled)),
                    "pii_plan_get_dft_path")

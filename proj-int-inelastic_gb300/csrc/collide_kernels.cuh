@@ -390,9 +390,22 @@ __global__ void __launch_bounds__(256) k_reduce(c2<T>* G, const c2<T>* buf, int6
   if (gid >= cells * N3) return;
   const int64_t ci = gid / N3, e = gid - ci * N3;
   const V* src = buf + ci * np * N3 + e;
-  V s = first ? mk<V>(T(0), T(0)) : G[(c0 + ci) * N3 + e];
-  for (int64_t p = 0; p < np; ++p) s = cadd(s, src[p * N3]);
-  G[(c0 + ci) * N3 + e] = s;
+  // eight independent partial sums: eight loads of the chunk in flight per thread
+  V s[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) s[u] = mk<V>(T(0), T(0));
+  int64_t p = 0;
+  for (; p + 8 <= np; p += 8) {
+    V v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = src[(p + u) * N3];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s[u] = cadd(s[u], v[u]);
+  }
+  for (; p < np; ++p) s[0] = cadd(s[0], src[p * N3]);
+  V t = cadd(cadd(cadd(s[0], s[1]), cadd(s[2], s[3])), cadd(cadd(s[4], s[5]), cadd(s[6], s[7])));
+  if (!first) t = cadd(t, G[(c0 + ci) * N3 + e]);
+  G[(c0 + ci) * N3 + e] = t;
 }
 
 // ---------------------------------------------------------------------------

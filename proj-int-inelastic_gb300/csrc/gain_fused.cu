@@ -103,6 +103,7 @@ struct FusedArgs {
   float2* part;  // [clusters + cells][N3]: the gain sums of each (cluster, cell) segment
   int* err;      // mapped stall word: 3 if an exchange wait gave up
   uint32_t wait_limit;
+  int withhold;  // test hook: issue no exchange stores and no expected bytes, so every exchange wait runs out
 };
 
 __device__ __forceinline__ uint32_t fz_rank() {
@@ -245,8 +246,8 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     }
     if constexpr (CS > 1) {
       fz_wait();  // every buffer of the cluster has been read by the previous item's stage C
-      if (t == 0) mbar_arrive_tx(&bars[0], XBYTES);
-      static_for<0, CS>([&](auto ri) {
+      if (t == 0 && !a.withhold) mbar_arrive_tx(&bars[0], XBYTES);
+      if (!a.withhold) static_for<0, CS>([&](auto ri) {
         constexpr int r = decltype(ri)::value;
         const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s, uint32_t(r));
         static_for<0, NPL>([&](auto mi) {
@@ -327,8 +328,8 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       if constexpr (CS > 1) {
         const int ag = rank * NPL + pl;  // the plane's a
         fz_wait();                       // every CTA has read its planes
-        if (t == 0) mbar_arrive_tx(&bars[1], XBYTES);
-        static_for<0, CS>([&](auto ri) {
+        if (t == 0 && !a.withhold) mbar_arrive_tx(&bars[1], XBYTES);
+        if (!a.withhold) static_for<0, CS>([&](auto ri) {
           constexpr int r = decltype(ri)::value;
           const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s + 8, uint32_t(r));
           static_for<0, NPL>([&](auto mi) {
@@ -514,6 +515,7 @@ static int fused_run_t(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.part = static_cast<float2*>(p->fz_part);
   a.err = p->dft_err;
   a.wait_limit = p->dft_wait_limit;
+  a.withhold = p->dft_withhold;
   const int clusters = int(std::min<int64_t>(p->fz_clusters, cells * a.QP));
   cudaLaunchConfig_t cfg;
   cudaLaunchAttribute attr[1];

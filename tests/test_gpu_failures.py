@@ -50,6 +50,33 @@ def test_tensor_core_dft_stall_is_reported_and_recovers():
     assert rel_linf(again.cpu().numpy(), good.cpu().numpy()) < 1e-12
 
 
+def test_fused_cluster_exchange_stall_is_reported_and_recovers():
+    """The fused kernel's exchange waits (n = 48: 8-CTA clusters) give up when
+    no CTA delivers its elements (withheld: no remote store and no expected
+    byte count is issued, so nothing is in flight when the waits run out);
+    the stall is reported once by the next call, and the plan then works."""
+    pkg = _pkg()
+    cfg = op_config(48, L8_S, 2, 6, 0.7, 0.7, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    f = torch.as_tensor(maxwellian(sm.v_center, 1.0, (0.5, -0.3, 0.2), 1.3)[None], device="cuda:0")
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=1)
+    assert col.plan.tuning["gain_path"] == "fused"
+    good = col.collide(f, with_loss=True).clone()
+    assert not col.plan.dft_stalled
+    col.plan.dft_test_hooks(wait_limit=1024, withhold=True)
+    col.collide(f, with_loss=True)  # enqueued; the stall surfaces on the next call
+    torch.cuda.synchronize()
+    assert col.plan.dft_stalled
+    with pytest.raises(RuntimeError, match="gave up waiting"):
+        col.collide(f, with_loss=True)
+    assert not col.plan.dft_stalled  # reported once, then cleared
+    col.plan.dft_test_hooks()  # defaults: exchanges issued, 2^22 polls
+    again = col.collide(f, with_loss=True)
+    torch.cuda.synchronize()
+    assert not col.plan.dft_stalled
+    assert rel_linf(again.cpu().numpy(), good.cpu().numpy()) < 1e-12
+
+
 def test_step_graph_cache_is_bounded():
     pkg = _pkg()
     cfg = op_config(8, L8_S, 4, 6, 0.9, 0.9, 1.0)
