@@ -3,8 +3,8 @@
 //
 // A 2-CTA thread-block cluster owns one (cell, range of quadrature pairs).
 // CTA r (r = 0, 1) holds the a-planes [16 r, 16 r + 16) of the 32^3 work grid
-// in 128 KB of shared memory (row-swizzled: element (b, c) of a plane sits at
-// b * 32 + (c ^ b), conflict-free for row and column access).  Per pair
+// in 132 KB of shared memory (rows padded: element (b, c) of a plane sits at
+// b * 33 + c, conflict-free for row and column access).  Per pair
 // (src/collision/inelastic_collisions.py:212-217):
 //   A  column pass: P = exp_rs(k) f^ (per-axis phase rows), full 32-point
 //      inverse transform along a for the CTA's columns; keep the CTA's planes
@@ -36,7 +36,7 @@ namespace cg = cooperative_groups;
 namespace pii {
 
 namespace gc {
-constexpr size_t SMEM = size_t(PLANES) * N2 * sizeof(float2) + size_t(16) * HSLOTS * sizeof(float2);
+constexpr size_t SMEM = size_t(PLANES) * PSTR * sizeof(float2) + size_t(16) * HSLOTS * sizeof(float2);
 // index of k_a = -(2 m + par) within the parity half
 __host__ __device__ constexpr int neg_m(int m, int par) { return par == 0 ? ((16 - m) & 15) : (15 - m); }
 }  // namespace gc
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_cluster(GainClusterArgs
   using namespace gc;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* W = reinterpret_cast<float2*>(smem_raw);
-  float2* H = W + PLANES * N2;
+  float2* H = W + PLANES * PSTR;
   cg::cluster_group cluster = cg::this_cluster();
   const int crank = int(cluster.block_rank());
   const float2* Wp = cluster.map_shared_rank(W, crank ^ 1);
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_cluster(GainClusterArgs
       }
       __syncthreads();
       // ---- B: warp `warp` owns plane `warp`; lane = row / column index
-      plane_pass(W + warp * N2, fr, lane);
+      plane_pass(W + warp * PSTR, fr, lane);
       cluster.sync();  // both CTAs' planes are final for this pair
       // ---- C
       if (crank == 0)

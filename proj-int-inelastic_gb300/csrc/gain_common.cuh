@@ -1,5 +1,5 @@
 // Pieces shared by the two fused n = 32 FP32 gain kernels (gain_cluster.cu,
-// gain_parity.cu): the swizzled plane layout, the per-plane pass and the
+// gain_parity.cu): the padded plane layout, the per-plane pass and the
 // thread -> column-pair map of the Hermitian accumulator.
 #pragma once
 #include "fft_reg.cuh"
@@ -16,9 +16,11 @@ constexpr int HSLOTS = 514;
 __host__ __device__ constexpr int neg_col(int j) {
   return (((NV - (j >> 5)) & 31) << 5) | ((NV - (j & 31)) & 31);
 }
-// element (b, c) of plane `plane`: rows swizzled so that row and column
-// accesses of a warp are both free of bank conflicts
-__device__ __forceinline__ int widx(int plane, int b, int c) { return plane * N2 + b * 32 + (c ^ b); }
+// element (b, c) of plane `plane`: rows padded to 33 elements, so that row
+// and column accesses of a warp are both free of bank conflicts and every
+// element of a line sits at a constant offset from the line's start
+constexpr int RSTR = 33, PSTR = 32 * RSTR;  // row and plane strides (complex elements)
+__device__ __forceinline__ int widx(int plane, int b, int c) { return plane * PSTR + b * RSTR + c; }
 
 // One warp transforms one 32 x 32 plane in place (src/collision/
 // inelastic_collisions.py:212-214 restricted to the plane's two axes):
@@ -30,15 +32,15 @@ template <bool F_ROW = false>
 __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane) {
   float2 x[32];
 #pragma unroll
-  for (int c = 0; c < 32; ++c) x[c] = P[lane * 32 + (c ^ lane)];
+  for (int c = 0; c < 32; ++c) x[c] = P[lane * RSTR + c];
   fft_line<32, +1>(x);
   static_for<0, 32>([&](auto ci) {
     constexpr int c = decltype(ci)::value;
-    P[lane * 32 + (c ^ lane)] = x[pos(32, c)];
+    P[lane * RSTR + c] = x[pos(32, c)];
   });
   __syncwarp();
 #pragma unroll
-  for (int b = 0; b < 32; ++b) x[b] = P[b * 32 + (lane ^ b)];
+  for (int b = 0; b < 32; ++b) x[b] = P[b * RSTR + lane];
   fft_line<32, +1>(x);
   float2 y[32];
   if constexpr (F_ROW) {
@@ -59,15 +61,15 @@ __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane)
   fft_line<32, -1>(y);
   static_for<0, 32>([&](auto ki) {
     constexpr int k = decltype(ki)::value;
-    P[k * 32 + (lane ^ k)] = y[pos(32, k)];
+    P[k * RSTR + lane] = y[pos(32, k)];
   });
   __syncwarp();
 #pragma unroll
-  for (int c = 0; c < 32; ++c) x[c] = P[lane * 32 + (c ^ lane)];
+  for (int c = 0; c < 32; ++c) x[c] = P[lane * RSTR + c];
   fft_line<32, -1>(x);
   static_for<0, 32>([&](auto ki) {
     constexpr int k = decltype(ki)::value;
-    P[lane * 32 + (k ^ lane)] = x[pos(32, k)];
+    P[lane * RSTR + k] = x[pos(32, k)];
   });
 }
 

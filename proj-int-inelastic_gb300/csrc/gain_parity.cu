@@ -3,7 +3,7 @@
 // pairs), no cluster and no exchange between them.
 //
 // CTA p (p = 0, 1) owns the a-planes a = 2 m + p (m < 16) of the 32^3 work
-// grid in 128 KB of shared memory (row-swizzled as in the cluster kernel).  Per
+// grid in 132 KB of shared memory (rows padded as in the cluster kernel).  Per
 // pair (src/collision/inelastic_collisions.py:212-217):
 //   A  inverse transform along a, decimated in frequency: the parity-p outputs
 //      of a 32-point inverse DFT are the 16-point inverse DFT of
@@ -39,7 +39,7 @@ constexpr int TMEM_COLS = 512;
 // pitch: each lane of the plane pass reads its 32 values in 16-byte loads
 // without bank conflicts
 constexpr int FPITCH = 36;
-constexpr size_t FS_OFF = size_t(PLANES) * N2 * sizeof(float2);
+constexpr size_t FS_OFF = size_t(PLANES) * PSTR * sizeof(float2);
 // packed mode: the current radial node's sinc slab gsxc[r] ([153][17] floats, 16-byte padded)
 constexpr int GSC = 153 * 17;
 constexpr size_t GSC_OFF = FS_OFF + size_t(PLANES) * 32 * FPITCH * sizeof(float);
@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       }
       __syncthreads();
       // ---- B: warp `warp` owns local plane `warp` (a = 2 warp + par)
-      plane_pass<true>(W + warp * N2, fS + (warp * 32 + lane) * FPITCH, lane);
+      plane_pass<true>(W + warp * PSTR, fS + (warp * 32 + lane) * FPITCH, lane);
       if constexpr (PACK) cp_async_wait_all();  // the rows copied at the top of this pass
       __syncthreads();
       // ---- C: the thread's two columns (the previous pair's TMEM stores are complete first)
