@@ -797,6 +797,13 @@ def main():
             roof["timed_kernels"] = "gain_parity + nyq_corr (the gain term)"
             roof["note"] = ("algorithmic FLOPs of the direct method (2 * 5 N log2 N + 16 N per (cell, pair)); the "
                             "packed path evaluates antipodal pairs together and performs about half of them")
+            # the same work counted as executed: one pass per antipodal pair
+            # (half the pairs) plus the Nyquist correction's 12 FMA per
+            # (output point, input-point pair, cell), about 1.5 n^2 Nq of them
+            nq = 3 * NV * NV - 3 * NV + 1
+            exe = per_launch / 2 + 2 * 12 * 1.5 * NV * NV * nq * NX
+            roof["executed_flops_per_launch"] = exe
+            roof["executed_frac"] = exe / (gain_ms / stages[dom]["launches"] / 1e3) / 1e12 / fp32_peak
     else:
         roof["achieved"] = roof["frac"] = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
