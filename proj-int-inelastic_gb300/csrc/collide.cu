@@ -199,7 +199,8 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
       for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
         cands.push_back({path, plan->gc_items_per_cluster, pts, dft});
   }
-  if (plan->fz_clusters > 0) cands.push_back({4, plan->gc_items_per_cluster, plan->chunk_points, 0});
+  if (plan->fz_clusters > 0 && pii::gain_fused_ensure(plan) == PII_OK)
+    cands.push_back({4, plan->gc_items_per_cluster, plan->chunk_points, 0});
   const int saved_path = plan->gain_path;
   const int saved_items = plan->gc_items_per_cluster;
   const int64_t saved_points = plan->chunk_points;
@@ -278,6 +279,7 @@ extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
     pii::set_error("pii_plan_set_gain_path: the fused kernel exists for n = 16, 24, 48, 64, FP32 3D plans only");
     return PII_ERR_ARG;
   }
+  if (path == 4) PII_TRY(pii::gain_fused_ensure(plan));
   if (path == 3 && (plan->ap_count == 0 || !plan->nq_part)) {
     pii::set_error("pii_plan_set_gain_path: the packed path needs an FP32 3D plan on an antipodally symmetric design");
     return PII_ERR_ARG;

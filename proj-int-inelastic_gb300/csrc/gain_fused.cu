@@ -472,15 +472,22 @@ static int fused_prepare_t(pii_plan* p) {
   PII_TRY((fused_setup<NV, false>(&c2)));
   const int clusters = std::min(c1, c2);
   if (clusters < 1) return PII_OK;  // no cluster of this shape fits: the pipeline stays in use
-  const size_t bytes = size_t(clusters + p->batch_max) * size_t(gfu::Geo<NV>::N3) * sizeof(float2);
-  PII_CUDA(cudaMalloc(&p->fz_part, bytes));
-  p->bytes += int64_t(bytes);
-  p->fz_clusters = clusters;
+  p->fz_clusters = clusters;  // the segment sums are allocated when the path is first chosen
   if (!p->dft_err_host) {  // the mapped stall word (shared with the tensor-core column passes)
     PII_CUDA(cudaHostAlloc(&p->dft_err_host, sizeof(int), cudaHostAllocMapped));
     *p->dft_err_host = 0;
     PII_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&p->dft_err), p->dft_err_host, 0));
   }
+  return PII_OK;
+}
+
+// the per-(cluster, cell) segment sums of the fused path, allocated on first use
+int gain_fused_ensure(pii_plan* p) {
+  if (p->fz_part || p->fz_clusters < 1) return PII_OK;
+  const size_t bytes = size_t(p->fz_clusters + p->batch_max) * size_t(p->N) * sizeof(float2);
+  PII_CUDA(cudaSetDevice(p->device));
+  PII_CUDA(cudaMalloc(&p->fz_part, bytes));
+  p->bytes += int64_t(bytes);
   return PII_OK;
 }
 

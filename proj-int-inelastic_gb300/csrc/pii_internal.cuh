@@ -296,6 +296,7 @@ int nyq_gen_run(pii_plan* p, int64_t cells, cudaStream_t s);
 // nyq_quad.cu: the same correction as a quadratic form in f^ with precomputed kernels
 int nyq_quad_prepare(pii_plan* p);
 int gain_fused_prepare(pii_plan* p);
+int gain_fused_ensure(pii_plan* p);
 int gain_fused_run(pii_plan* p, int64_t cells, cudaStream_t s);
 void nyq_quad_release(pii_plan* p);
 int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s);

@@ -456,7 +456,13 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
     free_plan(p);
     return s2;
   }
-  if (p->fz_clusters > 0 && n != 64) p->gain_path = 4;  // at n = 64 the packed pipeline is faster
+  if (p->fz_clusters > 0 && n != 64) {  // at n = 64 the packed pipeline is faster
+    if ((s2 = gain_fused_ensure(p)) != PII_OK) {
+      free_plan(p);
+      return s2;
+    }
+    p->gain_path = 4;
+  }
   // the Nyquist correction: the quadratic form wherever its kernels fit the
   // memory budget (3.4x to 9x faster than the direct kernels), else the direct
   // kernels

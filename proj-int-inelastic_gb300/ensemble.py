@@ -74,6 +74,10 @@ class Ensemble:
             self._classes.append((op, F, idx))
         self._graph = None
         self._stream = torch.cuda.Stream(device=self.device)
+        # one stream per size class: the classes are independent, so their
+        # kernels run side by side (parallel branches of the captured graph),
+        # the smaller classes on the SMs the largest one leaves free
+        self._side = [torch.cuda.Stream(device=self.device) for _ in self._classes]
 
     @property
     def plan_count(self):
@@ -86,14 +90,19 @@ class Ensemble:
         self._graph = None  # a replay would run the old choices
         return out
 
-    def _launch_all(self, stream):
+    def _launch_all(self):
         v1 = np.zeros(1)
-        for op, F, idx in self._classes:
+        main = torch.cuda.current_stream(self.device)
+        for (op, F, idx), side in zip(self._classes, self._side):
+            side.wait_stream(main)
             plan = op.plan
             st = plan._lib.pii_step(plan.handle, _INT[self.integrator], F.data_ptr(), len(idx), self.dt,
                                     _lib.iptr(self.K), _lib.dptr(self.h), 1, 0.0, _lib.dptr(v1), _lib.BC_EXTRAP,
-                                    _lib.BC_EXTRAP, self.kn, int(self.with_loss), int(self.mass_fix), 0, stream)
+                                    _lib.BC_EXTRAP, self.kn, int(self.with_loss), int(self.mass_fix), 0,
+                                    side.cuda_stream)
             _lib.check(st, "pii_step")
+        for side in self._side:
+            main.wait_stream(side)
 
     def step(self, use_graph=True):
         """One macro-step of every instance (one CUDA-graph launch after the first call)."""
@@ -101,12 +110,12 @@ class Ensemble:
         self._stream.wait_stream(cur)
         with torch.cuda.stream(self._stream):
             if not use_graph:
-                self._launch_all(self._stream.cuda_stream)
+                self._launch_all()
             else:
                 if self._graph is None:
                     g = torch.cuda.CUDAGraph()
                     with torch.cuda.graph(g, stream=self._stream):
-                        self._launch_all(torch.cuda.current_stream(self.device).cuda_stream)
+                        self._launch_all()
                     self._graph = g
                 self._graph.replay()
         cur.wait_stream(self._stream)
