@@ -129,3 +129,22 @@ def test_fused_kernel_unpacked_design(n):
     qd = qd.cpu().numpy()
     for c in range(2):
         assert rel_linf(qf[c], qd[c]) < TOL and rel_linf(qp[c], qd[c]) < TOL, c
+
+
+def test_fused_path_rules():
+    """The fused kernel exists for FP32 3D plans of n = 16, 24, 48, 64; other
+    plans refuse it with ValueError and keep their kernel choice."""
+    import proj_int_inelastic_gb300 as pkg
+
+    for n, precision in ((32, "mixed"), (8, "mixed"), (16, "double")):
+        cfg = op_config(n, L8_S, 2, 6, 0.9, 0.9, 1.0)
+        col = pkg.FSInelasticVHSCollision(cfg, pkg.SpectralMesh(cfg), precision=precision, batch_max=1)
+        before = col.plan.tuning["gain_path"]
+        with pytest.raises(ValueError):
+            col.plan.set_tuning("fused", 6, 131072)
+        assert col.plan.tuning["gain_path"] == before
+    cfg = op_config(64, L8_S, 2, 6, 0.9, 0.9, 1.0)
+    col = pkg.FSInelasticVHSCollision(cfg, pkg.SpectralMesh(cfg), precision="mixed", batch_max=2)
+    assert col.plan.tuning["gain_path"] == "packed"  # the 64^3 default; the fused kernel on request
+    col.plan.set_tuning("fused", 6, 131072)
+    assert col.plan.tuning["gain_path"] == "fused"
