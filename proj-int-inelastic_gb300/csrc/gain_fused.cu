@@ -76,15 +76,23 @@ struct Geo {
   static constexpr int M1 = 3 * (NV / 2) * (NV / 2) + 1;
   static constexpr size_t SLAB_OFF = ROW_OFF + size_t(6 * NV) * sizeof(float2);
   static constexpr size_t BAR_OFF = (SLAB_OFF + size_t(M1) * sizeof(float) + 15) / 16 * 16;
-  static constexpr size_t SMEM = BAR_OFF + 16 + 16;  // two mbarriers, the tensor-memory slot
   static constexpr int WARPS = THREADS / 32;
-  static constexpr int TCOLS_USED = ((WARPS + 3) / 4) * 2 * NV;
-  static constexpr int TCOLS = TCOLS_USED <= 32    ? 32
-                               : TCOLS_USED <= 64  ? 64
-                               : TCOLS_USED <= 128 ? 128
-                               : TCOLS_USED <= 256 ? 256
-                                                   : 512;
+  static constexpr int REGIONS = (WARPS + 3) / 4;  // column groups of 2 n tensor-memory columns
+  static constexpr int TCOLS_USED = REGIONS * 2 * NV;
+  // the gain sums, then (where they fit) each column's spectrum: region REGIONS + warp / 4
+  static constexpr int TCOLS_ALL = 2 * TCOLS_USED;
+  static constexpr int TCOLS = TCOLS_ALL <= 32    ? 32
+                               : TCOLS_ALL <= 64  ? 64
+                               : TCOLS_ALL <= 128 ? 128
+                               : TCOLS_ALL <= 256 ? 256
+                                                  : 512;
   static constexpr int CHUNKS = 2 * NV / 16;  // 16-column tensor-memory chunks of a thread's sum
+  // warps from FW0 on find no tensor-memory region for their columns' spectra
+  // (n = 48: the ninth) and keep them in shared memory, [a][lane] per warp
+  static constexpr int FW0 = (TCOLS / (2 * NV) - REGIONS) * 4;
+  static constexpr int SMW = WARPS > FW0 ? WARPS - FW0 : 0;
+  static constexpr size_t FSM_OFF = BAR_OFF + 16 + 16;  // after two mbarriers and the tensor-memory slot
+  static constexpr size_t SMEM = FSM_OFF + size_t(SMW) * 32 * NV * sizeof(float2);
   static_assert(THREADS % 32 == 0 && NV % CS == 0 && TCOLS_USED <= 512 && (2 * NV) % 16 == 0, "launch shape");
   static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
 };
@@ -168,6 +176,12 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
   tm_fence_after();
   const uint32_t tbase = *tslot;
   const uint32_t treg = tbase + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 2 * NV);
+  // the column's spectrum f^(a, j), a < n, in tensor memory for a cell's whole
+  // range of passes, where a region is left for the warp (n = 48: not for the
+  // ninth warp, which reads it from L2 every pass)
+  const bool f_tm = warp < G::FW0;
+  const uint32_t freg = treg + uint32_t(G::REGIONS * 2 * NV);
+  float2* fsm = reinterpret_cast<float2*>(smem_raw + G::FSM_OFF) + (f_tm ? 0 : (warp - G::FW0) * 32 * NV) + (t & 31);
   // stages A and C: this thread's column (jb, jc), jb in the CTA's rows;
   // stage B: plane pl = t / NV of the CTA, line l = t mod NV (the same numbers)
   const int pl = t / NV, l = t - pl * NV;
@@ -215,6 +229,25 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       for (int i = 0; i < 16; ++i) z[i] = 0u;
 #pragma unroll
       for (int c = 0; c < G::CHUNKS; ++c) tm_st16(treg + 16 * c, z);
+      if (f_tm) {  // the column's spectrum, chunk c = a in [8 c, 8 c + 8)
+        const float2* fh = a.fhat + cell * N3 + j;
+#pragma unroll
+        for (int c = 0; c < G::CHUNKS; ++c) {
+          uint32_t r[16];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const float2 v = fh[int64_t(8 * c + i) * N2];
+            r[2 * i] = __float_as_uint(v.x);
+            r[2 * i + 1] = __float_as_uint(v.y);
+          }
+          tm_st16(freg + 16 * c, r);
+        }
+        tm_wait_st();
+      } else {  // the thread's own entries of its warp's shared-memory copy
+        const float2* fh = a.fhat + cell * N3 + j;
+#pragma unroll 4
+        for (int q = 0; q < NV; ++q) fsm[q * 32] = fh[int64_t(q) * N2];
+      }
       // f of the CTA's planes (read in stage B after the exchange barrier below)
       const float* fc = a.fT + cell * N3 + int64_t(rank * NPL) * N2;
       for (int e = t; e < NPL * N2; e += G::THREADS) {
@@ -227,7 +260,26 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     float2 x[NV];
     // ---- A: phase product and inverse transform along a of the column
     {
-      const float2* fh = a.fhat + cell * N3 + j;
+      if (f_tm) {  // two 16-column chunks in flight at a time (the last alone when their count is odd)
+        static_for<0, (G::CHUNKS + 1) / 2>([&](auto ci) {
+          constexpr int c = 2 * decltype(ci)::value;
+          constexpr bool two = c + 1 < G::CHUNKS;
+          uint32_t r0[16], r1[16];
+          tm_ld16(freg + 16 * c, r0);
+          if constexpr (two) tm_ld16(freg + 16 * c + 16, r1);
+          tm_wait_ld(r0);
+          if constexpr (two) tm_wait_ld(r1);
+          static_for<0, 8>([&](auto ii) {
+            constexpr int i = decltype(ii)::value;
+            x[8 * c + i] = make_float2(__uint_as_float(r0[2 * i]), __uint_as_float(r0[2 * i + 1]));
+            if constexpr (two)
+              x[8 * c + 8 + i] = make_float2(__uint_as_float(r1[2 * i]), __uint_as_float(r1[2 * i + 1]));
+          });
+        });
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = fsm[q * 32];
+      }
       const float2* ep = erow;
       if constexpr (PACK) {
         float cp, cm, th;
@@ -235,12 +287,12 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
           const float2 e = ep[q];
-          x[q] = cscale(fh[q * N2], q == H ? th : fmaf(e.y, cm, e.x * cp));
+          x[q] = cscale(x[q], q == H ? th : fmaf(e.y, cm, e.x * cp));
         }
       } else {
         const float2 ebc = cmul(ep[NV + jb], ep[2 * NV + jc]);
 #pragma unroll
-        for (int q = 0; q < NV; ++q) x[q] = cmul(fh[q * N2], cmul(ep[q], ebc));
+        for (int q = 0; q < NV; ++q) x[q] = cmul(x[q], cmul(ep[q], ebc));
       }
       fft_line<NV, +1>(x);
     }
