@@ -21,10 +21,13 @@
 // a buffer still being read.  The phase and gain rows of a pass and the sinc
 // row of its radial node are copied to shared memory by cp.async one stage
 // ahead of their use.
-// The gain sum of the CTA's columns, n k_a values each (n = 64: 64 KB per
-// CTA ... 110 KB at n = 48), lives in tensor memory for all the items of a
-// cell; at the end of a cell's range the CTA writes it to a per-part slot,
-// and k_fused_expand adds the parts of each cell into G.  Antipodally
+// The gain sum of the CTA's columns, n k_a values each (110 KB per CTA at
+// n = 48, 131 KB at n = 64), lives in tensor memory for all the items of a
+// cell, next to the columns' spectra f^(a, j), which are the same for every
+// pass of the cell (copied there once per cell; at n = 48 the ninth warp,
+// which finds no region left, keeps them in shared memory).  At the end of a
+// cell's range the CTA writes its sums to a per-part slot, and
+// k_fused_expand adds the parts of each cell into G.  Antipodally
 // symmetric designs run the packed passes (real phase t, real coefficient
 // 2 s; pack.cuh), followed by the Nyquist correction.
 #include <algorithm>
