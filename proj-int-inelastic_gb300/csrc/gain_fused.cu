@@ -10,7 +10,7 @@
 // A cluster of CS CTAs holds the item: CTA r owns the a-planes
 // [r NPL, (r + 1) NPL) in stage B and the columns (b, c) with b in the same
 // range in stages A and C (NPL = n / CS; n = 16, 24: CS = 1, the item fits one
-// CTA; n = 48: CS = 8; n = 64: CS = 16).  Between the layouts each thread
+// CTA; n = 48: CS = 6; n = 64: CS = 16).  Between the layouts each thread
 // stores its line straight into the owning CTA's shared memory with st.async,
 // which counts the bytes on the receiver's mbarrier: a column's n values go to
 // the n / NPL plane owners, a plane column's n values to the column owners,
@@ -21,11 +21,14 @@
 // a buffer still being read.  The phase and gain rows of a pass and the sinc
 // row of its radial node are copied to shared memory by cp.async one stage
 // ahead of their use.
-// The gain sum of the CTA's columns, n k_a values each (110 KB per CTA at
+// The gain sum of the CTA's columns, n k_a values each (147 KB per CTA at
 // n = 48, 131 KB at n = 64), lives in tensor memory for all the items of a
 // cell, next to the columns' spectra f^(a, j), which are the same for every
-// pass of the cell (copied there once per cell; at n = 48 the ninth warp,
-// which finds no region left, keeps them in shared memory).  At the end of a
+// pass of the cell (copied there once per cell).  At n = 48 f of the CTA's
+// planes takes the rest of tensor memory instead, one row per plane line, so
+// that the CTA's shared memory holds only its planes: the spectra of five
+// warps are kept in the shared memory left over, the other seven warps read
+// theirs from L2 every pass.  At the end of a
 // cell's range the CTA writes its sums to a per-part slot, and
 // k_fused_expand adds the parts of each cell into G.  Antipodally
 // symmetric designs run the packed passes (real phase t, real coefficient
@@ -43,21 +46,27 @@ namespace pii {
 namespace gfu {
 template <int NV>
 struct Cfg;
+// CS: CTAs of a cluster; F_TM: f of the CTA's planes in tensor memory (one
+// n-column row per plane line) instead of shared memory
 template <>
 struct Cfg<16> {
   static constexpr int CS = 1;
+  static constexpr bool F_TM = false;
 };
 template <>
 struct Cfg<24> {
   static constexpr int CS = 1;
+  static constexpr bool F_TM = false;
 };
 template <>
-struct Cfg<48> {
-  static constexpr int CS = 8;
+struct Cfg<48> {  // 6 CTAs of 12 warps: three 6-CTA clusters per 19-SM GPC
+  static constexpr int CS = 6;
+  static constexpr bool F_TM = true;
 };
 template <>
 struct Cfg<64> {
   static constexpr int CS = 16;
+  static constexpr bool F_TM = false;
 };
 
 template <int NV>
@@ -71,33 +80,49 @@ struct Geo {
   static constexpr int PLANE = NPL * NV * LD;
   static constexpr int COLS = NV * NCOL;
   static constexpr int BUF = PLANE > COLS ? PLANE : COLS;
+  static constexpr bool F_TM = Cfg<NV>::F_TM;
   static constexpr size_t F_OFF = size_t(BUF) * sizeof(float2);
   // f of the CTA's planes, rows padded to LD floats (the row pass reads
-  // f[pl][b][c] for one c across lanes of consecutive b)
-  static constexpr size_t ROW_OFF = F_OFF + size_t(NPL) * NV * LD * sizeof(float);
+  // f[pl][b][c] for one c across lanes of consecutive b), unless in tensor memory
+  static constexpr size_t ROW_OFF = F_OFF + (F_TM ? 0 : size_t(NPL) * NV * LD * sizeof(float));
   // the pass's phase row and gain row (3 n complex each), the radial node's sinc row
+  // (n = 48: entry m = |k|^2 at m + m / 32; the lanes of a warp gather at
+  // |k|^2 values that differ by squares, which fall into few banks without the
+  // pad word: 5.5 wavefronts per gather, 2.3 with it.  At n = 64, 8 and 2.7,
+  // but the index arithmetic adds spills at 255 registers: 8 % slower)
   static constexpr int M1 = 3 * (NV / 2) * (NV / 2) + 1;
+  static constexpr bool SLAB_PAD = NV == 48;
+  static constexpr int M1P = SLAB_PAD ? M1 + M1 / 32 + 1 : M1;
+  __host__ __device__ static constexpr int slab_at(int m) { return SLAB_PAD ? m + (m >> 5) : m; }
   static constexpr size_t SLAB_OFF = ROW_OFF + size_t(6 * NV) * sizeof(float2);
-  static constexpr size_t BAR_OFF = (SLAB_OFF + size_t(M1) * sizeof(float) + 15) / 16 * 16;
+  static constexpr size_t BAR_OFF = (SLAB_OFF + size_t(M1P) * sizeof(float) + 15) / 16 * 16;
   static constexpr int WARPS = THREADS / 32;
   static constexpr int REGIONS = (WARPS + 3) / 4;  // column groups of 2 n tensor-memory columns
   static constexpr int TCOLS_USED = REGIONS * 2 * NV;
-  // the gain sums, then (where they fit) each column's spectrum: region REGIONS + warp / 4
-  static constexpr int TCOLS_ALL = 2 * TCOLS_USED;
+  // then the f rows of the plane lines (F_TM): column FCOL0 + (warp / 4) n
+  static constexpr int FCOL0 = TCOLS_USED;
+  static constexpr int TCOLS_F = TCOLS_USED + (F_TM ? REGIONS * NV : 0);
+  // then (where they fit) each column's spectrum: region (warp / 4) of 2 n columns
+  static constexpr int TCOLS_ALL = TCOLS_F + TCOLS_USED;
   static constexpr int TCOLS = TCOLS_ALL <= 32    ? 32
                                : TCOLS_ALL <= 64  ? 64
                                : TCOLS_ALL <= 128 ? 128
                                : TCOLS_ALL <= 256 ? 256
                                                   : 512;
+  static constexpr int SCOL0 = TCOLS_F;
   static constexpr int CHUNKS = 2 * NV / 16;  // 16-column tensor-memory chunks of a thread's sum
-  // warps from FW0 on find no tensor-memory region for their columns' spectra
-  // (n = 48: the ninth) and keep them in shared memory, [a][lane] per warp
-  static constexpr int FW0 = (TCOLS / (2 * NV) - REGIONS) * 4;
-  static constexpr int SMW = WARPS > FW0 ? WARPS - FW0 : 0;
+  // warps from FW0 on find no tensor-memory region for their columns' spectra;
+  // the next SMW keep them in shared memory, [a][lane] per warp, as many as
+  // fit, and the rest read them from L2 every pass
+  static constexpr int FW0_ = (TCOLS - TCOLS_F) / (2 * NV) * 4;
+  static constexpr int FW0 = FW0_ < WARPS ? FW0_ : WARPS;
   static constexpr size_t FSM_OFF = BAR_OFF + 16 + 16;  // after two mbarriers and the tensor-memory slot
+  static constexpr size_t SMEM_MAX = 227 * 1024;
+  static constexpr int SMW_FIT = int((SMEM_MAX - FSM_OFF) / (32 * NV * sizeof(float2)));
+  static constexpr int SMW = WARPS - FW0 < SMW_FIT ? WARPS - FW0 : SMW_FIT;
   static constexpr size_t SMEM = FSM_OFF + size_t(SMW) * 32 * NV * sizeof(float2);
-  static_assert(THREADS % 32 == 0 && NV % CS == 0 && TCOLS_USED <= 512 && (2 * NV) % 16 == 0, "launch shape");
-  static_assert(SMEM <= 227 * 1024, "shared memory of one CTA");
+  static_assert(THREADS % 32 == 0 && NV % CS == 0 && TCOLS_F <= 512 && (2 * NV) % 16 == 0, "launch shape");
+  static_assert(SMEM <= SMEM_MAX && FSM_OFF <= SMEM_MAX, "shared memory of one CTA");
 };
 }  // namespace gfu
 
@@ -179,12 +204,15 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
   tm_fence_after();
   const uint32_t tbase = *tslot;
   const uint32_t treg = tbase + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 2 * NV);
-  // the column's spectrum f^(a, j), a < n, in tensor memory for a cell's whole
-  // range of passes, where a region is left for the warp (n = 48: not for the
-  // ninth warp, which reads it from L2 every pass)
-  const bool f_tm = warp < G::FW0;
-  const uint32_t freg = treg + uint32_t(G::REGIONS * 2 * NV);
-  float2* fsm = reinterpret_cast<float2*>(smem_raw + G::FSM_OFF) + (f_tm ? 0 : (warp - G::FW0) * 32 * NV) + (t & 31);
+  // the column's spectrum f^(a, j), a < n, for a cell's whole range of
+  // passes: in tensor memory where a region is left for the warp, else in
+  // shared memory where room is left, else read from L2 every pass
+  const bool f_tm = G::FW0 >= G::WARPS || warp < G::FW0;
+  const bool f_sm = !f_tm && (G::FW0 + G::SMW >= G::WARPS || warp < G::FW0 + G::SMW);
+  const uint32_t freg = tbase + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(G::SCOL0 + (warp >> 2) * 2 * NV);
+  float2* fsm = reinterpret_cast<float2*>(smem_raw + G::FSM_OFF) + (f_sm ? (warp - G::FW0) * 32 * NV : 0) + (t & 31);
+  // f of the plane line (pl, l) in tensor memory (F_TM)
+  const uint32_t frow = tbase + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(G::FCOL0 + (warp >> 2) * NV);
   // stages A and C: this thread's column (jb, jc), jb in the CTA's rows;
   // stage B: plane pl = t / NV of the CTA, line l = t mod NV (the same numbers)
   const int pl = t / NV, l = t - pl * NV;
@@ -246,16 +274,32 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
           tm_st16(freg + 16 * c, r);
         }
         tm_wait_st();
-      } else {  // the thread's own entries of its warp's shared-memory copy
+      } else if (f_sm) {  // the thread's own entries of its warp's shared-memory copy
         const float2* fh = a.fhat + cell * N3 + j;
 #pragma unroll 4
         for (int q = 0; q < NV; ++q) fsm[q * 32] = fh[int64_t(q) * N2];
       }
       // f of the CTA's planes (read in stage B after the exchange barrier below)
       const float* fc = a.fT + cell * N3 + int64_t(rank * NPL) * N2;
-      for (int e = t; e < NPL * N2; e += G::THREADS) {
-        const int p2 = e / N2, rem = e - p2 * N2, b = rem / NV, c = rem - b * NV;
-        fS[(p2 * NV + b) * LD + c] = fc[e];
+      if constexpr (G::F_TM) {  // the thread's plane line, n / 16 chunks of 16 columns
+        const float4* fl = reinterpret_cast<const float4*>(fc + (pl * NV + l) * NV);
+#pragma unroll
+        for (int c = 0; c < NV / 16; ++c) {
+          uint32_t r[16];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float4 v = fl[4 * c + i];
+            r[4 * i] = __float_as_uint(v.x), r[4 * i + 1] = __float_as_uint(v.y);
+            r[4 * i + 2] = __float_as_uint(v.z), r[4 * i + 3] = __float_as_uint(v.w);
+          }
+          tm_st16(frow + 16 * c, r);
+        }
+        tm_wait_st();
+      } else {
+        for (int e = t; e < NPL * N2; e += G::THREADS) {
+          const int p2 = e / N2, rem = e - p2 * N2, b = rem / NV, c = rem - b * NV;
+          fS[(p2 * NV + b) * LD + c] = fc[e];
+        }
       }
       cur = cell;
     }
@@ -279,9 +323,13 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
               x[8 * c + 8 + i] = make_float2(__uint_as_float(r1[2 * i]), __uint_as_float(r1[2 * i + 1]));
           });
         });
-      } else {
+      } else if (f_sm) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) x[q] = fsm[q * 32];
+      } else {
+        const float2* fh = a.fhat + cur * N3 + j;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) x[q] = fh[int64_t(q) * N2];
       }
       const float2* ep = erow;
       if constexpr (PACK) {
@@ -336,7 +384,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       const int64_t key = a.gs_stride ? cell * 65536 + ir : ir;
       if (key != slab_key) {
         const float* src = a.gsinc + cell * a.gs_stride + int64_t(ir) * (a.M + 1);
-        for (int e = t; e < G::M1; e += G::THREADS) cp_async4(slab + e, src + e);
+        for (int e = t; e < G::M1; e += G::THREADS) cp_async4(slab + G::slab_at(e), src + e);
         slab_key = key;
       }
       cp_async_commit();
@@ -357,15 +405,28 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     // inverse along c, * f, forward along c (row (pl, l))
     {
       float2* row = buf + (pl * NV + l) * LD;
-      const float* fr = fS + (pl * NV + l) * LD;
 #pragma unroll
       for (int c = 0; c < NV; ++c) x[c] = row[c];
       fft_line<NV, +1>(x);
       float2 y[NV];
-      static_for<0, NV>([&](auto ci) {
-        constexpr int c = decltype(ci)::value;
-        y[c] = cscale(x[pos(NV, c)], fr[c]);
-      });
+      if constexpr (G::F_TM) {
+        static_for<0, NV / 16>([&](auto ci) {
+          constexpr int c = decltype(ci)::value;
+          uint32_t r[16];
+          tm_ld16(frow + 16 * c, r);
+          tm_wait_ld(r);
+          static_for<0, 16>([&](auto ii) {
+            constexpr int i = decltype(ii)::value;
+            y[16 * c + i] = cscale(x[pos(NV, 16 * c + i)], __uint_as_float(r[i]));
+          });
+        });
+      } else {
+        const float* fr = fS + (pl * NV + l) * LD;
+        static_for<0, NV>([&](auto ci) {
+          constexpr int c = decltype(ci)::value;
+          y[c] = cscale(x[pos(NV, c)], fr[c]);
+        });
+      }
       fft_line<NV, -1>(y);
       static_for<0, NV>([&](auto ci) {
         constexpr int c = decltype(ci)::value;
@@ -414,7 +475,9 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       }
       fft_line<NV, -1>(x);
       const float2* gp = grow;
-      const float* gs = slab + mbc;
+      auto gs = [&](int kk) {
+        return slab[G::slab_at(mbc + kk)];
+      };
       float2 v[NV];
       if constexpr (PACK) {
         float dp, dm, sh;
@@ -424,14 +487,14 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
           constexpr int kq = kval(q, NV);
           const float2 g = gp[q];
           const float sv = q == H ? sh : fmaf(-g.y, dm, g.x * dp);
-          v[q] = cscale(x[pos(NV, q)], 2.f * sv * gs[kq * kq]);
+          v[q] = cscale(x[pos(NV, q)], 2.f * sv * gs(kq * kq));
         });
       } else {
         const float2 gbc = cmul(gp[NV + jb], gp[2 * NV + jc]);
         static_for<0, NV>([&](auto qi) {
           constexpr int q = decltype(qi)::value;
           constexpr int kq = kval(q, NV);
-          v[q] = cmul(x[pos(NV, q)], cscale(cmul(gp[q], gbc), gs[kq * kq]));
+          v[q] = cmul(x[pos(NV, q)], cscale(cmul(gp[q], gbc), gs(kq * kq)));
         });
       }
       tm_wait_st();

@@ -51,7 +51,7 @@ def test_tensor_core_dft_stall_is_reported_and_recovers():
 
 
 def test_fused_cluster_exchange_stall_is_reported_and_recovers():
-    """The fused kernel's exchange waits (n = 48: 8-CTA clusters) give up when
+    """The fused kernel's exchange waits (n = 48: 6-CTA clusters) give up when
     no CTA delivers its elements (withheld: no remote store and no expected
     byte count is issued, so nothing is in flight when the waits run out);
     the stall is reported once by the next call, and the plan then works."""
