@@ -116,11 +116,65 @@ template <typename V> PII_HD V cfma(V a, V b, V acc) {
   return mk<V>(acc.x + a.x * b.x - a.y * b.y, acc.y + a.x * b.y + a.y * b.x);
 }
 template <typename V> PII_HD V cscale(V a, decltype(V::x) s) { return mk<V>(a.x * s, a.y * s); }
+
 // multiply by DIR * i  (DIR = +1: i, DIR = -1: -i)
 template <int DIR, typename V> PII_HD V mul_i(V a) {
   if constexpr (DIR > 0) return mk<V>(-a.y, a.x);
   else return mk<V>(a.y, -a.x);
 }
+
+// Butterfly arithmetic of the FP32 transforms on the packed FP32x2 pipe
+// (add / sub / fma .f32x2: one instruction for both components of a complex
+// value, rounded like the scalar instructions).  Device code only; the host
+// and FP64 paths use the scalar helpers above.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned long long f2pk(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2up(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2pk(a)), "l"(f2pk(b)));
+  return f2up(d);
+}
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2pk(a)), "l"(f2pk(b)));
+  return f2up(d);
+}
+// a * b + c, componentwise
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2pk(a)), "l"(f2pk(b)), "l"(f2pk(c)));
+  return f2up(d);
+}
+#define PII_F32X2 1
+#else
+#define PII_F32X2 0
+#endif
+// butterfly sum / difference: packed on the device for float2 when PK (the
+// pairing constraint of the packed operands costs registers, so each kernel
+// chooses: faster where registers are left, slower where they are not)
+template <bool PK, typename V> PII_HD V bsum(V a, V b) {
+#if PII_F32X2
+  if constexpr (PK && std::is_same_v<V, float2>) return f2add(a, b);
+#endif
+  return cadd(a, b);
+}
+template <bool PK, typename V> PII_HD V bdif(V a, V b) {
+#if PII_F32X2
+  if constexpr (PK && std::is_same_v<V, float2>) return f2sub(a, b);
+#endif
+  return csub(a, b);
+}
+// a + DIR * i * d (scalar: the packed form would need d's components swapped)
+template <int DIR, typename V> PII_HD V b_add_i(V a, V d) { return cadd(a, mul_i<DIR>(d)); }
 
 // multiply by exp(DIR * 2 pi i * num / den) with compile-time constants
 template <long long NUM, long long DEN, int DIR, typename V>
@@ -172,20 +226,20 @@ PII_CX int pos(int n, int k) {
 }
 
 // small DFTs on y[0..R-1] (in place, natural order in and out)
-template <int R, int DIR, typename V>
+template <int R, int DIR, bool PK = false, typename V>
 PII_HD void small_dft(V* y) {
   using S = decltype(V::x);
   if constexpr (R == 2) {
     V a = y[0], b = y[1];
-    y[0] = cadd(a, b);
-    y[1] = csub(a, b);
+    y[0] = bsum<PK>(a, b);
+    y[1] = bdif<PK>(a, b);
   } else if constexpr (R == 4) {
-    V a0 = cadd(y[0], y[2]), a1 = csub(y[0], y[2]);
-    V b0 = cadd(y[1], y[3]), b1 = mul_i<DIR>(csub(y[1], y[3]));
-    y[0] = cadd(a0, b0);
-    y[2] = csub(a0, b0);
-    y[1] = cadd(a1, b1);
-    y[3] = csub(a1, b1);
+    V a0 = bsum<PK>(y[0], y[2]), a1 = bdif<PK>(y[0], y[2]);
+    V b0 = bsum<PK>(y[1], y[3]), d = bdif<PK>(y[1], y[3]);
+    y[0] = bsum<PK>(a0, b0);
+    y[2] = bdif<PK>(a0, b0);
+    y[1] = b_add_i<DIR>(a1, d);
+    y[3] = b_add_i<-DIR>(a1, d);
   } else {  // R == 3
     constexpr S c = S(-0.5);
     constexpr S s = S(DIR * 0.86602540378443864676372317075293618);
@@ -202,7 +256,7 @@ PII_HD void small_dft(V* y) {
 }
 
 // in-place DIF on x[O + S*j], j in [0, N)
-template <int N, int S, int O, int DIR, typename V>
+template <int N, int S, int O, int DIR, bool PK = false, typename V>
 PII_HD void dif(V* x) {
   if constexpr (N > 1) {
     constexpr int R = pick_radix(N);
@@ -214,7 +268,7 @@ PII_HD void dif(V* x) {
         constexpr int j = decltype(ji)::value;
         y[j] = x[O + S * (m + j * M)];
       });
-      small_dft<R, DIR>(y);
+      small_dft<R, DIR, PK>(y);
       static_for<0, R>([&](auto qi) {
         constexpr int q = decltype(qi)::value;
         x[O + S * (m + q * M)] = twiddle<(long long)m * q, N, DIR>(y[q]);
@@ -222,15 +276,16 @@ PII_HD void dif(V* x) {
     });
     static_for<0, R>([&](auto qi) {
       constexpr int q = decltype(qi)::value;
-      dif<M, S, O + S * q * M, DIR>(x);
+      dif<M, S, O + S * q * M, DIR, PK>(x);
     });
   }
 }
 
-// Full line transform; on return x[pos(N,k)] holds X[k].
-template <int N, int DIR, typename V>
+// Full line transform; on return x[pos(N,k)] holds X[k].  PK: the radix-2 / 4
+// butterflies' sums and differences on the packed FP32x2 pipe (FP32 only).
+template <int N, int DIR, bool PK = false, typename V>
 PII_HD void fft_line(V* x) {
-  dif<N, 1, 0, DIR>(x);
+  dif<N, 1, 0, DIR, PK>(x);
 }
 
 // Re-order a transformed line into natural order (compile-time register renaming).
