@@ -28,12 +28,12 @@ __device__ __forceinline__ int widx(int plane, int b, int c) { return plane * PS
 // F_ROW = false: `fr` points at f[a][0][lane] in global memory (row stride 32);
 // F_ROW = true: `fr` points at this lane's 32 values f[a][0..31][lane],
 // contiguous and 16-byte aligned (shared memory).
-template <bool F_ROW = false>
+template <bool F_ROW = false, bool PK = false>
 __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane) {
   float2 x[32];
 #pragma unroll
   for (int c = 0; c < 32; ++c) x[c] = P[lane * RSTR + c];
-  fft_line<32, +1>(x);
+  fft_line<32, +1, PK>(x);
   static_for<0, 32>([&](auto ci) {
     constexpr int c = decltype(ci)::value;
     P[lane * RSTR + c] = x[pos(32, c)];
@@ -41,7 +41,7 @@ __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane)
   __syncwarp();
 #pragma unroll
   for (int b = 0; b < 32; ++b) x[b] = P[b * RSTR + lane];
-  fft_line<32, +1>(x);
+  fft_line<32, +1, PK>(x);
   float2 y[32];
   if constexpr (F_ROW) {
     static_for<0, 8>([&](auto qi) {
@@ -58,7 +58,7 @@ __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane)
       y[b] = cscale(x[pos(32, b)], fr[b * 32]);
     });
   }
-  fft_line<32, -1>(y);
+  fft_line<32, -1, PK>(y);
   static_for<0, 32>([&](auto ki) {
     constexpr int k = decltype(ki)::value;
     P[k * RSTR + lane] = y[pos(32, k)];
@@ -66,7 +66,7 @@ __device__ __forceinline__ void plane_pass(float2* P, const float* fr, int lane)
   __syncwarp();
 #pragma unroll
   for (int c = 0; c < 32; ++c) x[c] = P[lane * RSTR + c];
-  fft_line<32, -1>(x);
+  fft_line<32, -1, PK>(x);
   static_for<0, 32>([&](auto ki) {
     constexpr int k = decltype(ki)::value;
     P[lane * RSTR + k] = x[pos(32, k)];

@@ -47,29 +47,30 @@ namespace gfu {
 template <int NV>
 struct Cfg;
 // CS: CTAs of a cluster; F_TM: f of the CTA's planes in tensor memory (one
-// n-column row per plane line) instead of shared memory; PK: the line
-// transforms' butterflies on the packed FP32x2 pipe
+// n-column row per plane line) instead of shared memory; PK_AC, PK_B: the line
+// transforms' butterflies on the packed FP32x2 pipe in stages A and C, in
+// stage B
 template <>
 struct Cfg<16> {
-  static constexpr bool PK = true;
+  static constexpr bool PK_AC = true, PK_B = true;
   static constexpr int CS = 1;
   static constexpr bool F_TM = false;
 };
 template <>
-struct Cfg<24> {  // packed butterflies: 4 % slower here (spills at 96 registers)
-  static constexpr bool PK = false;
+struct Cfg<24> {  // packed butterflies: 0.538 ms per Q (32 cells) instead of 0.526
+  static constexpr bool PK_AC = false, PK_B = false;
   static constexpr int CS = 1;
   static constexpr bool F_TM = false;
 };
 template <>
-struct Cfg<48> {  // 6 CTAs of 12 warps: three 6-CTA clusters per 19-SM GPC
-  static constexpr bool PK = true;
+struct Cfg<48> {  // 6 CTAs of 12 warps: three 6-CTA clusters per 19-SM GPC; 7.61 -> 7.25 ms per Q (16 cells) packed
+  static constexpr bool PK_AC = true, PK_B = true;
   static constexpr int CS = 6;
   static constexpr bool F_TM = true;
 };
 template <>
-struct Cfg<64> {  // packed butterflies: 98.5 -> 85.2 ms on 16 cells
-  static constexpr bool PK = true;
+struct Cfg<64> {  // packed butterflies: 99.5 -> 88.7 ms per Q on 16 cells (A and C alone: 88.1)
+  static constexpr bool PK_AC = true, PK_B = true;
   static constexpr int CS = 16;
   static constexpr bool F_TM = false;
 };
@@ -86,7 +87,7 @@ struct Geo {
   static constexpr int COLS = NV * NCOL;
   static constexpr int BUF = PLANE > COLS ? PLANE : COLS;
   static constexpr bool F_TM = Cfg<NV>::F_TM;
-  static constexpr bool PK = Cfg<NV>::PK;
+  static constexpr bool PK_AC = Cfg<NV>::PK_AC, PK_B = Cfg<NV>::PK_B;
   static constexpr size_t F_OFF = size_t(BUF) * sizeof(float2);
   // f of the CTA's planes, rows padded to LD floats (the row pass reads
   // f[pl][b][c] for one c across lanes of consecutive b), unless in tensor memory
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
 #pragma unroll
         for (int q = 0; q < NV; ++q) x[q] = cmul(x[q], cmul(ep[q], ebc));
       }
-      fft_line<NV, +1, G::PK>(x);
+      fft_line<NV, +1, G::PK_AC>(x);
     }
     if constexpr (CS > 1) {
       fz_wait();  // every buffer of the cluster has been read by the previous item's stage C
@@ -400,7 +401,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       float2* col = buf + pl * NV * LD + l;
 #pragma unroll
       for (int b = 0; b < NV; ++b) x[b] = col[b * LD];
-      fft_line<NV, +1, G::PK>(x);
+      fft_line<NV, +1, G::PK_B>(x);
       static_for<0, NV>([&](auto bi) {
         constexpr int b = decltype(bi)::value;
         col[b * LD] = x[pos(NV, b)];
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       float2* row = buf + (pl * NV + l) * LD;
 #pragma unroll
       for (int c = 0; c < NV; ++c) x[c] = row[c];
-      fft_line<NV, +1, G::PK>(x);
+      fft_line<NV, +1, G::PK_B>(x);
       float2 y[NV];
       if constexpr (G::F_TM) {
         static_for<0, NV / 16>([&](auto ci) {
@@ -433,7 +434,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
           y[c] = cscale(x[pos(NV, c)], fr[c]);
         });
       }
-      fft_line<NV, -1, G::PK>(y);
+      fft_line<NV, -1, G::PK_B>(y);
       static_for<0, NV>([&](auto ci) {
         constexpr int c = decltype(ci)::value;
         row[c] = y[pos(NV, c)];
@@ -446,7 +447,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
 #pragma unroll
       for (int b = 0; b < NV; ++b) x[b] = col[b * LD];
       if constexpr (CS > 1) fz_arrive();  // this thread's reads of its planes are done
-      fft_line<NV, -1, G::PK>(x);
+      fft_line<NV, -1, G::PK_B>(x);
       if constexpr (CS > 1) {
         const int ag = rank * NPL + pl;  // the plane's a
         fz_wait();                       // every CTA has read its planes
@@ -479,7 +480,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
 #pragma unroll
         for (int q = 0; q < NV; ++q) x[q] = buf[(q * NV + jb) * LD + jc];
       }
-      fft_line<NV, -1, G::PK>(x);
+      fft_line<NV, -1, G::PK_AC>(x);
       const float2* gp = grow;
       auto gs = [&](int kk) {
         return slab[G::slab_at(mbc + kk)];

@@ -31,6 +31,10 @@
 #include "tmem.cuh"
 
 namespace pii {
+// packed FP32x2 butterflies in the 16-point a-axis transforms of stages A and
+// C (16.82 instead of 17.27 ms per 128-cell launch), not in the plane pass's
+// 32-point ones (18.09 ms)
+constexpr bool PAR_PK_AC = true, PAR_PK_B = false;
 
 namespace gpar {
 using namespace gc;
@@ -95,8 +99,8 @@ __device__ __forceinline__ void par_stage_a_pair(float2* W, const float2* fh, co
     else
       u1[k1] = cmul(cfma(clo, epp[16 + k1], cmul(chi, epp[k1])), ebc1);
   });
-  fft_line<16, +1>(u0);
-  fft_line<16, +1>(u1);
+  fft_line<16, +1, PAR_PK_AC>(u0);
+  fft_line<16, +1, PAR_PK_AC>(u1);
   static_for<0, 16>([&](auto mi) {
     constexpr int m = decltype(mi)::value;
     W[widx(m, jb, jc)] = u0[pos(16, m)];
@@ -115,7 +119,7 @@ __device__ __forceinline__ void par_stage_a_col(float2* W, const float2* fh, con
   float2 u[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) u[k] = cmul(cfma(fh[(k + 16) * N2 + j], epp[16 + k], cmul(fh[k * N2 + j], epp[k])), ebc);
-  fft_line<16, +1>(u);
+  fft_line<16, +1, PAR_PK_AC>(u);
   static_for<0, 16>([&](auto mi) {
     constexpr int m = decltype(mi)::value;
     W[widx(m, jb, jc)] = u[pos(16, m)];
@@ -136,7 +140,7 @@ __device__ __forceinline__ void par_stage_c(const float2* W, int j, const float2
   float2 z[16];
 #pragma unroll
   for (int m = 0; m < 16; ++m) z[m] = W[widx(m, jb, jc)];
-  fft_line<16, -1>(z);
+  fft_line<16, -1, PAR_PK_AC>(z);
   const int kb = kval(jb, 32), kc = kval(jc, 32);
   const float4* grow = reinterpret_cast<const float4*>(gsr + (kb * kb + kc * kc) * 20);
   float g[20];
@@ -239,8 +243,8 @@ __device__ __forceinline__ void pack_stage_a_pair(float2* W, const float2* fh, c
     const float2 y1 = make_float2(A.x * ta + sg * B.x * tb, A.y * ta + sg * B.y * tb);
     u1[k1] = twiddle<PAR * k1, 32, +1>(y1);
   });
-  fft_line<16, +1>(u0);
-  fft_line<16, +1>(u1);
+  fft_line<16, +1, PAR_PK_AC>(u0);
+  fft_line<16, +1, PAR_PK_AC>(u1);
   static_for<0, 16>([&](auto mi) {
     constexpr int m = decltype(mi)::value;
     W[widx(m, jb, jc)] = u0[pos(16, m)];
@@ -263,7 +267,7 @@ __device__ __forceinline__ void pack_stage_a_col(float2* W, const float2* fh, co
     const float th = k == 0 ? c0.t16 : pack_t(ep[k + 16], c0);
     u[k] = twiddle<PAR * k, 32, +1>(make_float2(lo.x * tl + sg * hi.x * th, lo.y * tl + sg * hi.y * th));
   });
-  fft_line<16, +1>(u);
+  fft_line<16, +1, PAR_PK_AC>(u);
   static_for<0, 16>([&](auto mi) {
     constexpr int m = decltype(mi)::value;
     W[widx(m, jb, jc)] = u[pos(16, m)];
@@ -306,7 +310,7 @@ __device__ __forceinline__ void pack_stage_c(const float2* W, int j, const float
   float2 z[16];
 #pragma unroll
   for (int m = 0; m < 16; ++m) z[m] = W[widx(m, jb, jc)];
-  fft_line<16, -1>(z);
+  fft_line<16, -1, PAR_PK_AC>(z);
   float2 zw[16];
   static_for<0, 16>([&](auto ki) {
     constexpr int k = decltype(ki)::value;
@@ -484,7 +488,7 @@ __global__ void __launch_bounds__(gc::THREADS, 1) k_gain_parity(GainParityArgs a
       }
       __syncthreads();
       // ---- B: warp `warp` owns local plane `warp` (a = 2 warp + par)
-      plane_pass<true>(W + warp * PSTR, fS + (warp * 32 + lane) * FPITCH, lane);
+      plane_pass<true, PAR_PK_B>(W + warp * PSTR, fS + (warp * 32 + lane) * FPITCH, lane);
       if constexpr (PACK) cp_async_wait_all();  // the rows copied at the top of this pass
       __syncthreads();
       // ---- C: the thread's two columns (the previous pair's TMEM stores are complete first)
