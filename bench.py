@@ -575,9 +575,10 @@ def ncu_case(cells):
     return 0
 
 
-def ncu_case64(cells, dft_path):
+def ncu_case64(cells, dft_path, gain_path="packed"):
     """Small profiling case at 64^3 (the 48 x 70 quadrature, 3-Maxwellian cells): one
-    mixed-precision Q(f,f) evaluation with the given first-axis column path."""
+    mixed-precision Q(f,f) evaluation with the given first-axis column path
+    (packed pipeline) or the fused gain kernel (gain_path "fused")."""
     import torch
 
     import proj_int_inelastic_gb300 as pkg
@@ -587,11 +588,15 @@ def ncu_case64(cells, dft_path):
            "collision-model": {"dim": 3, "type": "vhs", "e": E64, "e0": E64, "gamma": 1.0}}
     sm = pkg.SpectralMesh(cfg)
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=cells)
-    col.plan.set_dft_path(dft_path)
+    if gain_path == "fused":
+        col.plan.set_tuning("fused", 6, 131072)
+    else:
+        col.plan.set_dft_path(dft_path)
     f = torch.as_tensor(mixture_states(sm.v_center, cells, 64), device="cuda:0").contiguous()
     q = col.collide(f, with_loss=True)
     torch.cuda.synchronize()
-    print(json.dumps({"ncu_case64_cells": cells, "dft_path": dft_path, "q_abs_max": float(q.abs().max()),
+    print(json.dumps({"ncu_case64_cells": cells, "dft_path": dft_path, "gain_path": col.plan.tuning["gain_path"],
+                      "q_abs_max": float(q.abs().max()),
                       "stalled": col.plan.dft_stalled}))
     return 0
 
@@ -646,6 +651,8 @@ def main():
                     help="profiling case: one 64^3 Q(f,f) evaluation on this many cells and exit")
     ap.add_argument("--dft-path", default="tensor", choices=["tensor", "fft"],
                     help="first-axis column path of the 64^3 profiling case")
+    ap.add_argument("--gain-path", default="packed", choices=["packed", "fused"],
+                    help="gain kernel of the 64^3 profiling case")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -654,7 +661,7 @@ def main():
     if args.ncu_class:
         return ncu_case_class(args.ncu_class, args.ncu_cells)
     if args.ncu_case64:
-        return ncu_case64(args.ncu_case64, args.dft_path)
+        return ncu_case64(args.ncu_case64, args.dft_path, args.gain_path)
     if args.c4_only or args.c3_only:
         import torch
 

@@ -96,7 +96,8 @@ struct Geo {
   // (n = 48: entry m = |k|^2 at m + m / 32; the lanes of a warp gather at
   // |k|^2 values that differ by squares, which fall into few banks without the
   // pad word: 5.5 wavefronts per gather, 2.3 with it.  At n = 64, 8 and 2.7,
-  // but the index arithmetic adds spills at 255 registers: 8 % slower)
+  // but the index arithmetic costs more at 255 registers: 87.6 instead of
+  // 86.2 ms per Q on 16 cells)
   static constexpr int M1 = 3 * (NV / 2) * (NV / 2) + 1;
   static constexpr bool SLAB_PAD = NV == 48;
   static constexpr int M1P = SLAB_PAD ? M1 + M1 / 32 + 1 : M1;
