@@ -154,6 +154,19 @@ int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms, void* stre
 int pii_plan_set_dft_path(pii_plan* plan, int path);
 int pii_plan_get_dft_path(const pii_plan* plan, int* path, int* stalled);
 /*
+ * Split of the fused gain path (gain path 4; no reference counterpart): the
+ * last round(fraction x cells) cells of a call (at most cells - 1) go to the
+ * packed column / plane pipeline on a stream of the plan's own, forked from
+ * and joined back into the caller's stream, while the fused kernel takes the
+ * rest.  At n = 48 and 64 the fused kernel's clusters leave SMs idle (one CTA
+ * of a cluster per SM, whole clusters per GPC), and the pipeline's kernels
+ * run there.  Needs an antipodally symmetric design; 0 (the default) turns
+ * it off.  The autotuner times shares around the idle SMs' share.  set drops
+ * captured step graphs; get returns -1 for NULL.
+ */
+int pii_plan_set_fused_split(pii_plan* plan, double fraction);
+double pii_plan_get_fused_split(const pii_plan* plan);
+/*
  * Nyquist-plane correction of the packed gain paths (no reference
  * counterpart: the packing is this library's): 0 = the quadratic form
  * C(k) = sum_q A(k, q) f^(q) f^(k - q) - B(k, q) conj f^(q) f^(k + q) with the

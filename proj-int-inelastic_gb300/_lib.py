@@ -51,6 +51,8 @@ SIGNATURES = {
     "pii_plan_set_tuning": (_c_int, [_vp, _c_int, _c_int, _c_i64]),
     "pii_plan_set_dft_path": (_c_int, [_vp, _c_int]),
     "pii_plan_get_dft_path": (_c_int, [_vp, _pint, _pint]),
+    "pii_plan_set_fused_split": (_c_int, [_vp, ctypes.c_double]),
+    "pii_plan_get_fused_split": (ctypes.c_double, [_vp]),
     "pii_plan_dft_test_hooks": (_c_int, [_vp, ctypes.c_uint32, _c_int]),
     "pii_plan_set_nyquist_path": (_c_int, [_vp, _c_int]),
     "pii_plan_get_nyquist_path": (_c_int, [_vp]),

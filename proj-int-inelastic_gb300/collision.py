@@ -254,13 +254,23 @@ class Plan:
                                                torch.cuda.current_stream().cuda_stream), "pii_plan_autotune")
         return best.value, self.tuning
 
-    def set_tuning(self, gain_path, items_per_cluster, chunk_points, dft_path=None, **_):
+    def set_tuning(self, gain_path, items_per_cluster, chunk_points, dft_path=None, fused_split=None, **_):
         """Restore choices (as returned by :attr:`tuning`), ``pii_plan_set_tuning``
-        (and ``pii_plan_set_dft_path`` when `dft_path` is given)."""
+        (and ``pii_plan_set_dft_path`` / ``pii_plan_set_fused_split`` when
+        `dft_path` / `fused_split` is given)."""
         _lib.check(self._lib.pii_plan_set_tuning(self.handle, _code(GAIN_PATHS, gain_path, "gain_path"),
                                                  int(items_per_cluster), int(chunk_points)), "pii_plan_set_tuning")
         if dft_path is not None:
             self.set_dft_path(dft_path)
+        if fused_split is not None:
+            self.set_fused_split(fused_split)
+
+    def set_fused_split(self, fraction):
+        """Share of a call's cells that the packed pipeline takes on a side
+        stream while the fused kernel runs (gain path "fused" at n = 48, 64,
+        whose clusters leave SMs idle; 0 turns it off),
+        ``pii_plan_set_fused_split``."""
+        _lib.check(self._lib.pii_plan_set_fused_split(self.handle, float(fraction)), "pii_plan_set_fused_split")
 
     def set_dft_path(self, dft_path):
         """'fft' (CUDA-core FFT) or 'tensor' (tensor-core split-FP16 DFT; n = 64
@@ -324,7 +334,8 @@ class Plan:
         dft = _lib.ctypes.c_int()
         _lib.check(self._lib.pii_plan_get_dft_path(self.handle, _lib.ctypes.byref(dft), None), "pii_plan_get_dft_path")
         return {"gain_path": {v: k for k, v in GAIN_PATHS.items()}[path.value], "items_per_cluster": items.value,
-                "chunk_points": pts.value, "dft_path": {v: k for k, v in DFT_PATHS.items()}[dft.value]}
+                "chunk_points": pts.value, "dft_path": {v: k for k, v in DFT_PATHS.items()}[dft.value],
+                "fused_split": float(self._lib.pii_plan_get_fused_split(self.handle))}
 
     @property
     def workspace_bytes(self):

@@ -1,5 +1,6 @@
 // Orchestration of one batched Q(f,f) evaluation (pii_collide) and dispatch on
 // (precision, n) to the templated kernels.
+#include <cmath>
 #include <type_traits>
 #include <vector>
 
@@ -18,11 +19,40 @@ static int finish_all(pii_plan* p, const double* f, double* q, int64_t cells, in
   return PII_OK;
 }
 
+// the pipeline's gain sums G of cells [c_lo, c_hi): (cell, pair) items, or
+// (cell, antipodal pass) items where packed; a chunk holds Cc cells x Pc of
+// them in the L2-resident buffer
+template <typename T, int NV>
+static int pipeline_gain(pii_plan* p, int64_t c_lo, int64_t c_hi, bool packed, cudaStream_t s) {
+  using K = CollideKernels<T, NV>;
+  const int64_t N = p->N, cells = c_hi - c_lo;
+  const int64_t QQ = packed ? p->ap_count : p->Q;
+  int64_t Cc = std::max<int64_t>(1, (p->chunk_points + N - 1) / N);
+  Cc = std::min<int64_t>(Cc, std::min<int64_t>(cells, p->chunk_items));
+  const int64_t Pc = std::max<int64_t>(1, std::min<int64_t>(QQ, p->chunk_items / Cc));
+  for (int64_t c0 = c_lo; c0 < c_hi; c0 += Cc) {
+    const int64_t cc = std::min(Cc, c_hi - c0);
+    for (int64_t p0 = 0; p0 < QQ; p0 += Pc) {
+      const int64_t np = std::min(Pc, QQ - p0);
+      PII_TRY(K::pairs(p, c0, cc, p0, np, p0 == 0, s, packed));
+    }
+  }
+  return PII_OK;
+}
+
+// the side stream of the fused path's split, with its fork / join events
+static int side_ready(pii_plan* p) {
+  if (p->side) return PII_OK;
+  PII_CUDA(cudaEventCreateWithFlags(&p->side_fork, cudaEventDisableTiming));
+  PII_CUDA(cudaEventCreateWithFlags(&p->side_join, cudaEventDisableTiming));
+  PII_CUDA(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+  return PII_OK;
+}
+
 template <typename T, int NV>
 static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int with_loss, double hb,
                      cudaStream_t s) {
   using K = CollideKernels<T, NV>;
-  const int64_t N = p->N;
   PII_TRY(K::fwd(p, f, 0, cells, s));
   if constexpr (std::is_same<T, float>::value && NV == 64) {
     if (p->dft_path == 1) PII_TRY(col_tc_bounds(p, cells, s));  // per-column scale bounds of f^
@@ -40,26 +70,30 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
   }
   if constexpr (std::is_same<T, float>::value && NV != 32) {
     if (p->gain_path == 4) {  // the fused kernel: every item on chip, packed where the design allows
-      PII_TRY(gain_fused_run(p, cells, s));
+      // split: the last cp cells go to the packed pipeline on a side stream,
+      // whose kernels run on the SMs that the fused kernel's clusters leave
+      // idle; the fused kernel is launched first so that its clusters are
+      // placed first
+      const bool pack_pipe = p->ap_count > 0 && p->nq_part;
+      const int64_t cp = pack_pipe && p->fz_split > 0 ? std::min<int64_t>(cells - 1, llround(p->fz_split * cells)) : 0;
+      if (cp > 0) {
+        PII_TRY(side_ready(p));
+        PII_CUDA(cudaEventRecord(p->side_fork, s));  // f^ and f of every cell are ready
+        PII_CUDA(cudaStreamWaitEvent(p->side, p->side_fork, 0));
+      }
+      PII_TRY(gain_fused_run(p, cells - cp, s));
+      if (cp > 0) {
+        PII_TRY((pipeline_gain<T, NV>(p, cells - cp, cells, true, p->side)));
+        PII_CUDA(cudaEventRecord(p->side_join, p->side));
+        PII_CUDA(cudaStreamWaitEvent(s, p->side_join, 0));
+      }
       if (p->ap_count > 0) PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_gen_run(p, cells, s));
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
   }
-  // items = (cell, pair), or (cell, antipodal pass) on the packed pipeline; a
-  // chunk holds Cc cells x Pc of them in the L2-resident buffer
   bool packed = false;
   if constexpr (std::is_same<T, float>::value && NV != 32) packed = p->gain_path == 3 && p->ap_count > 0;
-  const int64_t QQ = packed ? p->ap_count : p->Q;
-  int64_t Cc = std::max<int64_t>(1, (p->chunk_points + N - 1) / N);
-  Cc = std::min<int64_t>(Cc, std::min<int64_t>(cells, p->chunk_items));
-  const int64_t Pc = std::max<int64_t>(1, std::min<int64_t>(QQ, p->chunk_items / Cc));
-  for (int64_t c0 = 0; c0 < cells; c0 += Cc) {
-    const int64_t cc = std::min(Cc, cells - c0);
-    for (int64_t p0 = 0; p0 < QQ; p0 += Pc) {
-      const int64_t np = std::min(Pc, QQ - p0);
-      PII_TRY(K::pairs(p, c0, cc, p0, np, p0 == 0, s, packed));
-    }
-  }
+  PII_TRY((pipeline_gain<T, NV>(p, 0, cells, packed, s)));
   // what the packed passes leave out, on the Nyquist planes
   if (packed) PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_gen_run(p, cells, s));
   return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
@@ -181,15 +215,16 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
     int path, items;
     int64_t points;
     int dft;
+    double split;  // fused path: share of the cells for the packed pipeline on the idle SMs
   };
   std::vector<Cand> cands;
   const bool cluster_ok = plan->gc_clusters > 0;
   const bool cluster_path_ok = cluster_ok && plan->tab.nsets == 1;  // the cluster kernel takes one table set
   if (cluster_ok) {
     if (cluster_path_ok)
-      for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points, 0});
-    cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points, 0});  // even split: no item knob
-    if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points, 0});
+      for (int items : {2, 4, 6, 8}) cands.push_back({1, items, plan->chunk_points, 0, 0.0});
+    cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points, 0, 0.0});  // even split: no item knob
+    if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points, 0, 0.0});
   }
   // the pipeline on (cell, pair) items, and on antipodal passes where it is packed (n != 32)
   const bool pack_pipe = plan->n != 32 && plan->ap_count > 0 && plan->nq_part;
@@ -197,22 +232,35 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
     if (path == 3 && !pack_pipe) continue;
     for (int dft = 0; dft <= (plan->dft_img ? 1 : 0); ++dft)
       for (int64_t pts : {int64_t(65536), int64_t(131072), int64_t(262144), int64_t(524288)})
-        cands.push_back({path, plan->gc_items_per_cluster, pts, dft});
+        cands.push_back({path, plan->gc_items_per_cluster, pts, dft, 0.0});
   }
-  if (plan->fz_clusters > 0 && pii::gain_fused_ensure(plan) == PII_OK)
-    cands.push_back({4, plan->gc_items_per_cluster, plan->chunk_points, 0});
+  if (plan->fz_clusters > 0 && pii::gain_fused_ensure(plan) == PII_OK) {
+    cands.push_back({4, plan->gc_items_per_cluster, plan->chunk_points, 0, 0.0});
+    // where the fused kernel's clusters leave SMs idle (n = 48, 64), shares of
+    // the cells for the packed pipeline around the idle SMs' share
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, plan->device);
+    if (pack_pipe && plan->fz_sms > 0 && plan->fz_sms < sms) {
+      const double idle = double(sms - plan->fz_sms) / double(sms);
+      for (double m : {0.5, 0.75, 1.0, 1.25})
+        for (int dft = 0; dft <= (plan->dft_img ? 1 : 0); ++dft)
+          cands.push_back({4, plan->gc_items_per_cluster, 65536, dft, idle * m});
+    }
+  }
   const int saved_path = plan->gain_path;
   const int saved_items = plan->gc_items_per_cluster;
   const int64_t saved_points = plan->chunk_points;
   const int saved_dft = plan->dft_path;
+  const double saved_split = plan->fz_split;
   float best = 1e30f;
-  Cand pick{saved_path, saved_items, saved_points, saved_dft};
+  Cand pick{saved_path, saved_items, saved_points, saved_dft, saved_split};
   int st = PII_OK;
   for (const Cand& c : cands) {
     plan->gain_path = c.path;
     plan->gc_items_per_cluster = c.items;
     plan->chunk_points = c.points;
     plan->dft_path = c.dft;
+    plan->fz_split = c.split;
     st = collide_impl(plan, f, q, cells, 1, 0.0, 0, s);  // warm-up
     if (st != PII_OK) break;
     cudaEventRecord(e0, s);
@@ -239,6 +287,7 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
   plan->gc_items_per_cluster = st == PII_OK ? pick.items : saved_items;
   plan->chunk_points = st == PII_OK ? pick.points : saved_points;
   plan->dft_path = st == PII_OK ? pick.dft : saved_dft;
+  plan->fz_split = st == PII_OK ? pick.split : saved_split;
   pii::graphs_clear(plan);  // captured graphs baked the old choices in
   if (best_ms) *best_ms = best;
   return st;
@@ -295,6 +344,18 @@ extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
   plan->gain_path = path;
   return PII_OK;
 }
+
+extern "C" int pii_plan_set_fused_split(pii_plan* plan, double fraction) {
+  if (!plan || !(fraction >= 0.0 && fraction < 1.0)) {
+    pii::set_error("pii_plan_set_fused_split: fraction must be in [0, 1)");
+    return PII_ERR_ARG;
+  }
+  plan->fz_split = fraction;
+  pii::graphs_clear(plan);  // captured graphs baked the old choice in
+  return PII_OK;
+}
+
+extern "C" double pii_plan_get_fused_split(const pii_plan* plan) { return plan ? plan->fz_split : -1.0; }
 
 extern "C" int pii_plan_set_dft_path(pii_plan* plan, int path) {
   if (!plan || path < 0 || path > 1) {

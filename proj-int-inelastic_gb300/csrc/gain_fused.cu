@@ -599,6 +599,7 @@ static int fused_prepare_t(pii_plan* p) {
   const int clusters = std::min(c1, c2);
   if (clusters < 1) return PII_OK;  // no cluster of this shape fits: the pipeline stays in use
   p->fz_clusters = clusters;  // the segment sums are allocated when the path is first chosen
+  p->fz_sms = clusters * gfu::Geo<NV>::CS * (gfu::Geo<NV>::CS == 1 ? 0 : 1);  // CS = 1: the grid fills every SM
   if (!p->dft_err_host) {  // the mapped stall word (shared with the tensor-core column passes)
     PII_CUDA(cudaHostAlloc(&p->dft_err_host, sizeof(int), cudaHostAllocMapped));
     *p->dft_err_host = 0;

@@ -224,6 +224,12 @@ struct pii_plan {
   // segment sums [clusters + batch_max][n^3] and the clusters resident at once
   void* fz_part = nullptr;
   int fz_clusters = 0;
+  int fz_sms = 0;           // SMs the resident clusters fill (clusters x CTAs per cluster, one CTA per SM)
+  // share of a call's cells that the packed pipeline takes on a side stream
+  // while the fused kernel fills its SMs (pii_plan_set_fused_split; 0: none)
+  double fz_split = 0.0;
+  cudaStream_t side = nullptr;                    // created on first use
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   void* nq_ft2 = nullptr;    // general kernel: f transposed within each a-plane [batch_max][n^3] (FP32)
   void* nq_fhn = nullptr;    // general kernel: f^ at the Nyquist-plane points [batch_max][3 n^2]
   // first-axis column transforms of the n = 64 FP32 pipeline: 0 = CUDA-core

@@ -353,6 +353,9 @@ static void free_plan(pii_plan* p) {
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (p->dft_err_host) cudaFreeHost(p->dft_err_host);
+  if (p->side_fork) cudaEventDestroy(p->side_fork);
+  if (p->side_join) cudaEventDestroy(p->side_join);
+  if (p->side) cudaStreamDestroy(p->side);
   delete p;
 }
 

@@ -148,3 +148,59 @@ def test_fused_path_rules():
     assert col.plan.tuning["gain_path"] == "packed"  # the 64^3 default; the fused kernel on request
     col.plan.set_tuning("fused", 6, 131072)
     assert col.plan.tuning["gain_path"] == "fused"
+
+
+@pytest.mark.parametrize("n,nr", [(48, 3), (64, 2)])
+def test_fused_split_with_pipeline(n, nr):
+    """The fused path with a share of the cells on the packed pipeline (side
+    stream, on the SMs the fused kernel's clusters leave idle): every cell
+    against the FP64 plan, and against the unsplit fused kernel."""
+    import proj_int_inelastic_gb300 as pkg
+
+    cfg = op_config(n, L8_S, nr, 6, 0.6, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    v = sm.v_center
+    rng = np.random.default_rng(n + 1)
+    f = np.stack([maxwellian(v, 1.0, rng.uniform(-1, 1, 3), rng.uniform(0.6, 1.4)) for _ in range(4)]
+                 + [rng.uniform(0.1, 1.0, (n, n, n)) * 0.05])
+    ft = torch.as_tensor(f, device="cuda:0")
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=5)
+    col.plan.set_tuning("fused", 6, 65536)
+    assert col.plan.tuning["fused_split"] == 0.0
+    q0 = col.collide(ft, with_loss=True).cpu().numpy()
+    col.plan.set_tuning("fused", 6, 65536, fused_split=0.4)  # the last 2 of 5 cells on the pipeline
+    assert col.plan.tuning["fused_split"] == 0.4
+    q1 = col.collide(ft, with_loss=True).cpu().numpy()
+    qd = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=5).collide(ft, with_loss=True)
+    qd = qd.cpu().numpy()
+    for c in range(5):
+        assert rel_linf(q1[c], qd[c]) < TOL and rel_linf(q0[c], qd[c]) < TOL, c
+        assert rel_linf(q1[c], q0[c]) < 2e-6, c
+    with pytest.raises(ValueError):
+        col.plan.set_fused_split(1.0)
+
+
+def test_fused_split_in_captured_graph():
+    """The split's fork onto the plan's side stream and join back are captured
+    into the macro-step graph: graph replay and eager steps agree bit for bit."""
+    import proj_int_inelastic_gb300 as pkg
+
+    rng = np.random.default_rng(48)
+    configs, f0s = [], []
+    for i in range(4):
+        cfg = op_config(48, L8_S, 3, 6, float(rng.uniform(0.3, 1.0)), 0.9, 1.0)
+        v = pkg.SpectralMesh(cfg).v_center
+        configs.append(cfg)
+        f0s.append(maxwellian(v, 1.0, rng.uniform(-1, 1, 3), rng.uniform(0.7, 1.3)))
+    kw = dict(dt=0.02, kn=1.0, integrator="PFE", inner_steps=[2], inner_dt=[0.005], with_loss=True)
+    graph = pkg.Ensemble(configs, f0s, precision="mixed", **kw)
+    eager = pkg.Ensemble(configs, f0s, precision="mixed", **kw)
+    for ens in (graph, eager):
+        for op, _, _ in ens._classes:
+            op.plan.set_tuning("fused", 6, 65536, fused_split=0.25)
+    for _ in range(2):
+        graph.step()
+        eager.step(use_graph=False)
+    torch.cuda.synchronize()
+    for i in range(4):
+        assert torch.equal(graph.f[i], eager.f[i]), i
