@@ -82,7 +82,14 @@ struct Geo {
   static constexpr int NPL = NV / CS;    // a-planes of a CTA
   static constexpr int NCOL = N2 / CS;   // (b, c) columns of a CTA
   static constexpr int THREADS = NCOL;   // = NPL * NV plane lines
-  static constexpr int LD = NV + 1;      // padded plane row (complex elements)
+  // padded plane row (complex elements): n + 1, or n + 2 where n is a
+  // multiple of 16 (48, 64), so that every row starts on 16 bytes and the row
+  // pass moves two elements per 16-byte access (a quarter-warp of 16-byte
+  // accesses at row stride 4 mod 32 words is conflict-free; so are the
+  // column pass's 8-byte accesses, whose half-warps never straddle planes)
+  static constexpr bool ROW16 = NV % 16 == 0;
+  static constexpr int LD = NV + (ROW16 ? 2 : 1);
+  static constexpr int LDF = NV + 1;  // row of f in shared memory (floats)
   static constexpr int PLANE = NPL * NV * LD;
   static constexpr int COLS = NV * NCOL;
   static constexpr int BUF = PLANE > COLS ? PLANE : COLS;
@@ -91,7 +98,7 @@ struct Geo {
   static constexpr size_t F_OFF = size_t(BUF) * sizeof(float2);
   // f of the CTA's planes, rows padded to LD floats (the row pass reads
   // f[pl][b][c] for one c across lanes of consecutive b), unless in tensor memory
-  static constexpr size_t ROW_OFF = F_OFF + (F_TM ? 0 : size_t(NPL) * NV * LD * sizeof(float));
+  static constexpr size_t ROW_OFF = F_OFF + (F_TM ? 0 : size_t(NPL) * NV * LDF * sizeof(float));
   // the pass's phase row and gain row (3 n complex each), the radial node's sinc row
   // (n = 48: entry m = |k|^2 at m + m / 32; the lanes of a warp gather at
   // |k|^2 values that differ by squares, which fall into few banks without the
@@ -306,7 +313,7 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       } else {
         for (int e = t; e < NPL * N2; e += G::THREADS) {
           const int p2 = e / N2, rem = e - p2 * N2, b = rem / NV, c = rem - b * NV;
-          fS[(p2 * NV + b) * LD + c] = fc[e];
+          fS[(p2 * NV + b) * G::LDF + c] = fc[e];
         }
       }
       cur = cell;
@@ -413,8 +420,18 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     // inverse along c, * f, forward along c (row (pl, l))
     {
       float2* row = buf + (pl * NV + l) * LD;
+      if constexpr (G::ROW16) {
+        const float4* r4 = reinterpret_cast<const float4*>(row);
 #pragma unroll
-      for (int c = 0; c < NV; ++c) x[c] = row[c];
+        for (int c = 0; c < NV / 2; ++c) {
+          const float4 v = r4[c];
+          x[2 * c] = make_float2(v.x, v.y);
+          x[2 * c + 1] = make_float2(v.z, v.w);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) x[c] = row[c];
+      }
       fft_line<NV, +1, G::PK_B>(x);
       float2 y[NV];
       if constexpr (G::F_TM) {
@@ -429,17 +446,26 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
           });
         });
       } else {
-        const float* fr = fS + (pl * NV + l) * LD;
+        const float* fr = fS + (pl * NV + l) * G::LDF;
         static_for<0, NV>([&](auto ci) {
           constexpr int c = decltype(ci)::value;
           y[c] = cscale(x[pos(NV, c)], fr[c]);
         });
       }
       fft_line<NV, -1, G::PK_B>(y);
-      static_for<0, NV>([&](auto ci) {
-        constexpr int c = decltype(ci)::value;
-        row[c] = y[pos(NV, c)];
-      });
+      if constexpr (G::ROW16) {
+        float4* r4 = reinterpret_cast<float4*>(row);
+        static_for<0, NV / 2>([&](auto ci) {
+          constexpr int c = decltype(ci)::value;
+          const float2 a0 = y[pos(NV, 2 * c)], a1 = y[pos(NV, 2 * c + 1)];
+          r4[c] = make_float4(a0.x, a0.y, a1.x, a1.y);
+        });
+      } else {
+        static_for<0, NV>([&](auto ci) {
+          constexpr int c = decltype(ci)::value;
+          row[c] = y[pos(NV, c)];
+        });
+      }
     }
     __syncthreads();
     // forward along b (column (pl, l)), then to the column owners
