@@ -70,24 +70,31 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
   }
   if constexpr (std::is_same<T, float>::value && NV != 32) {
     if (p->gain_path == 4) {  // the fused kernel: every item on chip, packed where the design allows
-      // split: the last cp cells go to the packed pipeline on a side stream,
-      // whose kernels run on the SMs that the fused kernel's clusters leave
-      // idle; the fused kernel is launched first so that its clusters are
-      // placed first
+      // Where the fused kernel's clusters leave SMs idle (n = 48, 64), a side
+      // stream runs there: the packed pipeline on the last cp cells (the
+      // split) and the partial sums of the quadratic-form Nyquist correction,
+      // which read f^ only; their sum into G follows the join.  The fused
+      // kernel is launched first so that its clusters are placed first.
       const bool pack_pipe = p->ap_count > 0 && p->nq_part;
       const int64_t cp = pack_pipe && p->fz_split > 0 ? std::min<int64_t>(cells - 1, llround(p->fz_split * cells)) : 0;
-      if (cp > 0) {
+      const bool quad = p->ap_count > 0 && nyq_use_quad(p);
+      const bool beside = cp > 0 || (quad && p->fz_sms > 0);
+      if (beside) {
         PII_TRY(side_ready(p));
         PII_CUDA(cudaEventRecord(p->side_fork, s));  // f^ and f of every cell are ready
         PII_CUDA(cudaStreamWaitEvent(p->side, p->side_fork, 0));
       }
       PII_TRY(gain_fused_run(p, cells - cp, s));
-      if (cp > 0) {
-        PII_TRY((pipeline_gain<T, NV>(p, cells - cp, cells, true, p->side)));
-        PII_CUDA(cudaEventRecord(p->side_join, p->side));
-        PII_CUDA(cudaStreamWaitEvent(s, p->side_join, 0));
+      if (cp > 0) PII_TRY((pipeline_gain<T, NV>(p, cells - cp, cells, true, p->side)));
+      if (quad) {
+        PII_TRY(beside ? nyq_quad_run2(p, cells, p->side, s, p->side_join) : nyq_quad_run(p, cells, s));
+      } else {
+        if (beside) {
+          PII_CUDA(cudaEventRecord(p->side_join, p->side));
+          PII_CUDA(cudaStreamWaitEvent(s, p->side_join, 0));
+        }
+        if (p->ap_count > 0) PII_TRY(nyq_gen_run(p, cells, s));
       }
-      if (p->ap_count > 0) PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_gen_run(p, cells, s));
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
   }

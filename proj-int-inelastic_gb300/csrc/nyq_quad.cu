@@ -603,7 +603,12 @@ int nyq_quad_prepare(pii_plan* p) {
 
 void nyq_quad_release(pii_plan* p) { free_quad(p); }
 
-int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s) {
+// the correction's partial sums (f^ only: it may run beside the gain kernels)
+// on stream s, then their sum into G on stream s_add (the caller orders s_add
+// after s and after the gain sums' writes of G)
+int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s) { return nyq_quad_run2(p, cells, s, s, nullptr); }
+
+int nyq_quad_run2(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add, cudaEvent_t partial_done) {
   using namespace nqq;
   if (!p->nq_A || p->nq_npts <= 0) {
     set_error("nyq_quad_run: the plan has no quadratic-form kernels");
@@ -629,20 +634,27 @@ int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s) {
   a.seg_j0 = reinterpret_cast<const int*>(static_cast<const char*>(p->nq_segs) + size_t(p->nq_nseg) * sizeof(int4));
   a.nseg = p->nq_nseg;
   a.n = n, a.npts = p->nq_npts, a.W = cfg.W, a.split = split;
-  StageTimer st(p, ST_NYQ, s);
-  const int tb = (n + 31) / 32;
-  k_quad_prep<<<unsigned(cells * n * tb * tb), 256, 0, s>>>(a.fhat, static_cast<float2*>(p->nq_fhT), n, cells);
-  PII_CHECK_LAUNCH();
-  const dim3 grid(unsigned(n / cfg.W), unsigned((cells + cfg.nc - 1) / cfg.nc), unsigned(3 * split));
-  if (cfg.nc == 4)
-    k_nyq_quad<4, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
-  else if (cfg.nc == 2)
-    k_nyq_quad<2, 512><<<grid, cfg.threads, cfg.smem, s>>>(a);
-  else
-    k_nyq_quad<1, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
-  PII_CHECK_LAUNCH();
+  {
+    StageTimer st(p, ST_NYQ, s);
+    const int tb = (n + 31) / 32;
+    k_quad_prep<<<unsigned(cells * n * tb * tb), 256, 0, s>>>(a.fhat, static_cast<float2*>(p->nq_fhT), n, cells);
+    PII_CHECK_LAUNCH();
+    const dim3 grid(unsigned(n / cfg.W), unsigned((cells + cfg.nc - 1) / cfg.nc), unsigned(3 * split));
+    if (cfg.nc == 4)
+      k_nyq_quad<4, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+    else if (cfg.nc == 2)
+      k_nyq_quad<2, 512><<<grid, cfg.threads, cfg.smem, s>>>(a);
+    else
+      k_nyq_quad<1, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+    PII_CHECK_LAUNCH();
+  }
+  if (partial_done) {
+    PII_CUDA(cudaEventRecord(partial_done, s));
+    PII_CUDA(cudaStreamWaitEvent(s_add, partial_done, 0));
+  }
+  StageTimer st(p, ST_NYQ, s_add);
   const int64_t tot = cells * 3 * n2;
-  k_quad_add<<<unsigned((tot + 255) / 256), 256, 0, s>>>(a.part, static_cast<float2*>(p->G), n, cells, split);
+  k_quad_add<<<unsigned((tot + 255) / 256), 256, 0, s_add>>>(a.part, static_cast<float2*>(p->G), n, cells, split);
   PII_CHECK_LAUNCH();
   return PII_OK;
 }

@@ -306,6 +306,8 @@ int gain_fused_ensure(pii_plan* p);
 int gain_fused_run(pii_plan* p, int64_t cells, cudaStream_t s);
 void nyq_quad_release(pii_plan* p);
 int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s);
+// partial sums on s; if partial_done, s_add waits for it; the sum into G on s_add
+int nyq_quad_run2(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add, cudaEvent_t partial_done);
 // the Nyquist correction of the packed paths: the quadratic form where it was
 // built and chosen, else the direct kernel of the plan's n
 inline bool nyq_use_quad(const pii_plan* p) { return p->nyq_path == 0 && p->nq_A != nullptr; }
