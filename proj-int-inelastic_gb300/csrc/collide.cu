@@ -98,11 +98,18 @@ static int collide_t(pii_plan* p, const double* f, double* q, int64_t cells, int
       return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
     }
   }
+  // the packed pipeline: FP32 for n != 32 (n = 32 has the a-parity kernel),
+  // FP64 for every n, where the quadratic-form correction is built
   bool packed = false;
-  if constexpr (std::is_same<T, float>::value && NV != 32) packed = p->gain_path == 3 && p->ap_count > 0;
+  if constexpr (!std::is_same<T, float>::value || NV != 32) packed = p->gain_path == 3 && p->ap_count > 0;
   PII_TRY((pipeline_gain<T, NV>(p, 0, cells, packed, s)));
   // what the packed passes leave out, on the Nyquist planes
-  if (packed) PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_gen_run(p, cells, s));
+  if (packed) {
+    if constexpr (std::is_same<T, float>::value)
+      PII_TRY(nyq_use_quad(p) ? nyq_quad_run(p, cells, s) : nyq_gen_run(p, cells, s));
+    else
+      PII_TRY(nyq_quad_run(p, cells, s));  // FP64: the quadratic form only
+  }
   return finish_all<T, NV>(p, f, q, cells, with_loss, hb, s);
 }
 
@@ -233,8 +240,9 @@ extern "C" int pii_plan_autotune(pii_plan* plan, int64_t cells, double* best_ms,
     cands.push_back({2, plan->gc_items_per_cluster, plan->chunk_points, 0, 0.0});  // even split: no item knob
     if (plan->ap_count > 0) cands.push_back({3, plan->gc_items_per_cluster, plan->chunk_points, 0, 0.0});
   }
-  // the pipeline on (cell, pair) items, and on antipodal passes where it is packed (n != 32)
-  const bool pack_pipe = plan->n != 32 && plan->ap_count > 0 && plan->nq_part;
+  // the pipeline on (cell, pair) items, and on antipodal passes where it is
+  // packed (FP32: n != 32; FP64: where the quadratic-form correction is built)
+  const bool pack_pipe = pii::packed_pipeline_ok(plan);
   for (int path : {0, 3}) {
     if (path == 3 && !pack_pipe) continue;
     for (int dft = 0; dft <= (plan->dft_img ? 1 : 0); ++dft)
@@ -336,8 +344,11 @@ extern "C" int pii_plan_set_gain_path(pii_plan* plan, int path) {
     return PII_ERR_ARG;
   }
   if (path == 4) PII_TRY(pii::gain_fused_ensure(plan));
-  if (path == 3 && (plan->ap_count == 0 || !plan->nq_part)) {
-    pii::set_error("pii_plan_set_gain_path: the packed path needs an FP32 3D plan on an antipodally symmetric design");
+  if (path == 3 && !(plan->n == 32 && plan->precision == PII_PREC_FP32 ? plan->ap_count > 0 && plan->nq_part
+                                                                          : pii::packed_pipeline_ok(plan))) {
+    pii::set_error(
+        "pii_plan_set_gain_path: the packed path needs a 3D plan on an antipodally symmetric design (FP64: with "
+        "the quadratic-form Nyquist correction within the memory budget)");
     return PII_ERR_ARG;
   }
   if ((path == 1 || path == 2) && (plan->gc_clusters <= 0 || plan->gp_ctas <= 0)) {
@@ -411,11 +422,15 @@ extern "C" int pii_plan_set_nyquist_path(pii_plan* plan, int path) {
     pii::set_error("pii_plan_set_nyquist_path: path must be 0 (quadratic form) or 1 (direct kernels)");
     return PII_ERR_ARG;
   }
+  if (path == 1 && plan->precision != PII_PREC_FP32) {
+    pii::set_error("pii_plan_set_nyquist_path: the direct kernels are FP32; FP64 plans use the quadratic form");
+    return PII_ERR_ARG;
+  }
   if (path == 0 && !plan->nq_A) {
     PII_CUDA(cudaSetDevice(plan->device));
     PII_TRY(pii::nyq_quad_prepare(plan));  // built on request
     if (!plan->nq_A) {
-      pii::set_error("pii_plan_set_nyquist_path: no quadratic-form kernels for this plan (not an FP32 3D plan on an "
+      pii::set_error("pii_plan_set_nyquist_path: no quadratic-form kernels for this plan (not a 3D plan on an "
                      "antipodally symmetric design, or beyond the memory budget)");
       return PII_ERR_ARG;
     }

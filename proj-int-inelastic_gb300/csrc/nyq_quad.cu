@@ -46,6 +46,7 @@
 // multiple of R with zero kernels, and slice 0's column up to i1 < h): the
 // same two planes per slice, about half the input points.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "fft_reg.cuh"
@@ -59,23 +60,31 @@ constexpr int SPLIT_MAX = 8;     // input-point ranges per orientation
 constexpr int TM = 64, TK = 16;  // GEMM tiles: 64 x 64 outputs, 16 passes per step
 }  // namespace nqq
 
-__device__ __forceinline__ float2 qq_conj(float2 v) { return make_float2(v.x, -v.y); }
+// the FP32 and FP64 plans run the same kernels in their own arithmetic
+template <typename V>
+__device__ __forceinline__ V qq_conj(V v) {
+  return mk<V>(v.x, -v.y);
+}
 
 // (X(k) - X~(k)) / 2 for the per-axis rows x (~ conjugates the factor of a
 // component equal to the Nyquist index h)
-__device__ __forceinline__ float2 qq_minus(const float2* rows, int n, int ka, int kb, int kc) {
+template <typename V>
+__device__ __forceinline__ V qq_minus(const V* rows, int n, int ka, int kb, int kc) {
+  using S = decltype(V::x);
   const int h = n / 2;
-  const float2 xa = rows[ka], xb = rows[n + kb], xc = rows[2 * n + kc];
-  const float2 p = cmul(cmul(xa, xb), xc);
-  const float2 q = cmul(cmul(ka == h ? qq_conj(xa) : xa, kb == h ? qq_conj(xb) : xb), kc == h ? qq_conj(xc) : xc);
-  return make_float2(0.5f * (p.x - q.x), 0.5f * (p.y - q.y));
+  const V xa = rows[ka], xb = rows[n + kb], xc = rows[2 * n + kc];
+  const V p = cmul(cmul(xa, xb), xc);
+  const V q = cmul(cmul(ka == h ? qq_conj(xa) : xa, kb == h ? qq_conj(xb) : xb), kc == h ? qq_conj(xc) : xc);
+  return mk<V>(S(0.5) * (p.x - q.x), S(0.5) * (p.y - q.y));
 }
 
 // T[p][i] = Re E-_p + Im E-_p at Nyquist point i; Al / Be[s][p][i] = w.x -+ ... for set s
+template <typename S>
 __global__ void __launch_bounds__(256) k_quad_coef(const int* pts, int npts, int n, const int* reps, int QP,
-                                                    int ns, int M, const float2* ephase, const float2* gphase,
-                                                    const float* gsinc, int64_t gph_set, int64_t gs_set, int sets,
-                                                    float* T, float* Al, float* Be) {
+                                                    int ns, int M, const c2<S>* ephase, const c2<S>* gphase,
+                                                    const S* gsinc, int64_t gph_set, int64_t gs_set, int sets,
+                                                    S* T, S* Al, S* Be) {
+  using V = c2<S>;
   const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t per = int64_t(QP) * npts;
   if (gid >= per * (sets + 1)) return;
@@ -86,14 +95,14 @@ __global__ void __launch_bounds__(256) k_quad_coef(const int* pts, int npts, int
   const int ka = code / n2, kb = (code / n) % n, kc = code % n;
   const int pair = reps[p];
   if (s1 == 0) {
-    const float2 em = qq_minus(ephase + int64_t(pair) * 3 * n, n, ka, kb, kc);
+    const V em = qq_minus(ephase + int64_t(pair) * 3 * n, n, ka, kb, kc);
     T[r] = em.x + em.y;
   } else {
     const int64_t s = s1 - 1;
-    const float2 gm = qq_minus(gphase + s * gph_set + int64_t(pair) * 3 * n, n, ka, kb, kc);
+    const V gm = qq_minus(gphase + s * gph_set + int64_t(pair) * 3 * n, n, ka, kb, kc);
     const int kk = kval(ka, n) * kval(ka, n) + kval(kb, n) * kval(kb, n) + kval(kc, n) * kval(kc, n);
-    const float g = gsinc[s * gs_set + int64_t(pair / ns) * (M + 1) + kk];
-    const float wx = g * gm.x, wy = g * gm.y;
+    const S g = gsinc[s * gs_set + int64_t(pair / ns) * (M + 1) + kk];
+    const S wx = g * gm.x, wy = g * gm.y;
     Al[s * per + r] = wx - wy;
     Be[s * per + r] = wx + wy;
   }
@@ -103,38 +112,39 @@ __global__ void __launch_bounds__(256) k_quad_coef(const int* pts, int npts, int
 // the paired kernel of slot j (q1 its input point, q2 = -q1; q1 < 0 marks a
 // padding slot, zero) at the output points ki (ki < 0: skipped, zero); T, X1
 // and X2 rows hold npts entries in point order
-__global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* X1, const float* X2, const int* q1,
-                                                    const int* q2, const float* w, const int* ki, float* C, int M,
+template <typename S>
+__global__ void __launch_bounds__(256) k_quad_gemm(const S* T, const S* X1, const S* X2, const int* q1,
+                                                    const int* q2, const S* w, const int* ki, S* C, int M,
                                                     int Ncol, int QP, int npts) {
   using namespace nqq;
-  __shared__ float ta[TK][TM], tb[TK][TM];
+  __shared__ S ta[TK][TM], tb[TK][TM];
   const int q0 = blockIdx.y * TM, k0 = blockIdx.x * TM;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads, 4 x 4 outputs each
-  float acc[4][4] = {};
+  S acc[4][4] = {};
   for (int p0 = 0; p0 < 2 * QP; p0 += TK) {  // the passes twice: + T(q) X1, - T(-q) X2
     for (int e = threadIdx.x; e < TK * TM; e += 256) {
       const int pp = e / TM, c = e - pp * TM;
       const int pg = p0 + pp, second = pg >= QP ? 1 : 0, p = pg - second * QP;
       const bool okp = pg < 2 * QP;
       const int kidx = okp && k0 + c < Ncol ? ki[k0 + c] : -1;
-      float tv = 0.f;
+      S tv = S(0);
       if (okp && q0 + c < M && q1[q0 + c] >= 0) {
         const int qq = second ? q2[q0 + c] : q1[q0 + c];
         tv = (second ? -w[q0 + c] : w[q0 + c]) * T[int64_t(p) * npts + qq];
       }
       ta[pp][c] = tv;
-      tb[pp][c] = kidx >= 0 ? (second ? X2 : X1)[int64_t(p) * npts + kidx] : 0.f;
+      tb[pp][c] = kidx >= 0 ? (second ? X2 : X1)[int64_t(p) * npts + kidx] : S(0);
     }
     __syncthreads();
 #pragma unroll
     for (int pp = 0; pp < TK; ++pp) {
-      float a[4], b[4];
+      S a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = ta[pp][ty * 4 + i], b[i] = tb[pp][tx * 4 + i];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
@@ -149,16 +159,17 @@ __global__ void __launch_bounds__(256) k_quad_gemm(const float* T, const float* 
 
 // f^ transposed within each a-plane: fhT[cell][a][c][b] = f^[cell][a][b][c]
 // (32 x 32 tiles through shared memory)
-__global__ void __launch_bounds__(256) k_quad_prep(const float2* fhat, float2* fhT, int n, int64_t cells) {
-  __shared__ float2 tile[32][33];
+template <typename V>
+__global__ void __launch_bounds__(256) k_quad_prep(const V* fhat, V* fhT, int n, int64_t cells) {
+  __shared__ V tile[32][33];
   const int tb_n = (n + 31) / 32;
   const int64_t n2 = int64_t(n) * n;
   const int64_t bid = blockIdx.x;
   const int64_t cp = bid / (tb_n * tb_n);  // (cell, a)
   if (cp >= cells * n) return;
   const int tt = int(bid - cp * tb_n * tb_n), tb = tt / tb_n, tc = tt - tb * tb_n;
-  const float2* src = fhat + cp * n2;
-  float2* dst = fhT + cp * n2;
+  const V* src = fhat + cp * n2;
+  V* dst = fhT + cp * n2;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   for (int j = ty; j < 32; j += 8) {
     const int b = tb * 32 + j, c = tc * 32 + tx;
@@ -171,35 +182,53 @@ __global__ void __launch_bounds__(256) k_quad_prep(const float2* fhat, float2* f
   }
 }
 
+template <typename S>
 struct QuadArgs {
-  const float* A;
-  const float* B;
-  const float2* fhat;
-  const float2* fhT;
-  float2* part;        // [split][cells][3][n][n]
+  using V = c2<S>;
+  const S* A;
+  const S* B;
+  const V* fhat;
+  const V* fhT;
+  V* part;             // [split][cells][3][n][n]
   const int4* segs;    // segments of the kernel slots: (slice, 0 row / 1 column, row i1, steps)
   const int* seg_j0;   // first kernel slot of each segment
   int nseg;
   int64_t cells;
-  int64_t set_stride;  // floats between consecutive cells' kernels (0: one set for every cell)
+  int64_t set_stride;  // entries between consecutive cells' kernels (0: one set for every cell)
   int n, npts, W, split;  // npts: kernel slots per orientation
 };
 
-__device__ __forceinline__ void qq_term(float2& acc, float a, float b, float2 f0, float2 gm, float2 gp) {
+template <typename S, typename V>
+__device__ __forceinline__ void qq_term(V& acc, S a, S b, V f0, V gm, V gp) {
   // acc += a f0 gm - b conj(f0) gp
-  const float x1 = fmaf(a, gm.x, -b * gp.x), x2 = fmaf(a, gm.y, b * gp.y);
-  const float x3 = fmaf(a, gm.y, -b * gp.y), x4 = fmaf(a, gm.x, b * gp.x);
-  acc.x = fmaf(f0.x, x1, fmaf(-f0.y, x2, acc.x));
-  acc.y = fmaf(f0.x, x3, fmaf(f0.y, x4, acc.y));
+  const S x1 = fma(a, gm.x, -b * gp.x), x2 = fma(a, gm.y, b * gp.y);
+  const S x3 = fma(a, gm.y, -b * gp.y), x4 = fma(a, gm.x, b * gp.x);
+  acc.x = fma(f0.x, x1, fma(-f0.y, x2, acc.x));
+  acc.y = fma(f0.x, x3, fma(f0.y, x4, acc.y));
 }
+
+// R = 4 consecutive kernel entries (16 bytes FP32, 2 x 16 bytes FP64)
+__device__ __forceinline__ void qq_ld4(const float* p, float (&o)[4]) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  o[0] = v.x, o[1] = v.y, o[2] = v.z, o[3] = v.w;
+}
+__device__ __forceinline__ void qq_ld4(const double* p, double (&o)[4]) {
+  const double2 v0 = __ldg(reinterpret_cast<const double2*>(p)), v1 = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  o[0] = v0.x, o[1] = v0.y, o[2] = v1.x, o[3] = v1.y;
+}
+// one complex element into shared memory
+__device__ __forceinline__ void qq_cp(float2* d, const float2* s) { cp_async8(d, s); }
+__device__ __forceinline__ void qq_cp(double2* d, const double2* s) { cp_async16(d, s); }
 
 // partial C over one range of one orientation's input points, for R output
 // points per thread and NC cells per CTA (NC = 1 when every cell has its own
 // kernels); grid (n / W, cell groups, 3 x split), n W / R threads
-template <int NC, int MAXT>
-__global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
+template <typename S, int NC, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs<S> a) {
+  using V = c2<S>;
   constexpr int R = nqq::R;
-  extern __shared__ float2 qsm[];
+  extern __shared__ __align__(16) unsigned char qsm_raw[];
+  V* qsm = reinterpret_cast<V*>(qsm_raw);
   const int n = a.n, h = n >> 1, n2 = n * n, LD = n + 1;
   const int64_t n3 = int64_t(n2) * n;
   const int d = blockIdx.z / a.split, range = blockIdx.z - d * a.split;
@@ -208,7 +237,7 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
   const int k20 = blockIdx.x * a.W + kb * R;
   const int64_t c0 = int64_t(blockIdx.y) * NC;
   const int per_cell = 2 * n * LD + 2 * n;  // P1 [n][LD], P2 [n][LD], QR [n], QC [n]
-  const float2* src[NC];
+  const V* src[NC];
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
     const int64_t cell = min(c0 + c, a.cells - 1);
@@ -219,13 +248,13 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
   const int s1 = d == 0 ? n : n2, vstride = d == 0 ? n2 : n;
   const int64_t kset = a.set_stride ? c0 * a.set_stride : 0;
   const int64_t kofs = kset + int64_t(d) * a.npts * n2 + (int64_t(k20 / R) * n + k1) * R;
-  const float* Ab = a.A + kofs;
-  const float* Bb = a.B + kofs;
-  float2 acc[NC][R];
+  const S* Ab = a.A + kofs;
+  const S* Bb = a.B + kofs;
+  V acc[NC][R];
 #pragma unroll
   for (int c = 0; c < NC; ++c)
 #pragma unroll
-    for (int r = 0; r < R; ++r) acc[c][r] = make_float2(0.f, 0.f);
+    for (int r = 0; r < R; ++r) acc[c][r] = mk<V>(S(0), S(0));
 
   const int nseg = a.nseg;
   const int g0 = range * nseg / a.split, g1 = (range + 1) * nseg / a.split;
@@ -238,18 +267,18 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
       const int vm = (h - s + n) % n, vp = (n - vm) % n, v2 = s == h ? h : vp;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        float2* P1 = qsm + c * per_cell;
-        float2* P2 = P1 + n * LD;
-        const float2* sm_ = src[c] + int64_t(vm) * vstride;
-        const float2* s2_ = src[c] + int64_t(v2) * vstride;
+        V* P1 = qsm + c * per_cell;
+        V* P2 = P1 + n * LD;
+        const V* sm_ = src[c] + int64_t(vm) * vstride;
+        const V* s2_ = src[c] + int64_t(v2) * vstride;
         for (int i1 = kb; i1 < n; i1 += rows_step) {
-          cp_async8(P1 + i1 * LD + k1, sm_ + int64_t(i1) * s1 + k1);
-          cp_async8(P2 + i1 * LD + k1, s2_ + int64_t(i1) * s1 + k1);
+          qq_cp(P1 + i1 * LD + k1, sm_ + int64_t(i1) * s1 + k1);
+          qq_cp(P2 + i1 * LD + k1, s2_ + int64_t(i1) * s1 + k1);
         }
         if (s != h && kb < 2) {  // QR: row h of the plane at s; QC: its column h
-          const float2* ss = src[c] + int64_t(s) * vstride;
-          float2* Q = P2 + n * LD + kb * n;
-          cp_async8(Q + k1, kb == 0 ? ss + int64_t(h) * s1 + k1 : ss + int64_t(k1) * s1 + h);
+          const V* ss = src[c] + int64_t(s) * vstride;
+          V* Q = P2 + n * LD + kb * n;
+          qq_cp(Q + k1, kb == 0 ? ss + int64_t(h) * s1 + k1 : ss + int64_t(k1) * s1 + h);
         }
       }
       cp_async_commit();
@@ -261,14 +290,14 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
       int rm = k1 - i1f, rp = k1 + i1f;
       rm += rm < 0 ? n : 0;
       rp -= rp >= n ? n : 0;
-      const float2* pm[NC];
-      const float2* pp[NC];
-      const float2* qrow[NC];
-      float2 wm[NC][R], wp[NC][R];
+      const V* pm[NC];
+      const V* pp[NC];
+      const V* qrow[NC];
+      V wm[NC][R], wp[NC][R];
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        const float2* P1 = qsm + c * per_cell;
-        const float2* P2 = P1 + n * LD;
+        const V* P1 = qsm + c * per_cell;
+        const V* P2 = P1 + n * LD;
         pm[c] = P1 + rm * LD;
         pp[c] = (s == h ? P1 : P2) + rp * LD;
         qrow[c] = s == h ? P2 + i1f * LD : P2 + n * LD;
@@ -277,23 +306,25 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
 #pragma unroll
         for (int r = 0; r < R - 1; ++r) wp[c][r] = pp[c][k20 + r];
       }
-      const float* Aj = Ab + int64_t(j0) * n2;
-      const float* Bj = Bb + int64_t(j0) * n2;
-      float4 an[R], bn[R];  // the kernels of the next R input points, loaded one block ahead
+      const S* Aj = Ab + int64_t(j0) * n2;
+      const S* Bj = Bb + int64_t(j0) * n2;
+      S an[R][R], bn[R][R];  // the kernels of the next R input points, loaded one block ahead
 #pragma unroll
       for (int t = 0; t < R; ++t) {
-        an[t] = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(t) * n2));
-        bn[t] = __ldg(reinterpret_cast<const float4*>(Bj + int64_t(t) * n2));
+        qq_ld4(Aj + int64_t(t) * n2, an[t]);
+        qq_ld4(Bj + int64_t(t) * n2, bn[t]);
       }
       for (int i20 = 0; i20 < len; i20 += R) {
-        float4 ac[R], bc[R];
+        S ac[R][R], bc[R][R];
 #pragma unroll
-        for (int t = 0; t < R; ++t) ac[t] = an[t], bc[t] = bn[t];
+        for (int t = 0; t < R; ++t)
+#pragma unroll
+          for (int r = 0; r < R; ++r) ac[t][r] = an[t][r], bc[t][r] = bn[t][r];
         if (i20 + R < len) {
 #pragma unroll
           for (int t = 0; t < R; ++t) {
-            an[t] = __ldg(reinterpret_cast<const float4*>(Aj + int64_t(i20 + R + t) * n2));
-            bn[t] = __ldg(reinterpret_cast<const float4*>(Bj + int64_t(i20 + R + t) * n2));
+            qq_ld4(Aj + int64_t(i20 + R + t) * n2, an[t]);
+            qq_ld4(Bj + int64_t(i20 + R + t) * n2, bn[t]);
           }
         }
 #pragma unroll
@@ -302,13 +333,13 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
           int um = k20 - i2, up = k20 + R - 1 + i2;
           um += um < 0 ? n : 0;
           up -= up >= n ? n : 0;
-          const float4 av = ac[t], bv = bc[t];
-          const float al[R] = {av.x, av.y, av.z, av.w}, be[R] = {bv.x, bv.y, bv.z, bv.w};
+          const S(&al)[R] = ac[t];
+          const S(&be)[R] = bc[t];
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
             wm[c][(R - t) % R] = pm[c][um];
             wp[c][(R - 1 + t) % R] = pp[c][up];
-            const float2 f0 = qrow[c][i2];
+            const V f0 = qrow[c][i2];
 #pragma unroll
             for (int r = 0; r < R; ++r) qq_term(acc[c][r], al[r], be[r], f0, wm[c][(r - t + R) % R], wp[c][(r + t) % R]);
           }
@@ -317,26 +348,28 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
     } else {  // the column i2 = h of slice s != h: i1 = m (m < h), m + 1 (m >= h), m < len
       const int cm = (k20 + h) % n;  // k2 -+ h for the thread's first k2 (no wrap within the R)
       // the column's input points are consecutive in the kernels: j0 + m
-      float4 an = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(j0) * n2));
-      float4 bn = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(j0) * n2));
+      S an[R], bn[R];
+      qq_ld4(Ab + int64_t(j0) * n2, an);
+      qq_ld4(Bb + int64_t(j0) * n2, bn);
       for (int m = 0; m < len; ++m) {
         const int i1 = m < h ? m : m + 1;
         int rm = k1 - i1, rp = k1 + i1;
         rm += rm < 0 ? n : 0;
         rp -= rp >= n ? n : 0;
-        const float4 av = an, bv = bn;
+        S al[R], be[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) al[r] = an[r], be[r] = bn[r];
         if (m + 1 < len) {
-          an = __ldg(reinterpret_cast<const float4*>(Ab + int64_t(j0 + m + 1) * n2));
-          bn = __ldg(reinterpret_cast<const float4*>(Bb + int64_t(j0 + m + 1) * n2));
+          qq_ld4(Ab + int64_t(j0 + m + 1) * n2, an);
+          qq_ld4(Bb + int64_t(j0 + m + 1) * n2, bn);
         }
-        const float al[R] = {av.x, av.y, av.z, av.w}, be[R] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-          const float2* P1 = qsm + c * per_cell;
-          const float2* P2 = P1 + n * LD;
-          const float2* gmr = P1 + rm * LD + cm;
-          const float2* gpr = P2 + rp * LD + cm;
-          const float2 f0 = P2[n * LD + n + i1];
+          const V* P1 = qsm + c * per_cell;
+          const V* P2 = P1 + n * LD;
+          const V* gmr = P1 + rm * LD + cm;
+          const V* gpr = P2 + rp * LD + cm;
+          const V f0 = P2[n * LD + n + i1];
 #pragma unroll
           for (int r = 0; r < R; ++r) qq_term(acc[c][r], al[r], be[r], f0, gmr[r], gpr[r]);
         }
@@ -347,7 +380,7 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
   for (int c = 0; c < NC; ++c) {
     const int64_t cell = c0 + c;
     if (cell >= a.cells) break;
-    float2* o = a.part + ((int64_t(range) * a.cells + cell) * 3 + d) * n2 + int64_t(k1) * n + k20;
+    V* o = a.part + ((int64_t(range) * a.cells + cell) * 3 + d) * n2 + int64_t(k1) * n + k20;
 #pragma unroll
     for (int r = 0; r < R; ++r) o[r] = acc[c][r];
   }
@@ -355,7 +388,8 @@ __global__ void __launch_bounds__(MAXT) k_nyq_quad(QuadArgs a) {
 
 // G[cell][k] += the partial sums of every range, for the output points of the
 // three planes (points of an earlier plane skipped)
-__global__ void __launch_bounds__(256) k_quad_add(const float2* part, float2* G, int n, int64_t cells, int split) {
+template <typename V>
+__global__ void __launch_bounds__(256) k_quad_add(const V* part, V* G, int n, int64_t cells, int split) {
   const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int n2 = n * n, h = n >> 1;
   if (gid >= cells * 3 * n2) return;
@@ -364,13 +398,13 @@ __global__ void __launch_bounds__(256) k_quad_add(const float2* part, float2* G,
   const int d = int(cd % 3);
   if ((d == 1 && k1 == h) || (d == 2 && (k1 == h || k2 == h))) return;
   const int64_t cell = cd / 3;
-  float2 sum = make_float2(0.f, 0.f);
+  V sum = mk<V>(0, 0);
   for (int r = 0; r < split; ++r) {
-    const float2 v = part[(int64_t(r) * cells * 3 + cd) * n2 + e];
+    const V v = part[(int64_t(r) * cells * 3 + cd) * n2 + e];
     sum.x += v.x, sum.y += v.y;
   }
   const int code = d == 0 ? h * n2 + k1 * n + k2 : d == 1 ? k1 * n2 + h * n + k2 : k1 * n2 + k2 * n + h;
-  float2* g = G + cell * int64_t(n2) * n + code;
+  V* g = G + cell * int64_t(n2) * n + code;
   g->x += sum.x;
   g->y += sum.y;
 }
@@ -383,27 +417,37 @@ struct QuadCfg {
   size_t smem;
 };
 
+// FP32: 4 cells per CTA up to n = 32, else 2; FP64 (twice the shared memory
+// and registers per value): 2 up to n = 48, else 1; one with a set per cell
+template <typename S>
 static QuadCfg quad_cfg(int n, int nsets) {
+  constexpr bool f64 = std::is_same<S, double>::value;
   QuadCfg c{};
-  c.nc = nsets > 1 ? 1 : (n <= 32 ? 4 : 2);
+  c.nc = nsets > 1 ? 1 : f64 ? (n <= 48 ? 2 : 1) : (n <= 32 ? 4 : 2);
   c.W = n == 32 || n == 48 ? 16 : n;
   if (n == 64) c.W = c.nc == 1 ? 16 : 32;  // 256 or 512 threads
   c.threads = n * c.W / nqq::R;
-  c.smem = size_t(c.nc) * size_t(2 * n * (n + 1) + 2 * n) * sizeof(float2);
+  c.smem = size_t(c.nc) * size_t(2 * n * (n + 1) + 2 * n) * sizeof(c2<S>);
   return c;
 }
 
-template <int NC, int MAXT>
+template <typename S, int NC, int MAXT>
 static int quad_occupancy(const QuadCfg& c, int* per_sm) {
-  PII_CUDA(cudaFuncSetAttribute(k_nyq_quad<NC, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(c.smem)));
-  PII_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_nyq_quad<NC, MAXT>, c.threads, c.smem));
+  PII_CUDA(cudaFuncSetAttribute(k_nyq_quad<S, NC, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(c.smem)));
+  PII_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_nyq_quad<S, NC, MAXT>, c.threads, c.smem));
   return PII_OK;
 }
 
+template <typename S>
 static int quad_kernel_setup(const QuadCfg& c, int* per_sm) {
-  if (c.nc == 4) return quad_occupancy<4, 256>(c, per_sm);
-  if (c.nc == 2) return quad_occupancy<2, 512>(c, per_sm);
-  return quad_occupancy<1, 256>(c, per_sm);
+  if constexpr (std::is_same<S, float>::value) {
+    if (c.nc == 4) return quad_occupancy<S, 4, 256>(c, per_sm);
+    if (c.nc == 2) return quad_occupancy<S, 2, 512>(c, per_sm);
+    return quad_occupancy<S, 1, 256>(c, per_sm);
+  } else {
+    if (c.nc == 2) return quad_occupancy<S, 2, 256>(c, per_sm);
+    return quad_occupancy<S, 1, 256>(c, per_sm);
+  }
 }
 
 // input-point ranges per orientation for `cells` cells: about two waves of CTAs
@@ -427,11 +471,11 @@ static void free_quad(pii_plan* p) {
 }
 
 // (Re)builds A and B for the plan's restitution sets; leaves the plan without
-// them (the direct correction kernels) when they exceed the memory budget
-int nyq_quad_prepare(pii_plan* p) {
+// them (FP32: the direct correction kernels; FP64: the unpacked pipeline)
+// when they exceed the memory budget
+template <typename S>
+static int quad_prepare_t(pii_plan* p) {
   using namespace nqq;
-  free_quad(p);
-  if (p->ap_count <= 0 || p->precision != PII_PREC_FP32 || p->dim != 3) return PII_OK;
   const int n = p->n, h = n / 2, n2 = n * n;
   if (n % 8 != 0 || n > 64) return PII_OK;  // R | h and the launch shapes below
   std::vector<int> pts;
@@ -480,7 +524,7 @@ int nyq_quad_prepare(pii_plan* p) {
   // per orientation and slot: the point q, its negative, the pair weight;
   // output points in the kernels' layout
   std::vector<int> q1, q2, ki;
-  std::vector<float> wq;
+  std::vector<S> wq;
   for (int d = 0; d < 3; ++d) {
     for (int g = 0; g < nseg; ++g) {
       const int4 sg = segs[g];
@@ -492,7 +536,7 @@ int nyq_quad_prepare(pii_plan* p) {
           c = code(d, sg.x, m < h ? m : m + 1, h);
         }
         if (c < 0) {
-          q1.push_back(-1), q2.push_back(0), wq.push_back(0.f);
+          q1.push_back(-1), q2.push_back(0), wq.push_back(S(0));
           continue;
         }
         const int cn = negc(c);
@@ -500,7 +544,7 @@ int nyq_quad_prepare(pii_plan* p) {
           set_error("nyq_quad_prepare: internal error in the input-point order");
           return PII_ERR_ARG;
         }
-        q1.push_back(pidx[c]), q2.push_back(pidx[cn]), wq.push_back(c == cn ? 0.5f : 1.f);
+        q1.push_back(pidx[c]), q2.push_back(pidx[cn]), wq.push_back(c == cn ? S(0.5) : S(1));
       }
     }
     for (int kbg = 0; kbg < n / R; ++kbg)
@@ -513,17 +557,17 @@ int nyq_quad_prepare(pii_plan* p) {
   }
   p->nq_nseg = nseg;
   const int64_t sets = p->tab.nsets, QP = p->ap_count;
-  const QuadCfg cfg = quad_cfg(n, int(sets));
+  const QuadCfg cfg = quad_cfg<S>(n, int(sets));
   int per_sm = 0, sms = 0;
-  PII_TRY(quad_kernel_setup(cfg, &per_sm));
+  PII_TRY(quad_kernel_setup<S>(cfg, &per_sm));
   PII_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
   if (per_sm < 1) return PII_OK;  // the launch shape does not fit: the direct kernels stay in use
   p->nq_slots = per_sm * sms;
   int64_t units = 0;  // (range, cell) units of the partial sums at the largest use
   for (int64_t c = 1; c <= p->batch_max; ++c) units = std::max(units, int64_t(quad_split(p, cfg, c)) * c);
-  const size_t kern = size_t(sets) * 3 * size_t(NJ) * n2 * sizeof(float);  // each of A, B
-  const size_t fhT = size_t(p->batch_max) * size_t(n2) * n * sizeof(float2);
-  const size_t part = size_t(units) * 3 * n2 * sizeof(float2);
+  const size_t kern = size_t(sets) * 3 * size_t(NJ) * n2 * sizeof(S);  // each of A, B
+  const size_t fhT = size_t(p->batch_max) * size_t(n2) * n * sizeof(c2<S>);
+  const size_t part = size_t(units) * 3 * n2 * sizeof(c2<S>);
   size_t free_b = 0, total_b = 0;
   PII_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const size_t budget = std::min<size_t>(size_t(16) << 30, free_b / 4);
@@ -532,9 +576,9 @@ int nyq_quad_prepare(pii_plan* p) {
     p->nq_nseg = 0;
     return PII_OK;
   }
-  float *T = nullptr, *Al = nullptr, *Be = nullptr, *dw = nullptr;
+  S *T = nullptr, *Al = nullptr, *Be = nullptr, *dw = nullptr;
   int *dpts = nullptr, *dq1 = nullptr, *dq2 = nullptr, *dki = nullptr;
-  const size_t coef = size_t(QP) * npts * sizeof(float);
+  const size_t coef = size_t(QP) * npts * sizeof(S);
   int st = PII_OK;
   auto al = [&](void** dst, size_t b) {
     if (st == PII_OK && cudaMalloc(dst, b) != cudaSuccess) {
@@ -553,34 +597,34 @@ int nyq_quad_prepare(pii_plan* p) {
   al((void**)&dpts, pts.size() * sizeof(int));
   al((void**)&dq1, q1.size() * sizeof(int));
   al((void**)&dq2, q2.size() * sizeof(int));
-  al((void**)&dw, wq.size() * sizeof(float));
+  al((void**)&dw, wq.size() * sizeof(S));
   al((void**)&dki, ki.size() * sizeof(int));
   if (st == PII_OK) {
     PII_CUDA(cudaMemcpy(dpts, pts.data(), pts.size() * sizeof(int), cudaMemcpyHostToDevice));
     PII_CUDA(cudaMemcpy(dq1, q1.data(), q1.size() * sizeof(int), cudaMemcpyHostToDevice));
     PII_CUDA(cudaMemcpy(dq2, q2.data(), q2.size() * sizeof(int), cudaMemcpyHostToDevice));
-    PII_CUDA(cudaMemcpy(dw, wq.data(), wq.size() * sizeof(float), cudaMemcpyHostToDevice));
+    PII_CUDA(cudaMemcpy(dw, wq.data(), wq.size() * sizeof(S), cudaMemcpyHostToDevice));
     PII_CUDA(cudaMemcpy(dki, ki.data(), ki.size() * sizeof(int), cudaMemcpyHostToDevice));
     PII_CUDA(cudaMemcpy(p->nq_segs, segs.data(), size_t(nseg) * sizeof(int4), cudaMemcpyHostToDevice));
     PII_CUDA(cudaMemcpy(static_cast<char*>(p->nq_segs) + size_t(nseg) * sizeof(int4), seg_j0.data(),
                         size_t(nseg) * sizeof(int), cudaMemcpyHostToDevice));
     const int64_t work = QP * npts * (sets + 1);
-    k_quad_coef<<<unsigned((work + 255) / 256), 256>>>(
-        dpts, npts, n, p->ap_reps, int(QP), p->ns, p->tab.M, static_cast<const float2*>(p->tab.ephase),
-        static_cast<const float2*>(p->tab.gphase), static_cast<const float*>(p->tab.gsinc), p->tab.gph_stride,
+    k_quad_coef<S><<<unsigned((work + 255) / 256), 256>>>(
+        dpts, npts, n, p->ap_reps, int(QP), p->ns, p->tab.M, static_cast<const c2<S>*>(p->tab.ephase),
+        static_cast<const c2<S>*>(p->tab.gphase), static_cast<const S*>(p->tab.gsinc), p->tab.gph_stride,
         p->tab.gs_stride, int(sets), T, Al, Be);
     const dim3 grid(unsigned((n2 + TM - 1) / TM), unsigned((NJ + TM - 1) / TM));
     for (int64_t s = 0; s < sets; ++s)
       for (int d = 0; d < 3; ++d) {
         const int64_t o = (s * 3 + d) * int64_t(NJ) * n2;
-        const float *al_s = Al + s * QP * npts, *be_s = Be + s * QP * npts;
+        const S *al_s = Al + s * QP * npts, *be_s = Be + s * QP * npts;
         const int *q1d = dq1 + d * NJ, *q2d = dq2 + d * NJ;
-        const float* wd = dw + d * NJ;
+        const S* wd = dw + d * NJ;
         // A~ = w (A(k, q) - B(k, -q)),  B~ = w (B(k, q) - A(k, -q))
-        k_quad_gemm<<<grid, 256>>>(T, al_s, be_s, q1d, q2d, wd, dki + d * n2, static_cast<float*>(p->nq_A) + o, NJ,
-                                   n2, int(QP), npts);
-        k_quad_gemm<<<grid, 256>>>(T, be_s, al_s, q1d, q2d, wd, dki + d * n2, static_cast<float*>(p->nq_B) + o, NJ,
-                                   n2, int(QP), npts);
+        k_quad_gemm<S><<<grid, 256>>>(T, al_s, be_s, q1d, q2d, wd, dki + d * n2, static_cast<S*>(p->nq_A) + o, NJ,
+                                      n2, int(QP), npts);
+        k_quad_gemm<S><<<grid, 256>>>(T, be_s, al_s, q1d, q2d, wd, dki + d * n2, static_cast<S*>(p->nq_B) + o, NJ,
+                                      n2, int(QP), npts);
       }
     const cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -601,6 +645,12 @@ int nyq_quad_prepare(pii_plan* p) {
   return PII_OK;
 }
 
+int nyq_quad_prepare(pii_plan* p) {
+  free_quad(p);
+  if (p->ap_count <= 0 || p->dim != 3) return PII_OK;
+  return p->precision == PII_PREC_FP32 ? quad_prepare_t<float>(p) : quad_prepare_t<double>(p);
+}
+
 void nyq_quad_release(pii_plan* p) { free_quad(p); }
 
 // the correction's partial sums (f^ only: it may run beside the gain kernels)
@@ -608,26 +658,24 @@ void nyq_quad_release(pii_plan* p) { free_quad(p); }
 // after s and after the gain sums' writes of G)
 int nyq_quad_run(pii_plan* p, int64_t cells, cudaStream_t s) { return nyq_quad_run2(p, cells, s, s, nullptr); }
 
-int nyq_quad_run2(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add, cudaEvent_t partial_done) {
+template <typename S>
+static int quad_run_t(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add, cudaEvent_t partial_done) {
   using namespace nqq;
-  if (!p->nq_A || p->nq_npts <= 0) {
-    set_error("nyq_quad_run: the plan has no quadratic-form kernels");
-    return PII_ERR_ARG;
-  }
+  using V = c2<S>;
   const int n = p->n, n2 = n * n;
-  const QuadCfg cfg = quad_cfg(n, int(p->tab.nsets));
+  const QuadCfg cfg = quad_cfg<S>(n, int(p->tab.nsets));
   int split = quad_split(p, cfg, cells);
   split = int(std::min<int64_t>(split, p->nq_qpart_units / std::max<int64_t>(cells, 1)));
   if (split < 1) {
     set_error("nyq_quad_run: %lld cells exceed the partial-sum buffer", (long long)cells);
     return PII_ERR_SIZE;
   }
-  QuadArgs a{};
-  a.A = static_cast<const float*>(p->nq_A);
-  a.B = static_cast<const float*>(p->nq_B);
-  a.fhat = static_cast<const float2*>(p->fhat);
-  a.fhT = static_cast<const float2*>(p->nq_fhT);
-  a.part = static_cast<float2*>(p->nq_qpart);
+  QuadArgs<S> a{};
+  a.A = static_cast<const S*>(p->nq_A);
+  a.B = static_cast<const S*>(p->nq_B);
+  a.fhat = static_cast<const V*>(p->fhat);
+  a.fhT = static_cast<const V*>(p->nq_fhT);
+  a.part = static_cast<V*>(p->nq_qpart);
   a.cells = cells;
   a.set_stride = p->tab.nsets > 1 ? int64_t(3) * p->nq_npts * n2 : 0;
   a.segs = static_cast<const int4*>(p->nq_segs);
@@ -637,15 +685,22 @@ int nyq_quad_run2(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add
   {
     StageTimer st(p, ST_NYQ, s);
     const int tb = (n + 31) / 32;
-    k_quad_prep<<<unsigned(cells * n * tb * tb), 256, 0, s>>>(a.fhat, static_cast<float2*>(p->nq_fhT), n, cells);
+    k_quad_prep<V><<<unsigned(cells * n * tb * tb), 256, 0, s>>>(a.fhat, static_cast<V*>(p->nq_fhT), n, cells);
     PII_CHECK_LAUNCH();
     const dim3 grid(unsigned(n / cfg.W), unsigned((cells + cfg.nc - 1) / cfg.nc), unsigned(3 * split));
-    if (cfg.nc == 4)
-      k_nyq_quad<4, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
-    else if (cfg.nc == 2)
-      k_nyq_quad<2, 512><<<grid, cfg.threads, cfg.smem, s>>>(a);
-    else
-      k_nyq_quad<1, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+    if constexpr (std::is_same<S, float>::value) {
+      if (cfg.nc == 4)
+        k_nyq_quad<S, 4, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+      else if (cfg.nc == 2)
+        k_nyq_quad<S, 2, 512><<<grid, cfg.threads, cfg.smem, s>>>(a);
+      else
+        k_nyq_quad<S, 1, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+    } else {
+      if (cfg.nc == 2)
+        k_nyq_quad<S, 2, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+      else
+        k_nyq_quad<S, 1, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
+    }
     PII_CHECK_LAUNCH();
   }
   if (partial_done) {
@@ -654,9 +709,18 @@ int nyq_quad_run2(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add
   }
   StageTimer st(p, ST_NYQ, s_add);
   const int64_t tot = cells * 3 * n2;
-  k_quad_add<<<unsigned((tot + 255) / 256), 256, 0, s_add>>>(a.part, static_cast<float2*>(p->G), n, cells, split);
+  k_quad_add<V><<<unsigned((tot + 255) / 256), 256, 0, s_add>>>(a.part, static_cast<V*>(p->G), n, cells, split);
   PII_CHECK_LAUNCH();
   return PII_OK;
+}
+
+int nyq_quad_run2(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add, cudaEvent_t partial_done) {
+  if (!p->nq_A || p->nq_npts <= 0) {
+    set_error("nyq_quad_run: the plan has no quadratic-form kernels");
+    return PII_ERR_ARG;
+  }
+  return p->precision == PII_PREC_FP32 ? quad_run_t<float>(p, cells, s, s_add, partial_done)
+                                       : quad_run_t<double>(p, cells, s, s_add, partial_done);
 }
 
 }  // namespace pii

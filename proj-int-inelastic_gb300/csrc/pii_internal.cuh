@@ -311,6 +311,12 @@ int nyq_quad_run2(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s_add
 // the Nyquist correction of the packed paths: the quadratic form where it was
 // built and chosen, else the direct kernel of the plan's n
 inline bool nyq_use_quad(const pii_plan* p) { return p->nyq_path == 0 && p->nq_A != nullptr; }
+// the packed column / plane pipeline with its Nyquist correction: FP32 (n !=
+// 32) with the direct kernels' buffers, FP64 with the quadratic form built
+inline bool packed_pipeline_ok(const pii_plan* p) {
+  if (p->ap_count <= 0 || p->dim != 3) return false;
+  return p->precision == PII_PREC_FP32 ? p->n != 32 && p->nq_part != nullptr : p->nq_A != nullptr;
+}
 // col_tc.cu: PII_ERR_STALL if a tensor-core DFT launch of an earlier call gave
 // up waiting (read from mapped host memory without a synchronisation; cleared
 // once reported)

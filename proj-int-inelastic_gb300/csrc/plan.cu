@@ -470,12 +470,14 @@ static int create(pii_plan** out, int dim, int n, int nr, int ns, const double* 
   // memory budget (3.4x to 9x faster than the direct kernels), else the direct
   // kernels
   p->nyq_path = 1;
-  if (precision == PII_PREC_FP32 && dim == 3 && p->ap_count > 0) {
+  if (dim == 3 && p->ap_count > 0) {
     if ((s2 = nyq_quad_prepare(p)) != PII_OK) {
       free_plan(p);
       return s2;
     }
     if (p->nq_A) p->nyq_path = 0;
+    // FP64: the packed pipeline (half the passes) wherever its correction is built
+    if (precision != PII_PREC_FP32 && p->nq_A) p->gain_path = 3;
   }
   *out = p;
   return PII_OK;
@@ -532,7 +534,11 @@ int pii_plan_set_restitution(pii_plan* plan, const double* e, const double* e0, 
   if (plan->dft_img) PII_TRY(col_tc_gain_tables(plan));  // the tensor-core path's sinc slices
   if (plan->nq_A) {  // A, B per set, rebuilt for the new sets (or dropped beyond the budget)
     PII_TRY(nyq_quad_prepare(plan));
-    if (!plan->nq_A) plan->nyq_path = 1;
+    if (!plan->nq_A) {
+      plan->nyq_path = 1;
+      // FP64 has no direct correction: back to the unpacked pipeline
+      if (plan->precision != PII_PREC_FP32 && plan->gain_path == 3) plan->gain_path = 0;
+    }
   }
   graphs_clear(plan);  // captured graphs baked the old tables in
   return PII_OK;

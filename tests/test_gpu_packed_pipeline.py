@@ -150,10 +150,12 @@ def test_fused_path_rules():
     assert col.plan.tuning["gain_path"] == "fused"
 
 
+@pytest.mark.parametrize("nyq", ["quadratic", "direct"])
 @pytest.mark.parametrize("n,nr", [(48, 3), (64, 2)])
-def test_fused_split_with_pipeline(n, nr):
+def test_fused_split_with_pipeline(n, nr, nyq):
     """The fused path with a share of the cells on the packed pipeline (side
-    stream, on the SMs the fused kernel's clusters leave idle): every cell
+    stream, on the SMs the fused kernel's clusters leave idle; the
+    quadratic-form correction's partial sums on that stream too): every cell
     against the FP64 plan, and against the unsplit fused kernel."""
     import proj_int_inelastic_gb300 as pkg
 
@@ -166,6 +168,7 @@ def test_fused_split_with_pipeline(n, nr):
     ft = torch.as_tensor(f, device="cuda:0")
     col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", batch_max=5)
     col.plan.set_tuning("fused", 6, 65536)
+    col.plan.set_nyquist_path(nyq)
     assert col.plan.tuning["fused_split"] == 0.0
     q0 = col.collide(ft, with_loss=True).cpu().numpy()
     col.plan.set_tuning("fused", 6, 65536, fused_split=0.4)  # the last 2 of 5 cells on the pipeline
@@ -204,3 +207,40 @@ def test_fused_split_in_captured_graph():
     torch.cuda.synchronize()
     for i in range(4):
         assert torch.equal(graph.f[i], eager.f[i]), i
+
+
+@pytest.mark.parametrize("n,nr,ns", [(8, 4, 6), (16, 4, 12), (32, 3, 6), (48, 2, 6)])
+def test_fp64_packed_pipeline(n, nr, ns):
+    """FP64 plans on a symmetric design default to the packed pipeline with
+    the FP64 quadratic-form Nyquist correction: against the unpacked FP64
+    pipeline and the oracle at 1e-12, with one restitution set per cell."""
+    import proj_int_inelastic_gb300 as pkg
+    from oracle import fs_inelastic as fo
+
+    cfg = op_config(n, L8_S, nr, ns, 0.6, 0.9, 1.0)
+    sm = pkg.SpectralMesh(cfg)
+    v = sm.v_center
+    rng = np.random.default_rng(n + 7)
+    f = np.stack([maxwellian(v, 1.0, (0.7, -0.4, 0.2), 1.1) + maxwellian(v, 0.6, (-1.2, 0.5, 0.3), 0.7),
+                  rng.uniform(0.1, 1.0, (n, n, n)) * 0.05])
+    ft = torch.as_tensor(f, device="cuda:0")
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="double", batch_max=2)
+    assert col.plan.tuning["gain_path"] == "packed"
+    assert col.plan.nyquist_path == "quadratic"
+    with pytest.raises(ValueError):
+        col.plan.set_nyquist_path("direct")  # FP32 kernels only
+    qp = col.collide(ft, with_loss=True).cpu().numpy()
+    col.plan.set_tuning("pipeline", 6, 131072)
+    qu = col.collide(ft, with_loss=True).cpu().numpy()
+    op = fo.FSInelasticVHS(fo.Mesh(n, L8_S, nr, ns), 0.6, 0.9, 1.0)
+    for c in range(2):
+        ref = op.collide_cell(f[c], with_loss=True)
+        assert rel_linf(qp[c], qu[c]) < 1e-12 and rel_linf(qp[c], ref) < 1e-12, c
+    # one restitution set per cell: the correction's kernels are rebuilt per set
+    es, e0s = [0.5, 0.95], [0.8, 0.7]
+    col.plan.set_tuning("packed", 6, 131072)
+    col.plan.set_restitution(es, e0s)
+    qs = col.collide(ft, with_loss=True).cpu().numpy()
+    for c in range(2):
+        ref = fo.FSInelasticVHS(fo.Mesh(n, L8_S, nr, ns), es[c], e0s[c], 1.0).collide_cell(f[c], with_loss=True)
+        assert rel_linf(qs[c], ref) < 1e-12, c
