@@ -109,18 +109,21 @@ int pii_plan_destroy(pii_plan* plan);
 int64_t pii_plan_workspace_bytes(const pii_plan* plan);
 
 /*
- * Kernel choice for the gain term of FP32 3D plans (tuning knob, no reference
- * counterpart).  n = 32: 3 = the fused a-parity kernel on antipodal direction
- * pairs (sigma, -sigma packed into one real-phase pass) plus the exact
- * Nyquist-plane correction (the default where the design is antipodally
- * symmetric), 2 = the fused a-parity kernel with its accumulator in tensor
- * memory, 1 = the fused 2-CTA-cluster kernel.  n = 16, 24, 48, 64: 4 = the
- * fused kernel (one work item per CTA, or per cluster of 8 / 16 CTAs at
- * n = 48 / 64, exchanging through distributed shared memory, the gain sum in
- * tensor memory; packed with the Nyquist correction where the design is
- * antipodally symmetric; the default at n = 16, 24, 48), 3 = the packed
- * column / plane pipeline.  0 = the column / plane pipeline on (cell, pair)
- * items, every size and FP64.  All compute the same operator.
+ * Kernel choice for the gain term of 3D plans (tuning knob, no reference
+ * counterpart).  FP32, n = 32: 3 = the fused a-parity kernel on antipodal
+ * direction pairs (sigma, -sigma packed into one real-phase pass) plus the
+ * exact Nyquist-plane correction (the default where the design is
+ * antipodally symmetric), 2 = the fused a-parity kernel with its accumulator
+ * in tensor memory, 1 = the fused 2-CTA-cluster kernel.  FP32, n = 16, 24,
+ * 48, 64: 4 = the fused kernel (one work item per CTA, or per cluster of
+ * 6 / 16 CTAs at n = 48 / 64, exchanging through distributed shared memory,
+ * the gain sum in tensor memory; packed with the Nyquist correction where the
+ * design is antipodally symmetric; the default at n = 16, 24, 48), 3 = the
+ * packed column / plane pipeline.  FP64, every n: 3 = the packed pipeline
+ * with the FP64 quadratic-form Nyquist correction (the default on an
+ * antipodally symmetric design where that correction fits the memory
+ * budget).  0 = the column / plane pipeline on (cell, pair) items, every size
+ * and precision.  All compute the same operator.
  */
 int pii_plan_set_gain_path(pii_plan* plan, int path);
 
@@ -171,11 +174,12 @@ double pii_plan_get_fused_split(const pii_plan* plan);
  * counterpart: the packing is this library's): 0 = the quadratic form
  * C(k) = sum_q A(k, q) f^(q) f^(k - q) - B(k, q) conj f^(q) f^(k + q) with the
  * kernels A, B (N x N real, N = 3 n^2 - 3 n + 1 Nyquist points) precomputed
- * once per plan and restitution set, 1 = the direct per-pass kernels.  FP32
- * 3D plans on an antipodally symmetric design, n a multiple of 8 up to 64;
- * the default is 0 where A, B (2 x 3 N n^2 floats per set) fit the memory
- * budget, else 1.  set drops captured step graphs (path 0 builds A, B on
- * request); get returns the path in use (-1 for NULL).
+ * once per plan and restitution set, 1 = the direct per-pass kernels (FP32
+ * only).  3D plans on an antipodally symmetric design, n a multiple of 8 up
+ * to 64, A and B in the plan's precision; the default is 0 where A, B
+ * (2 x 3 N n^2 values per set) fit the memory budget, else 1 (FP64: the
+ * unpacked pipeline instead).  set drops captured step graphs (path 0 builds
+ * A, B on request); get returns the path in use (-1 for NULL).
  */
 int pii_plan_set_nyquist_path(pii_plan* plan, int path);
 int pii_plan_get_nyquist_path(const pii_plan* plan);
