@@ -417,13 +417,14 @@ struct QuadCfg {
   size_t smem;
 };
 
-// FP32: 4 cells per CTA up to n = 32, else 2; FP64 (twice the shared memory
+// FP32: 2 cells per CTA (4 at n = 32 hold 253 registers, 8 warps per SM:
+// 0.948 against 0.906 ms per 128-cell step); FP64 (twice the shared memory
 // and registers per value): 2 up to n = 48, else 1; one with a set per cell
 template <typename S>
 static QuadCfg quad_cfg(int n, int nsets) {
   constexpr bool f64 = std::is_same<S, double>::value;
   QuadCfg c{};
-  c.nc = nsets > 1 ? 1 : f64 ? (n <= 48 ? 2 : 1) : (n <= 32 ? 4 : 2);
+  c.nc = nsets > 1 ? 1 : f64 ? (n <= 48 ? 2 : 1) : 2;
   c.W = n == 32 || n == 48 ? 16 : n;
   if (n == 64) c.W = c.nc == 1 ? 16 : 32;  // 256 or 512 threads
   c.threads = n * c.W / nqq::R;
@@ -441,7 +442,6 @@ static int quad_occupancy(const QuadCfg& c, int* per_sm) {
 template <typename S>
 static int quad_kernel_setup(const QuadCfg& c, int* per_sm) {
   if constexpr (std::is_same<S, float>::value) {
-    if (c.nc == 4) return quad_occupancy<S, 4, 256>(c, per_sm);
     if (c.nc == 2) return quad_occupancy<S, 2, 512>(c, per_sm);
     return quad_occupancy<S, 1, 256>(c, per_sm);
   } else {
@@ -689,9 +689,7 @@ static int quad_run_t(pii_plan* p, int64_t cells, cudaStream_t s, cudaStream_t s
     PII_CHECK_LAUNCH();
     const dim3 grid(unsigned(n / cfg.W), unsigned((cells + cfg.nc - 1) / cfg.nc), unsigned(3 * split));
     if constexpr (std::is_same<S, float>::value) {
-      if (cfg.nc == 4)
-        k_nyq_quad<S, 4, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
-      else if (cfg.nc == 2)
+      if (cfg.nc == 2)
         k_nyq_quad<S, 2, 512><<<grid, cfg.threads, cfg.smem, s>>>(a);
       else
         k_nyq_quad<S, 1, 256><<<grid, cfg.threads, cfg.smem, s>>>(a);
