@@ -558,20 +558,22 @@ def run_reference(args):
     return 0
 
 
-def ncu_case(cells):
-    """Small profiling case: 3 mixed-precision Q(f,f) evaluations on `cells` cells."""
+def ncu_case(cells, precision="mixed"):
+    """Small profiling case: 3 Q(f,f) evaluations on `cells` cells of the
+    workload, in mixed precision or (precision "double") in FP64."""
     import torch
 
     import proj_int_inelastic_gb300 as pkg
 
     cfg = op_config()
     sm = pkg.SpectralMesh(cfg)
-    col = pkg.FSInelasticVHSCollision(cfg, sm, precision="mixed", with_loss=True, batch_max=cells)
+    col = pkg.FSInelasticVHSCollision(cfg, sm, precision=precision, with_loss=True, batch_max=cells)
     f = torch.as_tensor(sod_state(sm.v_center)[:cells], device="cuda:0").contiguous()
     for _ in range(3):
         q = col.collide(f, with_loss=True)
     torch.cuda.synchronize()
-    print(json.dumps({"ncu_case_cells": cells, "q_abs_max": float(q.abs().max())}))
+    print(json.dumps({"ncu_case_cells": cells, "precision": precision, "tuning": col.plan.tuning,
+                      "q_abs_max": float(q.abs().max())}))
     return 0
 
 
@@ -644,6 +646,8 @@ def main():
     ap.add_argument("--c3-only", action="store_true", help="measure only the ensemble configuration and exit")
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: run 3 Q(f,f) evaluations on this many cells of the workload and exit")
+    ap.add_argument("--ncu-precision", default="mixed", choices=["mixed", "double"],
+                    help="precision of the --ncu-case evaluations")
     ap.add_argument("--ncu-class", type=int, default=0,
                     help="profiling case: one ensemble size class n^3 (with --ncu-cells cells) and exit")
     ap.add_argument("--ncu-cells", type=int, default=4)
@@ -657,7 +661,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.ncu_case:
-        return ncu_case(args.ncu_case)
+        return ncu_case(args.ncu_case, args.ncu_precision)
     if args.ncu_class:
         return ncu_case_class(args.ncu_class, args.ncu_cells)
     if args.ncu_case64:
