@@ -185,7 +185,8 @@ def test_fused_split_with_pipeline(n, nr, nyq):
 
 def test_fused_split_in_captured_graph():
     """The split's fork onto the plan's side stream and join back are captured
-    into the macro-step graph: graph replay and eager steps agree bit for bit."""
+    into the macro-step graph: graph replay and eager steps agree bit for bit,
+    and with one restitution set per instance both match the FP64 ensemble."""
     import proj_int_inelastic_gb300 as pkg
 
     rng = np.random.default_rng(48)
@@ -198,15 +199,19 @@ def test_fused_split_in_captured_graph():
     kw = dict(dt=0.02, kn=1.0, integrator="PFE", inner_steps=[2], inner_dt=[0.005], with_loss=True)
     graph = pkg.Ensemble(configs, f0s, precision="mixed", **kw)
     eager = pkg.Ensemble(configs, f0s, precision="mixed", **kw)
+    dbl = pkg.Ensemble(configs, f0s, precision="double", **kw)
     for ens in (graph, eager):
         for op, _, _ in ens._classes:
-            op.plan.set_tuning("fused", 6, 65536, fused_split=0.25)
+            op.plan.set_tuning("fused", 6, 65536, fused_split=0.25)  # the last instance on the pipeline
     for _ in range(2):
         graph.step()
         eager.step(use_graph=False)
+        dbl.step(use_graph=False)
     torch.cuda.synchronize()
     for i in range(4):
         assert torch.equal(graph.f[i], eager.f[i]), i
+        # one restitution set per instance, on both sides of the split
+        assert rel_linf(graph.f[i].cpu().numpy(), dbl.f[i].cpu().numpy()) < 1e-5, i
 
 
 @pytest.mark.parametrize("n,nr,ns", [(8, 4, 6), (16, 4, 12), (32, 3, 6), (48, 2, 6)])
