@@ -14,7 +14,9 @@
 // stores its line straight into the owning CTA's shared memory with st.async,
 // which counts the bytes on the receiver's mbarrier: a column's n values go to
 // the n / NPL plane owners, a plane column's n values to the column owners,
-// 256 contiguous bytes per warp store.  A CTA waits (bounded) for its
+// 256 contiguous bytes per warp store; the CTA's own share goes by plain
+// shared-memory stores (the cluster path runs at ~16 B/clk per SM, and the
+// exchanges' stores were a third of the kernel's time at n = 48).  A CTA waits (bounded) for its
 // mbarrier to see all N3 / CS elements of an exchange; a cluster barrier
 // arrived on right after a buffer's last read (split arrive / wait, so the
 // transform that follows hides it) keeps the next exchange from overwriting
@@ -211,8 +213,11 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     tm_relinquish();
   }
   if (CS > 1 && t == 0) {
-    mbar_init(&bars[0], 1);  // stage-A exchange: its thread 0 arrives with the expected bytes
-    mbar_init(&bars[1], 1);  // stage-B exchange
+    // an exchange's barrier completes when the other CTAs' bytes have landed
+    // (thread 0 arrives with their count) and every thread has arrived after
+    // its plain stores into the CTA's own buffer
+    mbar_init(&bars[0], G::THREADS + 1);  // stage-A exchange
+    mbar_init(&bars[1], G::THREADS + 1);  // stage-B exchange
   }
   tm_fence_before();
   __syncthreads();
@@ -237,7 +242,9 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
   const int mbc = kb * kb + kc * kc;
   const uint32_t buf_s = static_cast<uint32_t>(__cvta_generic_to_shared(buf));
   const uint32_t bar_s = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
-  constexpr uint32_t XBYTES = uint32_t(N3 / CS) * 8;  // bytes one CTA receives per exchange
+  // bytes one CTA receives from the other CTAs per exchange (its own share it
+  // stores itself)
+  constexpr uint32_t XBYTES = uint32_t(N3 / CS) * 8 / CS * (CS - 1);
   uint32_t phase = 0;
   bool gave_up = false;
   // the first wait (before the first exchange) also makes sure that every CTA
@@ -365,14 +372,24 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
     if constexpr (CS > 1) {
       fz_wait();  // every buffer of the cluster has been read by the previous item's stage C
       if (t == 0 && !a.withhold) mbar_arrive_tx(&bars[0], XBYTES);
-      if (!a.withhold) static_for<0, CS>([&](auto ri) {
-        constexpr int r = decltype(ri)::value;
-        const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s, uint32_t(r));
-        static_for<0, NPL>([&](auto mi) {
-          constexpr int m = decltype(mi)::value;
-          fz_st_async(base + uint32_t(((m * NV + jb) * LD + jc) * 8), x[pos(NV, r * NPL + m)], rb);
+      if (!a.withhold) {
+        static_for<0, CS>([&](auto ri) {
+          constexpr int r = decltype(ri)::value;
+          if (r == rank) {  // the CTA's own planes: plain stores
+            static_for<0, NPL>([&](auto mi) {
+              constexpr int m = decltype(mi)::value;
+              buf[(m * NV + jb) * LD + jc] = x[pos(NV, r * NPL + m)];
+            });
+          } else {
+            const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s, uint32_t(r));
+            static_for<0, NPL>([&](auto mi) {
+              constexpr int m = decltype(mi)::value;
+              fz_st_async(base + uint32_t(((m * NV + jb) * LD + jc) * 8), x[pos(NV, r * NPL + m)], rb);
+            });
+          }
         });
-      });
+        mbar_arrive(&bars[0]);  // release: this thread's own-plane stores
+      }
       // the planes of the CTA are complete once every CTA's elements have landed
       if (!fz_wait_bar(&bars[0], phase, a.wait_limit)) gave_up = true;
     } else {
@@ -479,14 +496,24 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
         const int ag = rank * NPL + pl;  // the plane's a
         fz_wait();                       // every CTA has read its planes
         if (t == 0 && !a.withhold) mbar_arrive_tx(&bars[1], XBYTES);
-        if (!a.withhold) static_for<0, CS>([&](auto ri) {
-          constexpr int r = decltype(ri)::value;
-          const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s + 8, uint32_t(r));
-          static_for<0, NPL>([&](auto mi) {
-            constexpr int m = decltype(mi)::value;
-            fz_st_async(base + uint32_t((ag * NCOL + m * NV + l) * 8), x[pos(NV, r * NPL + m)], rb);
+        if (!a.withhold) {
+          static_for<0, CS>([&](auto ri) {
+            constexpr int r = decltype(ri)::value;
+            if (r == rank) {  // the CTA's own columns: plain stores
+              static_for<0, NPL>([&](auto mi) {
+                constexpr int m = decltype(mi)::value;
+                buf[ag * NCOL + m * NV + l] = x[pos(NV, r * NPL + m)];
+              });
+            } else {
+              const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s + 8, uint32_t(r));
+              static_for<0, NPL>([&](auto mi) {
+                constexpr int m = decltype(mi)::value;
+                fz_st_async(base + uint32_t((ag * NCOL + m * NV + l) * 8), x[pos(NV, r * NPL + m)], rb);
+              });
+            }
           });
-        });
+          mbar_arrive(&bars[1]);  // release: this thread's own-column stores
+        }
         if (!fz_wait_bar(&bars[1], phase, a.wait_limit)) gave_up = true;  // the CTA's columns have landed
         phase ^= 1;
       } else {
