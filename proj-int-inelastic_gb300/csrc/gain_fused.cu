@@ -16,8 +16,9 @@
 // the n / NPL plane owners, a plane column's n values to the column owners,
 // 256 contiguous bytes per warp store; the CTA's own share goes by plain
 // shared-memory stores (the cluster path runs at ~16 B/clk per SM, and the
-// exchanges' stores were a third of the kernel's time at n = 48).  A CTA waits (bounded) for its
-// mbarrier to see all N3 / CS elements of an exchange; a cluster barrier
+// exchanges' stores were a third of the kernel's time at n = 48).  A CTA
+// waits (bounded) for its mbarrier to see the other CTAs' bytes of an
+// exchange and every own thread's arrival after its plain stores; a cluster barrier
 // arrived on right after a buffer's last read (split arrive / wait, so the
 // transform that follows hides it) keeps the next exchange from overwriting
 // a buffer still being read.  The phase and gain rows of a pass and the sinc
