@@ -140,6 +140,7 @@ struct Geo {
   static constexpr int SMW = WARPS - FW0 < SMW_FIT ? WARPS - FW0 : SMW_FIT;
   static constexpr size_t SMEM = FSM_OFF + size_t(SMW) * 32 * NV * sizeof(float2);
   static_assert(THREADS % 32 == 0 && NV % CS == 0 && TCOLS_F <= 512 && (2 * NV) % 16 == 0, "launch shape");
+  static_assert(CS == 1 || (NPL % 2 == 0 && LD % 2 == 0 && NCOL % 2 == 0 && NV % 2 == 0), "16-byte exchange pairs");
   static_assert(SMEM <= SMEM_MAX && FSM_OFF <= SMEM_MAX, "shared memory of one CTA");
 };
 }  // namespace gfu
@@ -169,6 +170,21 @@ __device__ __forceinline__ uint32_t fz_map(uint32_t addr, uint32_t rank) {
   uint32_t r;
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
   return r;
+}
+__device__ __forceinline__ void fz_st_async4(uint32_t addr, float4 v, uint32_t mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(addr),
+               "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ float2 fz_xor1(float2 v) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, 1), __shfl_xor_sync(0xffffffffu, v.y, 1));
+}
+// a lane pair (columns c, c + 1 of one line set) turns its values of two
+// planes m, m + 1 into one 16-byte pair per lane: the even lane takes plane
+// m, the odd lane plane m + 1; returns the pair and sets (m, first column)
+__device__ __forceinline__ float4 fz_pair(float2 a0, float2 a1, bool odd) {
+  const float2 w = fz_xor1(odd ? a0 : a1);
+  return odd ? make_float4(w.x, w.y, a1.x, a1.y) : make_float4(a0.x, a0.y, w.x, w.y);
 }
 __device__ __forceinline__ void fz_st_async(uint32_t addr, float2 v, uint32_t mbar) {
   asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
@@ -374,20 +390,21 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
       fz_wait();  // every buffer of the cluster has been read by the previous item's stage C
       if (t == 0 && !a.withhold) mbar_arrive_tx(&bars[0], XBYTES);
       if (!a.withhold) {
+        // 16 bytes per store: lanes of columns (jc, jc + 1) pair up their
+        // values of planes (m, m + 1)
+        const bool odd = (jc & 1) != 0;
         static_for<0, CS>([&](auto ri) {
           constexpr int r = decltype(ri)::value;
-          if (r == rank) {  // the CTA's own planes: plain stores
-            static_for<0, NPL>([&](auto mi) {
-              constexpr int m = decltype(mi)::value;
-              buf[(m * NV + jb) * LD + jc] = x[pos(NV, r * NPL + m)];
-            });
-          } else {
-            const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s, uint32_t(r));
-            static_for<0, NPL>([&](auto mi) {
-              constexpr int m = decltype(mi)::value;
-              fz_st_async(base + uint32_t(((m * NV + jb) * LD + jc) * 8), x[pos(NV, r * NPL + m)], rb);
-            });
-          }
+          const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s, uint32_t(r));
+          static_for<0, NPL / 2>([&](auto mi) {
+            constexpr int m0 = 2 * decltype(mi)::value;
+            const float4 v = fz_pair(x[pos(NV, r * NPL + m0)], x[pos(NV, r * NPL + m0 + 1)], odd);
+            const int e = ((m0 + (odd ? 1 : 0)) * NV + jb) * LD + (jc & ~1);
+            if (r == rank)  // the CTA's own planes: plain stores
+              *reinterpret_cast<float4*>(buf + e) = v;
+            else
+              fz_st_async4(base + uint32_t(e * 8), v, rb);
+          });
         });
         mbar_arrive(&bars[0]);  // release: this thread's own-plane stores
       }
@@ -498,20 +515,19 @@ __global__ void __launch_bounds__(gfu::Geo<NV>::THREADS, 1) k_gain_fused(FusedAr
         fz_wait();                       // every CTA has read its planes
         if (t == 0 && !a.withhold) mbar_arrive_tx(&bars[1], XBYTES);
         if (!a.withhold) {
+          const bool odd = (l & 1) != 0;
           static_for<0, CS>([&](auto ri) {
             constexpr int r = decltype(ri)::value;
-            if (r == rank) {  // the CTA's own columns: plain stores
-              static_for<0, NPL>([&](auto mi) {
-                constexpr int m = decltype(mi)::value;
-                buf[ag * NCOL + m * NV + l] = x[pos(NV, r * NPL + m)];
-              });
-            } else {
-              const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s + 8, uint32_t(r));
-              static_for<0, NPL>([&](auto mi) {
-                constexpr int m = decltype(mi)::value;
-                fz_st_async(base + uint32_t((ag * NCOL + m * NV + l) * 8), x[pos(NV, r * NPL + m)], rb);
-              });
-            }
+            const uint32_t base = fz_map(buf_s, uint32_t(r)), rb = fz_map(bar_s + 8, uint32_t(r));
+            static_for<0, NPL / 2>([&](auto mi) {
+              constexpr int m0 = 2 * decltype(mi)::value;
+              const float4 v = fz_pair(x[pos(NV, r * NPL + m0)], x[pos(NV, r * NPL + m0 + 1)], odd);
+              const int e = ag * NCOL + (m0 + (odd ? 1 : 0)) * NV + (l & ~1);
+              if (r == rank)  // the CTA's own columns: plain stores
+                *reinterpret_cast<float4*>(buf + e) = v;
+              else
+                fz_st_async4(base + uint32_t(e * 8), v, rb);
+            });
           });
           mbar_arrive(&bars[1]);  // release: this thread's own-column stores
         }
