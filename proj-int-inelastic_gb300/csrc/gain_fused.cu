@@ -179,17 +179,12 @@ __device__ __forceinline__ void fz_st_async4(uint32_t addr, float4 v, uint32_t m
 __device__ __forceinline__ float2 fz_xor1(float2 v) {
   return make_float2(__shfl_xor_sync(0xffffffffu, v.x, 1), __shfl_xor_sync(0xffffffffu, v.y, 1));
 }
-// a lane pair (columns c, c + 1 of one line set) turns its values of two
-// planes m, m + 1 into one 16-byte pair per lane: the even lane takes plane
-// m, the odd lane plane m + 1; returns the pair and sets (m, first column)
+// a lane pair (columns c, c + 1 of one line set, c even) turns its values
+// a0, a1 of two planes m, m + 1 into one 16-byte pair per lane: the even lane
+// returns plane m's elements at columns (c, c + 1), the odd lane plane m + 1's
 __device__ __forceinline__ float4 fz_pair(float2 a0, float2 a1, bool odd) {
   const float2 w = fz_xor1(odd ? a0 : a1);
   return odd ? make_float4(w.x, w.y, a1.x, a1.y) : make_float4(a0.x, a0.y, w.x, w.y);
-}
-__device__ __forceinline__ void fz_st_async(uint32_t addr, float2 v, uint32_t mbar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
-               "f"(v.x), "f"(v.y), "r"(mbar)
-               : "memory");
 }
 // waits (bounded) for phase `parity` of a barrier whose bytes other CTAs deliver
 __device__ __forceinline__ bool fz_wait_bar(uint64_t* mbar, uint32_t parity, uint32_t limit) {
